@@ -1,0 +1,68 @@
+// Philox4x32-10 counter-based generator (Salmon, Moraes, Dror, Shaw,
+// "Parallel random numbers: as easy as 1, 2, 3", SC'11) and the thermal-field
+// Gaussian draws built on it.
+//
+// Stream definition (shared by every solver form, so FP32 and FP64 runs see
+// the same noise up to rounding): for a layer with key (seed_lo, seed_hi) at
+// absolute step s, one Philox block with counter {s_lo, s_hi, 0x7E4D, 0}
+// gives four words w0..w3; u_k = (w_k + 0.5) * 2^-32 lies in (0, 1); the
+// Box-Muller transform gives g0, g1 from (u0, u1) and g2 from (u2, u3).
+#pragma once
+#include <stdint.h>
+
+#define CMTJ_PHILOX_M0 0xD2511F53u
+#define CMTJ_PHILOX_M1 0xCD9E8D57u
+#define CMTJ_PHILOX_W0 0x9E3779B9u
+#define CMTJ_PHILOX_W1 0xBB67AE85u
+#define CMTJ_THERMAL_TAG 0x7E4Du
+
+__device__ __forceinline__ uint4 cmtj_philox4x32_10(uint4 c, uint32_t k0, uint32_t k1) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    const uint32_t hi0 = __umulhi(CMTJ_PHILOX_M0, c.x), lo0 = CMTJ_PHILOX_M0 * c.x;
+    const uint32_t hi1 = __umulhi(CMTJ_PHILOX_M1, c.z), lo1 = CMTJ_PHILOX_M1 * c.z;
+    c = make_uint4(hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0);
+    k0 += CMTJ_PHILOX_W0;
+    k1 += CMTJ_PHILOX_W1;
+  }
+  return c;
+}
+
+__device__ __forceinline__ uint4 cmtj_thermal_words(uint32_t seed_lo, uint32_t seed_hi, uint64_t step) {
+  return cmtj_philox4x32_10(make_uint4((uint32_t)step, (uint32_t)(step >> 32), CMTJ_THERMAL_TAG, 0u),
+                            seed_lo, seed_hi);
+}
+
+// FP64 draws (plain form).
+__device__ __forceinline__ void cmtj_gaussian3_f64(uint32_t seed_lo, uint32_t seed_hi, uint64_t step,
+                                                   double &g0, double &g1, double &g2) {
+  const uint4 w = cmtj_thermal_words(seed_lo, seed_hi, step);
+  const double s = 2.3283064365386963e-10;  // 2^-32
+  const double u0 = ((double)w.x + 0.5) * s, u1 = ((double)w.y + 0.5) * s;
+  const double u2 = ((double)w.z + 0.5) * s, u3 = ((double)w.w + 0.5) * s;
+  const double r0 = sqrt(-2.0 * log(u0)), r1 = sqrt(-2.0 * log(u2));
+  const double a0 = 6.283185307179586 * u1, a1 = 6.283185307179586 * u3;
+  g0 = r0 * cos(a0);
+  g1 = r0 * sin(a0);
+  g2 = r1 * cos(a1);
+}
+
+// FP32 draws (batched form): the same words, transformed in single precision.
+__device__ __forceinline__ void cmtj_gaussian3_f32(uint32_t seed_lo, uint32_t seed_hi, uint64_t step,
+                                                   float &g0, float &g1, float &g2) {
+  const uint4 w = cmtj_thermal_words(seed_lo, seed_hi, step);
+  const float s = 2.3283064365386963e-10f;
+  const float u0 = ((float)w.x + 0.5f) * s, u1 = ((float)w.y + 0.5f) * s;
+  const float u2 = ((float)w.z + 0.5f) * s, u3 = ((float)w.w + 0.5f) * s;
+  // (float)w rounds to 24 bits, so u may round to exactly 1.0 (r = 0);
+  // logf keeps -2 log(u) >= 0 near u = 1, where __logf's absolute error
+  // could turn it negative.
+  const float r0 = sqrtf(-2.0f * logf(u0));
+  const float r1 = sqrtf(-2.0f * logf(u2));
+  float s0, c0, s1, c1;
+  sincospif(2.0f * u1, &s0, &c0);
+  sincospif(2.0f * u3, &s1, &c1);
+  g0 = r0 * c0;
+  g1 = r0 * s0;
+  g2 = r1 * c1;
+}

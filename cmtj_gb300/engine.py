@@ -1,0 +1,80 @@
+"""GPU execution of lowered junctions through libcmtj_gpu.so.
+
+Device memory and streams come from PyTorch; the compute is the library's
+CUDA kernels.  There is no CPU path: without a CUDA device or without the
+built library every entry point raises.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _abi
+from ._lower import RunPlan, apply_results, lower, plan_run  # noqa: F401
+
+_torch = None
+
+
+def torch():
+    global _torch
+    if _torch is None:
+        import torch as t
+        _torch = t
+    return _torch
+
+
+def require_gpu():
+    t = torch()
+    if not t.cuda.is_available():
+        raise RuntimeError("cmtj_gb300 runs on a CUDA GPU (sm_103a); no CUDA device is available")
+    return _abi.load()
+
+
+def to_device(arr):
+    """numpy array -> device tensor holding the same bytes."""
+    t = torch()
+    flat = np.ascontiguousarray(arr).view(np.uint8).reshape(-1)
+    return t.from_numpy(flat.copy()).to("cuda", non_blocking=False)
+
+
+def ptr(tensor):
+    return ctypes.c_void_p(tensor.data_ptr()) if tensor is not None else None
+
+
+def stream_ptr(stream=None):
+    t = torch()
+    s = stream if stream is not None else t.cuda.current_stream()
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+def run_lowered_f64(lowered, stream=None):
+    """Run a lowered batch on the FP64 plain form; returns host arrays
+    (log [n][n_log][width], status [n*2], updated layers)."""
+    lib = require_gpu()
+    t = torch()
+    n = len(lowered.junctions)
+    p = lowered.params
+    n_log = int(p["n_log"][0])
+    width = lowered.log_width
+    d_j = to_device(lowered.junctions)
+    d_l = to_device(lowered.layers)
+    d_tab = to_device(lowered.tables) if lowered.tables is not None else None
+    d_log = t.empty((n, max(n_log, 1), width), dtype=t.float64, device="cuda")
+    d_status = t.zeros(2 * n, dtype=t.int32, device="cuda")
+    rc = lib.cmtj_run_simulation_f64(ptr(d_j), n, ptr(d_l), ptr(d_tab), p.ctypes.data, ptr(d_log), ptr(d_status),
+                                     stream_ptr(stream))
+    _abi.check(rc, lib)
+    log = d_log.cpu().numpy()
+    status = d_status.cpu().numpy().view(np.uint32)
+    layers = d_l.cpu().numpy().view(_abi.LAYER_DTYPE).copy()
+    return log, status, layers
+
+
+def run_junctions(junctions, plan, solver, calculate_energies=False):
+    """Junction::runSimulation for a list of junctions sharing one plan
+    (each junction keeps its own layers, drivers and log)."""
+    lowered = lower(junctions, plan, solver, calculate_energies)
+    require_gpu()
+    log, status, layers = run_lowered_f64(lowered)
+    lowered.layers = layers
+    apply_results(junctions, lowered, log, status, plan)
+    return lowered

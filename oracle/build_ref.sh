@@ -1,0 +1,43 @@
+#!/usr/bin/env bash
+# Build the reference cmtj extension (_cmtj) from its own sources, in place,
+# into oracle/_ref/.  The product never loads this: it is the checker that
+# pins the C++ restatement in oracle/ and generates tests/golden/ fixtures.
+#
+# Reads:   $CMTJ_REF (default /root/reference): python/cmtj.cpp + core/*.hpp
+# Writes:  oracle/_ref/_cmtj<ext-suffix>, oracle/_ref/cmtj/__init__.py (shim)
+#
+# Flags follow setup.py:51-88 on Linux (C++17, -fvisibility=hidden,
+# -Wno-unused-variable) at -O3, plus -ffp-contract=off so that no compiler
+# fuses a*b+c into an FMA (x86-64 baseline has no FMA; aarch64 does, and GCC
+# contracts by default there).  The kissfft submodule is not vendored, so the
+# project-written stand-in header under oracle/stubs/ satisfies noise.hpp.
+set -euo pipefail
+HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
+REF="${CMTJ_REF:-/root/reference}"
+OUT="$HERE/_ref"
+if [ ! -f "$REF/python/cmtj.cpp" ]; then
+  echo "reference sources not found at $REF; skipping _cmtj build" >&2
+  exit 0
+fi
+mkdir -p "$OUT"
+EXT="$(python3 -c 'import sysconfig;print(sysconfig.get_config_var("EXT_SUFFIX"))')"
+PYBIND_INC="$(python3 -m pybind11 --includes)"
+TARGET="$OUT/_cmtj$EXT"
+if [ ! -f "$TARGET" ] || [ "$REF/core/junction.hpp" -nt "$TARGET" ]; then
+  g++ -O3 -shared -fPIC -std=c++17 -fvisibility=hidden -Wno-unused-variable \
+      -ffp-contract=off -DVERSION_INFO='"ref-local"' \
+      -I"$REF" -I"$REF/core" -I"$HERE/stubs/third_party" \
+      $PYBIND_INC "$REF/python/cmtj.cpp" -o "$TARGET.tmp"
+  mv "$TARGET.tmp" "$TARGET"
+fi
+# A shim package named `cmtj` whose submodules (cmtj.utils, cmtj.stack, ...)
+# resolve from the reference tree, so no reference file is copied here.
+mkdir -p "$OUT/cmtj"
+cat > "$OUT/cmtj/__init__.py" <<EOF
+import os as _os
+__path__ = [_os.path.join("$REF", "cmtj")]
+__version__ = "ref-local"
+import _cmtj
+from _cmtj import *
+EOF
+echo "built $TARGET"

@@ -1,0 +1,586 @@
+// cmtj_oracle.cpp -- CPU restatement of the reference macrospin time loop.
+//
+// TEST INFRASTRUCTURE ONLY.  This file is the oracle: the tests, the smoke
+// check and the CPU-baseline leg of bench.py call it to check (and time) the
+// GPU solver.  The product (cmtj_gb300 and libcmtj_gpu.so) never links,
+// loads or calls it.
+//
+// It restates, in plain FP64 C++ with no FMA contraction (build with
+// -ffp-contract=off), the arithmetic of LemurPwned/cmtj:
+//   core/drivers.hpp:73-108, 262-305   ScalarDriver::getCurrentScalarValue
+//   core/cvector.hpp:179-192           CVector length / normalize
+//   core/junction.hpp:54-72            calculate_tensor_interaction
+//   core/junction.hpp:580-701          calculateHeff and its field terms
+//   core/junction.hpp:716-831          solveLLG (LLG + STT + SOT), stochasticTorque
+//   core/junction.hpp:1017-1041        Layer::rk4_step
+//   core/junction.hpp:1111-1128        thermal field standard deviation
+//   core/junction.hpp:1580-1636        logLayerParams
+//   core/junction.hpp:1668-1815        runners (single/multi layer, Euler-Heun, Heun)
+//   core/junction.hpp:1835-1867        strip / classic magnetoresistance
+//   core/junction.hpp:1948-1981        runSimulation fixed-step loop
+// keeping the reference's expression order so that deterministic runs are
+// bit-identical to the reference build (checked by tests/test_oracle_pin.py).
+//
+// The thermal field uses Philox4x32-10 (Salmon et al., SC'11) and the
+// Box-Muller transform instead of the reference's unseeded std::mt19937, so
+// thermal runs are reproducible; against the reference they agree in
+// statistics only.
+//
+// The scalar type is a template parameter so that the same code, run on a
+// counting type, yields the FLOP count per layer-step used for the roofline.
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <thread>
+#include <vector>
+#include <atomic>
+
+#include "../include/cmtj_gpu.h"
+
+namespace oracle {
+using std::cos;
+using std::erf;
+using std::exp;
+using std::fabs;
+using std::log;
+using std::pow;
+using std::sin;
+using std::sqrt;
+
+// ---------------------------------------------------------------- vectors
+template <typename T> struct V3 {
+  T x, y, z;
+  V3() : x(0.0), y(0.0), z(0.0) {}
+  V3(T a, T b, T c) : x(a), y(b), z(c) {}
+  V3 operator+(const V3 &v) const { return V3(x + v.x, y + v.y, z + v.z); }
+  V3 operator-(const V3 &v) const { return V3(x - v.x, y - v.y, z - v.z); }
+  V3 operator*(const T &s) const { return V3(x * s, y * s, z * s); }
+  V3 operator/(const T &s) const { return V3(x / s, y / s, z / s); }
+};
+template <typename T> V3<T> smul(const T &s, const V3<T> &v) { return V3<T>(s * v.x, s * v.y, s * v.z); }
+template <typename T> T dot(const V3<T> &a, const V3<T> &b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+template <typename T> V3<T> cross(const V3<T> &a, const V3<T> &b) {
+  return V3<T>(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+template <typename T> T sq(const T &a) { return a * a; }  // pow(a, 2): GCC folds it to a*a
+template <typename T> V3<T> normalized(const V3<T> &v) {
+  const T mag = sqrt(sq(v.x) + sq(v.y) + sq(v.z));
+  if (mag != 0) return V3<T>(v.x / mag, v.y / mag, v.z / mag);
+  return v;
+}
+template <typename T> V3<T> tensor_mul(const V3<T> &m, const double *t, const T &Ms, const T &mu0) {
+  V3<T> r(t[0] * m.x + t[1] * m.y + t[2] * m.z, t[3] * m.x + t[4] * m.y + t[5] * m.z,
+          t[6] * m.x + t[7] * m.y + t[8] * m.z);
+  return r * (Ms / mu0);
+}
+template <typename T> V3<T> v3(const double *p) { return V3<T>(p[0], p[1], p[2]); }
+
+// ---------------------------------------------------------------- drivers
+// drivers.hpp:262-305; table drivers hold host-sampled custom callbacks.
+template <typename T> struct Tables {
+  const double *data = nullptr;
+  uint32_t step = 0;   // current iteration (table row)
+  int stage = 0;       // 0: t, 1: t + dt/2, 2: t + dt
+};
+
+template <typename T> T driver_value(const cmtj_driver_t &d, const T &time, const Tables<T> &tb) {
+  T rv = d.constantValue;
+  switch (d.update) {
+  case CMTJ_DRV_CONSTANT: break;
+  case CMTJ_DRV_PULSE: {
+    const int n = (int)(double)(time / d.period);
+    const T dT = d.cycle * d.period;
+    const T nT = n * d.period;
+    if (nT <= time && time <= (nT + dT)) rv = rv + d.amplitude;
+    break;
+  }
+  case CMTJ_DRV_SINE: rv = rv + d.amplitude * sin(2 * M_PI * time * d.frequency + d.phase); break;
+  case CMTJ_DRV_POSINE: rv = rv + fabs(d.amplitude * sin(2 * M_PI * time * d.frequency + d.phase)); break;
+  case CMTJ_DRV_HALFSINE: {
+    const T tamp = d.amplitude * sin(2 * M_PI * time * d.frequency + d.phase);
+    if (tamp <= 0) rv = rv + tamp;
+    break;
+  }
+  case CMTJ_DRV_STEP:
+    if (time >= d.timeStart && time <= d.timeStop) rv = rv + d.amplitude;
+    break;
+  case CMTJ_DRV_TRAPEZOID: {
+    const double ts = d.timeStart, e = d.edgeTime, s = d.steadyTime, a = d.amplitude;
+    T add = 0.0;
+    if (time < ts) add = 0.0;
+    else if (time <= ts + e) add = (a / e) * (time - ts);
+    else if (time <= ts + e + s) add = a;
+    else if (time <= ts + 2 * e + s) add = a - (a / e) * (time - (ts + e + s));
+    rv = rv + add;
+    break;
+  }
+  case CMTJ_DRV_GAUSSIMPULSE:
+    rv = rv + d.amplitude * exp(-sq(time - d.timeStart) / (2 * sq(T(d.edgeTime))));
+    break;
+  case CMTJ_DRV_GAUSSSTEP:
+    rv = rv + 0.5 * d.amplitude * (1 + erf((time - d.timeStart) / (sqrt(2.0) * d.edgeTime)));
+    break;
+  case CMTJ_DRV_TABLE:
+    return tb.data[d.table_offset + (int64_t)tb.step * 3 + tb.stage];
+  default: break;
+  }
+  return rv;
+}
+
+// ---------------------------------------------------------------- philox
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11), counter-based.
+struct U4 { uint32_t v[4]; };
+inline U4 philox4x32_10(U4 c, uint32_t k0, uint32_t k1) {
+  const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u, W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+  for (int r = 0; r < 10; ++r) {
+    const uint64_t p0 = (uint64_t)M0 * c.v[0];
+    const uint64_t p1 = (uint64_t)M1 * c.v[2];
+    const uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+    const uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+    U4 n;
+    n.v[0] = hi1 ^ c.v[1] ^ k0;
+    n.v[1] = lo1;
+    n.v[2] = hi0 ^ c.v[3] ^ k1;
+    n.v[3] = lo0;
+    c = n;
+    k0 += W0;
+    k1 += W1;
+  }
+  return c;
+}
+// Three N(0,1) draws of one layer at one step: Box-Muller on the four
+// 32-bit words, u = (w + 0.5) / 2^32 in (0, 1).
+inline void gaussian3(uint32_t seed_lo, uint32_t seed_hi, uint64_t step, double g[3]) {
+  U4 c;
+  c.v[0] = (uint32_t)step;
+  c.v[1] = (uint32_t)(step >> 32);
+  c.v[2] = 0x7E4Du;  // thermal-field stream tag
+  c.v[3] = 0u;
+  const U4 w = philox4x32_10(c, seed_lo, seed_hi);
+  const double s = 2.3283064365386963e-10;  // 2^-32
+  const double u0 = ((double)w.v[0] + 0.5) * s, u1 = ((double)w.v[1] + 0.5) * s;
+  const double u2 = ((double)w.v[2] + 0.5) * s, u3 = ((double)w.v[3] + 0.5) * s;
+  const double r0 = sqrt(-2.0 * log(u0)), r1 = sqrt(-2.0 * log(u2));
+  const double a0 = 6.283185307179586 * u1, a1 = 6.283185307179586 * u3;
+  g[0] = r0 * cos(a0);
+  g[1] = r0 * sin(a0);
+  g[2] = r1 * cos(a1);
+}
+
+// ---------------------------------------------------------------- physics
+template <typename T> struct Side {  // side effects logged with calculateEnergies
+  T K = 0.0, K2 = 0.0, Jb = 0.0, Jt = 0.0, I = 0.0;
+  V3<T> Hext, Hiec, Hanis, Hdemag, Hfl, Hdl;
+};
+
+template <typename T> struct Ctx {
+  const cmtj_layer_t *L;
+  const cmtj_constants_t *c;
+  Tables<T> tb;
+  Side<T> *side;
+};
+
+template <typename T> V3<T> axial(const cmtj_layer_t &L, int slot, const T &t, const Tables<T> &tb) {
+  return V3<T>(driver_value<T>(L.drv[slot], t, tb), driver_value<T>(L.drv[slot + 1], t, tb),
+               driver_value<T>(L.drv[slot + 2], t, tb));
+}
+
+// calculateHeff (junction.hpp:580-622).
+template <typename T>
+V3<T> heff(Ctx<T> &cx, const T &time, const V3<T> &m, const V3<T> &bottom, const V3<T> &top) {
+  const cmtj_layer_t &L = *cx.L;
+  const T mu0 = cx.c->mu0;
+  const T Ms = L.Ms;
+  const V3<T> Hdipole = tensor_mul<T>(bottom, L.dipole_bottom, Ms, mu0) + tensor_mul<T>(top, L.dipole_top, Ms, mu0);
+  const V3<T> Hext = axial<T>(L, CMTJ_SLOT_HEXT, time, cx.tb);
+  const V3<T> Hoe = axial<T>(L, CMTJ_SLOT_HOE, time, cx.tb);
+  const V3<T> Hdemag = tensor_mul<T>(m, L.demag, Ms, mu0);
+  // calculateIEC (654-675)
+  const T Jb = driver_value<T>(L.drv[CMTJ_SLOT_IEC_BOTTOM], time, cx.tb);
+  const T Jt = driver_value<T>(L.drv[CMTJ_SLOT_IEC_TOP], time, cx.tb);
+  const T J2b = driver_value<T>(L.drv[CMTJ_SLOT_IECQ_BOTTOM], time, cx.tb);
+  const T J2t = driver_value<T>(L.drv[CMTJ_SLOT_IECQ_TOP], time, cx.tb);
+  const T Mst = Ms * T(L.thickness);
+  const V3<T> Hiec = (bottom * (Jb + 2 * J2b * dot(bottom, m))) / Mst + (top * (Jt + 2 * J2t * dot(top, m))) / Mst;
+  // calculateIDMI (677-701)
+  const V3<T> Db = axial<T>(L, CMTJ_SLOT_IDMI_BOTTOM, time, cx.tb);
+  const V3<T> Dt = axial<T>(L, CMTJ_SLOT_IDMI_TOP, time, cx.tb);
+  const V3<T> Hidmi = smul<T>(-1.0, cross(Db, bottom)) / Mst + smul<T>(-1.0, cross(Dt, top)) / Mst;
+  // calculateAnisotropy (638-643)
+  const V3<T> anis = v3<T>(L.anis);
+  const T K = driver_value<T>(L.drv[CMTJ_SLOT_ANIS], time, cx.tb);
+  const V3<T> Hanis = anis * ((2 * K) * dot(anis, m) / Ms);
+  const V3<T> Hdmi = axial<T>(L, CMTJ_SLOT_HDMI, time, cx.tb);
+  const V3<T> Hres = axial<T>(L, CMTJ_SLOT_HRES, time, cx.tb);
+  // calculateSecondOrderAnisotropy (645-652)
+  const T K2 = driver_value<T>(L.drv[CMTJ_SLOT_ANIS2], time, cx.tb);
+  const T da = dot(anis, m);
+  const V3<T> Hanis2 = anis * ((4 * K2) * pow(da, 3) / Ms);
+  const V3<T> Hfl;  // Hfluctuation default argument: zero vector
+  const V3<T> H = Hext + Hanis + Hanis2 + Hiec + Hidmi + Hoe + Hdmi + Hfl - Hdemag - Hdipole + Hres;
+  if (cx.side) {
+    cx.side->K = K; cx.side->K2 = K2; cx.side->Jb = Jb; cx.side->Jt = Jt;
+    cx.side->Hext = Hext; cx.side->Hiec = Hiec; cx.side->Hanis = Hanis; cx.side->Hdemag = Hdemag;
+  }
+  return H;
+}
+
+// solveLLG (junction.hpp:716-815).
+template <typename T>
+V3<T> llg(Ctx<T> &cx, const T &time, const V3<T> &m, const V3<T> &bottom, const V3<T> &top, const V3<T> &H) {
+  const cmtj_layer_t &L = *cx.L;
+  const T GYRO = cx.c->gyro;
+  const T damping = L.damping;
+  const V3<T> prod = cross(m, H);
+  const V3<T> prod2 = cross(m, prod);
+  const T convTerm = 1 / (1 + sq(damping));
+  const V3<T> dmdt = prod + prod2 * damping;
+  V3<T> reference;
+  switch (L.referenceType) {
+  case CMTJ_REF_FIXED: reference = v3<T>(L.ref); break;
+  case CMTJ_REF_TOP: reference = top; break;
+  case CMTJ_REF_BOTTOM: reference = bottom; break;
+  default: break;
+  }
+  if (L.includeSTT) {
+    const T I = driver_value<T>(L.drv[CMTJ_SLOT_CURRENT], time, cx.tb);
+    if (cx.side) cx.side->I = I;
+    const T aJ = cx.c->hbar * I / (cx.c->echarge * L.Ms * L.thickness);
+    T eta = 0;
+    if (L.alternativeSTT) {
+      eta = (L.spinPolarisation) / (1 + L.slonczewski * dot(m, reference));
+    } else {
+      const T slonSq = sq(T(L.slonczewski));
+      eta = (L.spinPolarisation * slonSq) / (slonSq + 1 + (slonSq - 1) * dot(m, reference));
+    }
+    const T sttTerm = GYRO * aJ * eta;
+    const V3<T> fieldLike = cross(m, reference);
+    const V3<T> dampingLike = cross(m, fieldLike);
+    return (dmdt * -GYRO + dampingLike * -sttTerm * T(L.kappa) + fieldLike * sttTerm * T(L.beta)) * convTerm;
+  } else if (L.includeSOT) {
+    T Hdl = 0, Hfl = 0, Hdl2 = 0, Hfl2 = 0;
+    if (L.dynamicSOT) {
+      Hdl = driver_value<T>(L.drv[CMTJ_SLOT_DL], time, cx.tb);
+      Hfl = driver_value<T>(L.drv[CMTJ_SLOT_FL], time, cx.tb);
+      Hdl2 = driver_value<T>(L.drv[CMTJ_SLOT_DL2], time, cx.tb);
+      Hfl2 = driver_value<T>(L.drv[CMTJ_SLOT_FL2], time, cx.tb);
+    } else {
+      const T I = driver_value<T>(L.drv[CMTJ_SLOT_CURRENT], time, cx.tb);
+      if (cx.side) cx.side->I = I;
+      Hdl = L.dampingLikeTorque * I;
+      Hfl = L.fieldLikeTorque * I;
+    }
+    const V3<T> ref2 = v3<T>(L.ref2);
+    if (cx.side) {
+      cx.side->Hfl = reference * (Hfl - damping * Hdl);
+      cx.side->Hdl = reference * (Hdl + damping * Hfl);
+    }
+    const V3<T> cm_p = cross(m, reference);
+    const V3<T> ccm_p = cross(m, cm_p);
+    const V3<T> cm_s = cross(m, ref2);
+    const V3<T> ccm_s = cross(m, cm_s);
+    const V3<T> flp = cm_p * (Hfl - damping * Hdl);
+    const V3<T> dlp = ccm_p * (Hdl + damping * Hfl);
+    const V3<T> fls = cm_s * (Hfl2 - damping * Hdl2);
+    const V3<T> dls = ccm_s * (Hdl2 + damping * Hfl2);
+    return (dmdt + flp + dlp + fls + dls) * -GYRO * convTerm;
+  }
+  return dmdt * -GYRO * convTerm;
+}
+
+template <typename T>
+V3<T> rhs(Ctx<T> &cx, const T &time, const V3<T> &m, const V3<T> &bottom, const V3<T> &top) {
+  const V3<T> H = heff<T>(cx, time, m, bottom, top);
+  return llg<T>(cx, time, m, bottom, top, H);
+}
+
+// stochasticTorque (junction.hpp:824-831).
+template <typename T> V3<T> stoch_torque(const cmtj_layer_t &L, const cmtj_constants_t &c, const V3<T> &m, const V3<T> &dW) {
+  const T convTerm = -T(c.gyro) / (1. + sq(T(L.damping)));
+  const V3<T> th = cross(m, dW);
+  const V3<T> th2 = cross(m, th);
+  return (th + th2 * T(L.damping)) * convTerm;
+}
+
+// getStochasticLangevinVector (junction.hpp:1111-1128).
+template <typename T> V3<T> langevin(const cmtj_layer_t &L, const cmtj_constants_t &c, const T &time,
+                                     uint64_t step, const Tables<T> &tb) {
+  if (!L.temperatureSet) return V3<T>();
+  const T temp = driver_value<T>(L.drv[CMTJ_SLOT_TEMPERATURE], time, tb);
+  const T mainFactor = (2 * T(L.damping) * T(c.kB) * temp) / (T(L.Ms) * T(L.cellVolume) * T(c.gyro));
+  const T sigma = sqrt(mainFactor);
+  double g[3];
+  gaussian3(L.seed_lo, L.seed_hi, L.noise_step + step, g);
+  return V3<T>(g[0], g[1], g[2]) * sigma;
+}
+
+// --------------------------------------------------------------- junction
+template <typename T> struct JunctionRun {
+  const cmtj_junction_t &J;
+  cmtj_layer_t *layers;  // J.n_layers entries
+  const cmtj_sim_params_t &p;
+  const double *tables;
+  std::vector<V3<T>> mag;
+  std::vector<Side<T>> side;
+
+  JunctionRun(const cmtj_junction_t &J_, cmtj_layer_t *layers_, const cmtj_sim_params_t &p_, const double *tables_)
+      : J(J_), layers(layers_), p(p_), tables(tables_), mag(J_.n_layers), side(J_.n_layers) {
+    for (int l = 0; l < J.n_layers; ++l) mag[l] = V3<T>(layers[l].mag[0], layers[l].mag[1], layers[l].mag[2]);
+  }
+
+  Ctx<T> ctx(int l, uint32_t step, int stage, bool record) {
+    Ctx<T> cx;
+    cx.L = &layers[l];
+    cx.c = &p.c;
+    cx.tb.data = tables;
+    cx.tb.step = step;
+    cx.tb.stage = stage;
+    cx.side = (record && p.calculate_energies) ? &side[l] : nullptr;
+    return cx;
+  }
+
+  // rk4_step (junction.hpp:1017-1041); false on NaN.
+  bool rk4(int l, const T &t, uint32_t i, const V3<T> &bottom, const V3<T> &top) {
+    const T dt = p.time_step;
+    V3<T> m_t = mag[l];
+    Ctx<T> c0 = ctx(l, i, 0, false), c1 = ctx(l, i, 1, false), c2 = ctx(l, i, 2, true);
+    const V3<T> k1 = rhs<T>(c0, t, m_t, bottom, top) * dt;
+    const V3<T> k2 = rhs<T>(c1, t + 0.5 * dt, m_t + k1 * 0.5, bottom, top) * dt;
+    const V3<T> k3 = rhs<T>(c1, t + 0.5 * dt, m_t + k2 * 0.5, bottom, top) * dt;
+    const V3<T> k4 = rhs<T>(c2, t + dt, m_t + k3, bottom, top) * dt;
+    m_t = m_t + (k1 + (k2 * 2.0) + (k3 * 2.0) + k4) / 6.0;
+    mag[l] = normalized(m_t);
+    return !std::isnan((double)mag[l].x);
+  }
+
+  // runSingleLayerSolver / runMultiLayerSolver (1668-1707).
+  bool step_rk4(const T &t, uint32_t i) {
+    const int n = J.n_layers;
+    std::vector<V3<T>> copies(n + 2);
+    for (int l = 0; l < n; ++l) copies[l + 1] = mag[l];
+    for (int l = 0; l < n; ++l)
+      if (!rk4(l, t, i, copies[l], copies[l + 2])) return false;
+    return true;
+  }
+
+  // eulerHeunSolverStep (1709-1754).
+  void step_euler_heun(const T &t, uint32_t i) {
+    const int n = J.n_layers;
+    const T dt = p.time_step;
+    std::vector<V3<T>> mPrime(n);
+    for (int l = 0; l < n; ++l) {
+      Ctx<T> c0 = ctx(l, i, 0, true);
+      const V3<T> dW = langevin<T>(layers[l], p.c, t, i, c0.tb);
+      const V3<T> bottom = (l == 0) ? V3<T>() : mag[l - 1];
+      const V3<T> top = (l == n - 1) ? V3<T>() : mag[l + 1];
+      const V3<T> f = rhs<T>(c0, t, mag[l], bottom, top);
+      const V3<T> g = stoch_torque<T>(layers[l], p.c, mag[l], dW);
+      const V3<T> mNext = mag[l] + g * sqrt(dt);
+      const V3<T> g2 = stoch_torque<T>(layers[l], p.c, mNext, dW);
+      mPrime[l] = mag[l] + f * dt + smul<T>(0.5, g + g2) * sqrt(dt);
+    }
+    for (int l = 0; l < n; ++l) mag[l] = normalized(mPrime[l]);
+  }
+
+  // heunSolverStep (1756-1815).
+  void step_heun(const T &t, uint32_t i) {
+    const int n = J.n_layers;
+    const T dt = p.time_step;
+    std::vector<V3<T>> fn(n), gn(n), dW(n), mNext(n);
+    for (int l = 0; l < n; ++l) {
+      const V3<T> bottom = (l == 0) ? V3<T>() : mag[l - 1];
+      const V3<T> top = (l == n - 1) ? V3<T>() : mag[l + 1];
+      Ctx<T> c0 = ctx(l, i, 0, false);
+      fn[l] = rhs<T>(c0, t, mag[l], bottom, top);
+      dW[l] = langevin<T>(layers[l], p.c, t, i, c0.tb);
+      gn[l] = stoch_torque<T>(layers[l], p.c, mag[l], dW[l]);
+      mNext[l] = mag[l] + fn[l] * dt + gn[l] * sqrt(dt);
+    }
+    for (int l = 0; l < n; ++l) {
+      const V3<T> bottom = (l == 0) ? V3<T>() : mNext[l - 1];
+      const V3<T> top = (l == n - 1) ? V3<T>() : mNext[l + 1];
+      Ctx<T> c2 = ctx(l, i, 2, true);
+      const V3<T> f2 = rhs<T>(c2, t + dt, mNext[l], bottom, top);
+      const V3<T> g2 = stoch_torque<T>(layers[l], p.c, mNext[l], dW[l]);
+      mag[l] = mag[l] + smul<T>(0.5 * dt, fn[l] + f2) + smul<T>(0.5, gn[l] + g2) * sqrt(dt);
+      mag[l] = normalized(mag[l]);
+    }
+  }
+
+  // logLayerParams (1580-1636) into one row of log_width doubles.
+  void log_row(double *row, const T &t) {
+    const int n = J.n_layers;
+    int col = 0;
+    for (int l = 0; l < n; ++l) {
+      if (p.calculate_energies) {
+        const Side<T> &s = side[l];
+        const T vals[26] = {s.K, s.K2, s.Jb, s.Jt, s.I,
+                            s.Hext.x, s.Hext.y, s.Hext.z, s.Hiec.x, s.Hiec.y, s.Hiec.z,
+                            s.Hanis.x, s.Hanis.y, s.Hanis.z, s.Hdemag.x, s.Hdemag.y, s.Hdemag.z,
+                            0.0, 0.0, 0.0,
+                            s.Hfl.x, s.Hfl.y, s.Hfl.z, s.Hdl.x, s.Hdl.y, s.Hdl.z};
+        for (int k = 0; k < 26; ++k) row[col++] = (double)vals[k];
+      }
+      row[col++] = (double)mag[l].x;
+      row[col++] = (double)mag[l].y;
+      row[col++] = (double)mag[l].z;
+    }
+    T r0 = 0.0, r1 = 0.0, r2 = 0.0;
+    if (J.mr_mode == CMTJ_MR_CLASSIC && n == 1) {
+      const T cosT = dot(mag[0], v3<T>(layers[0].ref));
+      r0 = J.Rp + (((J.Rap - J.Rp) / 2.0) * (1.0 - cosT));
+    } else if (J.mr_mode == CMTJ_MR_CLASSIC && n > 1) {
+      const T cosT = dot(mag[0], mag[1]);
+      r0 = J.Rp + (((J.Rap - J.Rp) / 2.0) * (1.0 - cosT));
+    } else if (J.mr_mode == CMTJ_MR_STRIP) {
+      T Rx_acc = 0.0, Ry_acc = 0.0;
+      for (int l = 0; l < n; ++l) {
+        const T Rx = J.Rx0[l] + J.AMR_X[l] * (mag[l].x * mag[l].x) + J.SMR_X[l] * (mag[l].y * mag[l].y);
+        const T Ry = J.Ry0[l] + 0.5 * J.AHE[l] * mag[l].z + (J.AMR_Y[l] + J.SMR_Y[l]) * mag[l].x * mag[l].y;
+        Rx_acc = Rx_acc + 1. / Rx;
+        Ry_acc = Ry_acc + 1. / Ry;
+      }
+      r0 = 1 / Rx_acc;
+      r1 = 1 / Ry_acc;
+      r2 = 0.;
+    }
+    row[col++] = (double)r0;
+    row[col++] = (double)r1;
+    row[col++] = (double)r2;
+    row[col++] = (double)t;
+  }
+
+  // runSimulation fixed-step loop (1966-1981).
+  uint32_t rows = 0;
+  uint32_t run(double *log) {
+    uint32_t row = 0;
+    uint32_t status = CMTJ_STATUS_OK;
+    for (uint32_t i = 0; i < p.total_iterations; ++i) {
+      const T t = (double)i * p.time_step;
+      if (p.solver == CMTJ_RK4) {
+        if (!step_rk4(t, i)) { status = CMTJ_STATUS_NAN; break; }
+      } else if (p.solver == CMTJ_EULER_HEUN) {
+        step_euler_heun(t, i);
+      } else {
+        step_heun(t, i);
+      }
+      if (!(i % p.write_every)) {
+        log_row(log + (size_t)row * p.log_width, t);
+        ++row;
+      }
+    }
+    rows = row;
+    for (int l = 0; l < J.n_layers; ++l) {
+      layers[l].mag[0] = (double)mag[l].x;
+      layers[l].mag[1] = (double)mag[l].y;
+      layers[l].mag[2] = (double)mag[l].z;
+    }
+    return status;
+  }
+};
+
+}  // namespace oracle
+
+namespace oracle_cnt {
+// ------------------------------------------------------------ op counting
+// A double that counts the arithmetic done on it; used once to fix the FLOP
+// count per layer-step.  add/sub/mul/div/sqrt count 1, transcendental 1.
+struct Counter { static thread_local uint64_t add, mul, div, sqrt_, trans; };
+thread_local uint64_t Counter::add = 0, Counter::mul = 0, Counter::div = 0, Counter::sqrt_ = 0, Counter::trans = 0;
+struct CD {
+  double v;
+  CD() : v(0) {}
+  CD(double x) : v(x) {}
+  explicit operator double() const { return v; }
+};
+inline CD operator+(CD a, CD b) { ++Counter::add; return CD(a.v + b.v); }
+inline CD operator-(CD a, CD b) { ++Counter::add; return CD(a.v - b.v); }
+inline CD operator*(CD a, CD b) { ++Counter::mul; return CD(a.v * b.v); }
+inline CD operator/(CD a, CD b) { ++Counter::div; return CD(a.v / b.v); }
+inline CD operator-(CD a) { return CD(-a.v); }
+inline CD operator+(CD a, double b) { return a + CD(b); }
+inline CD operator+(double a, CD b) { return CD(a) + b; }
+inline CD operator-(CD a, double b) { return a - CD(b); }
+inline CD operator-(double a, CD b) { return CD(a) - b; }
+inline CD operator*(CD a, double b) { return a * CD(b); }
+inline CD operator*(double a, CD b) { return CD(a) * b; }
+inline CD operator/(CD a, double b) { return a / CD(b); }
+inline CD operator/(double a, CD b) { return CD(a) / b; }
+inline CD operator*(int a, CD b) { return CD((double)a) * b; }
+inline CD operator+(int a, CD b) { return CD((double)a) + b; }
+inline CD operator/(int a, CD b) { return CD((double)a) / b; }
+inline bool operator<(CD a, CD b) { return a.v < b.v; }
+inline bool operator<=(CD a, CD b) { return a.v <= b.v; }
+inline bool operator>=(CD a, CD b) { return a.v >= b.v; }
+inline bool operator<(CD a, double b) { return a.v < b; }
+inline bool operator<=(CD a, double b) { return a.v <= b; }
+inline bool operator<=(CD a, int b) { return a.v <= b; }
+inline bool operator>=(CD a, double b) { return a.v >= b; }
+inline bool operator<=(double a, CD b) { return a <= b.v; }
+inline bool operator!=(CD a, int b) { return a.v != b; }
+inline CD sqrt(CD a) { ++Counter::sqrt_; return CD(std::sqrt(a.v)); }
+inline CD sin(CD a) { ++Counter::trans; return CD(std::sin(a.v)); }
+inline CD exp(CD a) { ++Counter::trans; return CD(std::exp(a.v)); }
+inline CD erf(CD a) { ++Counter::trans; return CD(std::erf(a.v)); }
+inline CD fabs(CD a) { return CD(std::fabs(a.v)); }
+inline CD pow(CD a, int n) { CD r = a; for (int k = 1; k < n; ++k) r = r * a; return r; }
+
+}  // namespace oracle_cnt
+
+// ----------------------------------------------------------------- C ABI
+extern "C" {
+
+int oracle_log_width(int n_layers, int calculate_energies) {
+  return n_layers * (calculate_energies ? CMTJ_ENERGY_COLS : 3) + 4;
+}
+
+// Junction::runSimulation on the CPU for n_junctions junctions, using
+// n_threads host threads (junctions are independent).  Same packed inputs,
+// log layout and [n][2] status words as cmtj_run_simulation_f64.
+int oracle_run_simulation(const cmtj_junction_t *junctions, int32_t n_junctions, cmtj_layer_t *layers,
+                          const double *tables, const cmtj_sim_params_t *p, double *log, uint32_t *status,
+                          int32_t n_threads) {
+  if (n_junctions < 0 || !p || p->write_every == 0) return CMTJ_ERR_ARG;
+  std::atomic<int32_t> next(0);
+  auto worker = [&]() {
+    for (;;) {
+      const int32_t j = next.fetch_add(1);
+      if (j >= n_junctions) break;
+      const cmtj_junction_t &J = junctions[j];
+      oracle::JunctionRun<double> run(J, layers + J.layer_offset, *p, tables);
+      status[2 * j] = run.run(log + (size_t)j * p->n_log * p->log_width);
+      status[2 * j + 1] = run.rows;
+    }
+  };
+  if (n_threads <= 1) {
+    worker();
+  } else {
+    std::vector<std::thread> pool;
+    for (int k = 0; k < n_threads; ++k) pool.emplace_back(worker);
+    for (auto &t : pool) t.join();
+  }
+  return CMTJ_OK;
+}
+
+// FLOP count of one junction run on the counting scalar type:
+// out[0] adds+subs, out[1] muls, out[2] divs, out[3] sqrts, out[4] sin/exp/erf.
+int oracle_count_flops(const cmtj_junction_t *junction, cmtj_layer_t *layers, const double *tables,
+                       const cmtj_sim_params_t *p, double *log, uint64_t *out) {
+  using oracle_cnt::Counter;
+  Counter::add = Counter::mul = Counter::div = Counter::sqrt_ = Counter::trans = 0;
+  oracle::JunctionRun<oracle_cnt::CD> run(*junction, layers, *p, tables);
+  run.run(log);
+  out[0] = Counter::add;
+  out[1] = Counter::mul;
+  out[2] = Counter::div;
+  out[3] = Counter::sqrt_;
+  out[4] = Counter::trans;
+  return CMTJ_OK;
+}
+
+// Three Gaussian draws of the thermal stream, exposed for the noise tests.
+void oracle_gaussian3(uint32_t seed_lo, uint32_t seed_hi, uint64_t step, double *g) {
+  oracle::gaussian3(seed_lo, seed_hi, step, g);
+}
+
+}  // extern "C"

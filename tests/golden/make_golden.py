@@ -1,0 +1,54 @@
+"""Generate the golden fixtures in tests/golden/ from the reference itself.
+
+Runs every case of tests/cases.py with the reference's `_cmtj` extension
+(built from the reference sources by oracle/build_ref.sh into oracle/_ref/)
+and stores the full-precision logs and final magnetisations as
+<case>.npz.  Needs the reference sources, so it runs in the development
+container only; the fixtures are committed and travel with the tests.
+
+    python tests/golden/make_golden.py [case ...]
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+sys.path.insert(0, ROOT)
+
+
+def reference_module():
+    from oracle.build import build_reference
+    ref = build_reference()
+    if ref is None:
+        raise SystemExit("reference sources not available; cannot regenerate fixtures")
+    sys.path.insert(0, ref)
+    import cmtj  # the shim package of oracle/_ref
+    import cmtj.stack  # noqa: F401
+    return cmtj
+
+
+def save_case(cm, name):
+    import cases
+    _, log, mags = cases.run_case(cm, name)
+    out = {"log__" + k: v for k, v in log.items()}
+    for lid, m in mags.items():
+        out["mag__" + lid] = np.asarray(m, dtype=np.float64)
+    path = os.path.join(HERE, name + ".npz")
+    np.savez_compressed(path, **out)
+    return path, sum(v.size for v in log.values())
+
+
+def main(argv):
+    import cases
+    cm = reference_module()
+    names = argv or list(cases.DETERMINISTIC)
+    for name in names:
+        path, n = save_case(cm, name)
+        print("%-20s %8d values  %7.1f KB" % (name, n, os.path.getsize(path) / 1024))
+
+
+if __name__ == "__main__":
+    main(sys.argv[1:])

@@ -1,0 +1,101 @@
+"""ctypes wrapper of the oracle (oracle/_build/libcmtj_oracle.so) for the
+tests, the smoke check and bench.py's CPU baseline.  It runs the same packed
+inputs that cmtj_gb300 lowers for the GPU, on the CPU restatement."""
+import ctypes
+import os
+import sys
+import types
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+import cmtj_gb300  # noqa: E402
+from cmtj_gb300 import _abi  # noqa: E402
+from cmtj_gb300._lower import apply_results, lower, plan_run  # noqa: E402
+
+_lib = None
+
+
+def oracle_lib():
+    global _lib
+    if _lib is None:
+        from oracle.build import build_oracle
+        path = build_oracle()
+        lib = ctypes.CDLL(path)
+        P = ctypes.c_void_p
+        lib.oracle_run_simulation.restype = ctypes.c_int
+        lib.oracle_run_simulation.argtypes = [P, ctypes.c_int32, P, P, P, P, P, ctypes.c_int32]
+        lib.oracle_count_flops.restype = ctypes.c_int
+        lib.oracle_count_flops.argtypes = [P, P, P, P, P, P]
+        lib.oracle_gaussian3.restype = None
+        lib.oracle_gaussian3.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64, P]
+        lib.oracle_log_width.restype = ctypes.c_int
+        lib.oracle_log_width.argtypes = [ctypes.c_int, ctypes.c_int]
+        _lib = lib
+    return _lib
+
+
+def _p(a):
+    return ctypes.c_void_p(a.ctypes.data) if a is not None else None
+
+
+def run_lowered(lowered, threads=1):
+    """Run a Lowered batch on the oracle; returns (log, status) and updates
+    lowered.layers[...]['mag'] in place."""
+    lib = oracle_lib()
+    n = len(lowered.junctions)
+    n_log = int(lowered.params["n_log"][0])
+    log = np.zeros((n, max(n_log, 1), lowered.log_width), dtype=np.float64)
+    status = np.zeros(2 * n, dtype=np.uint32)
+    rc = lib.oracle_run_simulation(_p(lowered.junctions), n, _p(lowered.layers), _p(lowered.tables),
+                                   _p(lowered.params), _p(log), _p(status), threads)
+    assert rc == 0, rc
+    return log, status
+
+
+def run_oracle(junctions, totalTime, timeStep=1e-13, writeFrequency=1e-11, verbose=False,
+               calculateEnergies=False, solverMode=cmtj_gb300.SolverMode.RK4, threads=1):
+    plan = plan_run(totalTime, timeStep, writeFrequency)
+    solver = junctions[0].getSolver(solverMode)
+    lowered = lower(junctions, plan, solver, calculateEnergies)
+    log, status = run_lowered(lowered, threads)
+    apply_results(junctions, lowered, log, status, plan)
+    return lowered
+
+
+class OracleJunction(cmtj_gb300.Junction):
+    """A cmtj_gb300.Junction whose runSimulation runs on the oracle."""
+
+    def runSimulation(self, totalTime, timeStep=1e-13, writeFrequency=1e-11, verbose=False,
+                      calculateEnergies=False, solverMode=cmtj_gb300.SolverMode.RK4):
+        run_oracle([self], totalTime, timeStep, writeFrequency, verbose, calculateEnergies, solverMode)
+
+
+def oracle_module():
+    """A stand-in for the `cmtj` module whose Junction runs on the oracle."""
+    m = types.SimpleNamespace(**{k: getattr(cmtj_gb300, k) for k in dir(cmtj_gb300) if not k.startswith("__")})
+    m.Junction = OracleJunction
+    return m
+
+
+def count_flops(junction, totalTime, timeStep, writeFrequency, solverMode=cmtj_gb300.SolverMode.RK4):
+    """[adds, muls, divs, sqrts, transcendentals] of one run of `junction`
+    on the counting scalar type."""
+    lib = oracle_lib()
+    plan = plan_run(totalTime, timeStep, writeFrequency)
+    solver = junction.getSolver(solverMode)
+    lowered = lower([junction], plan, solver, False)
+    log = np.zeros((max(plan.n_log, 1), lowered.log_width), dtype=np.float64)
+    out = np.zeros(5, dtype=np.uint64)
+    lib.oracle_count_flops(_p(lowered.junctions), _p(lowered.layers), _p(lowered.tables), _p(lowered.params),
+                           _p(log), _p(out))
+    return out
+
+
+def gaussian3(seed_lo, seed_hi, step):
+    g = np.zeros(3, dtype=np.float64)
+    oracle_lib().oracle_gaussian3(seed_lo, seed_hi, step, _p(g))
+    return g

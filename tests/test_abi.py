@@ -1,0 +1,46 @@
+"""The C-ABI library loads (no GPU needed) and exports every symbol that
+include/*.h declares, with struct layouts matching the Python mirror."""
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = set()
+    for fn in os.listdir(os.path.join(ROOT, "include")):
+        if not fn.endswith(".h"):
+            continue
+        src = open(os.path.join(ROOT, "include", fn)).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        for m in re.finditer(r"^\s*(?:const\s+)?[A-Za-z_][A-Za-z0-9_]*\s*\*?\s*(cmtj_[A-Za-z0-9_]+)\s*\(", src, re.M):
+            names.add(m.group(1))
+    return names
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from cmtj_gb300 import _abi, build
+    build.build()
+    return _abi.load()
+
+
+def test_library_exports_header_symbols(lib):
+    names = declared_functions()
+    assert "cmtj_run_simulation_f64" in names
+    for n in sorted(names):
+        assert hasattr(lib, n), n
+
+
+def test_python_prototypes_cover_header(lib):
+    from cmtj_gb300 import _abi
+    assert declared_functions() <= set(_abi.PROTOTYPES), declared_functions() - set(_abi.PROTOTYPES)
+
+
+def test_struct_layout_and_version(lib):
+    from cmtj_gb300 import _abi
+    _abi.check_layout(lib)
+    assert lib.cmtj_log_width(2, 0) == _abi.log_width(2, False) == 10
+    assert lib.cmtj_log_width(3, 1) == 3 * 29 + 4

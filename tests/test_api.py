@@ -1,0 +1,195 @@
+"""Host API of cmtj_gb300 against the reference's API tests (tests/test_drivers.py,
+test_sanity.py, test_basic.py, test_sot_torques.py, test_constants.py,
+test_imports.py in the reference suite): construction, driver arithmetic,
+error types and messages.  No simulation runs here."""
+import math
+
+import pytest
+
+import cmtj_gb300 as cmtj
+from cmtj_gb300 import AxialDriver, CVector, Junction, Layer, ScalarDriver, constantDriver, sineDriver
+
+DEMAG = [CVector(0, 0, 0), CVector(0, 0, 0), CVector(0, 0, 1)]
+
+
+def _layer(id="free", **kw):
+    args = dict(mag=CVector(0, 0, 1), anis=CVector(1, 0, 0), Ms=1.65, thickness=3e-9, cellSurface=0,
+                demagTensor=DEMAG, damping=0.005)
+    args.update(kw)
+    return Layer(id, **args)
+
+
+def test_cvector_operators():
+    cvec1, cvec2, cvec3 = CVector(1.0, 2.0, 3.0), CVector(1.0, 2.0, 3.0), CVector(2, 4, 6)
+    assert (1.0, 2.0, 3.0)[0] == cvec1[0] and cvec1[2] == 3.0
+    assert cvec1 == cvec2 and cvec1 != cvec3
+    assert (cvec1 + cvec2) == cvec3 and (cvec3 - cvec1) == cvec1
+    assert 2 * cvec1 == cvec3 and cvec3 * 0.5 == cvec1
+    cvec1 += CVector(1.0, 2.0, 3.0)
+    assert cvec1 == cvec3
+    cvec3 -= cvec2
+    assert cvec3 == cvec2
+    assert len(cvec1) == 3 and cvec1.tolist() == [2.0, 4.0, 6.0]
+    v = CVector(3, 0, 4)
+    assert v.length() == 5.0
+    v.normalize()
+    assert v == CVector(0.6, 0, 0.8)
+
+
+def test_axial_definitions_and_aliases():
+    cvec = CVector(1.0, 2.0, 3.0)
+    assert AxialDriver(1.0, 2.0, 3.0).getCurrentAxialDrivers(0.0) == cvec
+    assert AxialDriver(cvec).getCurrentAxialDrivers(0.0) == cvec
+    d1 = AxialDriver(constantDriver(1.0), constantDriver(2.0), constantDriver(3.0))
+    assert d1.getCurrentAxialDrivers(1e6) == cvec
+    d2 = AxialDriver([constantDriver(1.0), constantDriver(2.0), constantDriver(3.0)])
+    assert d2.getCurrentAxialDrivers(0.0) == cvec
+    d2.applyMask([1, 0, 1])
+    assert d2.getCurrentAxialDrivers(0.0) == CVector(1.0, 0.0, 3.0)
+    with pytest.raises(RuntimeError, match="mask must be binary"):
+        d2.applyMask([1, 2, 1])
+
+
+def test_driver_ops():
+    """Exact values of test_drivers.py:51-65: the operators shift or scale
+    both the offset and the amplitude."""
+    driver = sineDriver(10, 20, 1, 0)
+    assert driver.getCurrentScalarValue(1 / 4) == 30
+    driver *= 2
+    assert driver.getCurrentScalarValue(1 / 4) == 60
+    driver = sineDriver(10, 20, 1, 0)
+    driver += 2
+    assert driver.getCurrentScalarValue(1 / 4) == 34
+    assert (sineDriver(10, 20, 1, 0) * 2).getCurrentScalarValue(1 / 4) == 60
+    assert (sineDriver(10, 20, 1, 0) + 2).getCurrentScalarValue(1 / 4) == 34
+
+
+def test_driver_waveforms():
+    assert cmtj.stepDriver(1, 2, 1.0, 2.0).getCurrentScalarValue(1.0) == 3  # inclusive start
+    assert cmtj.stepDriver(1, 2, 1.0, 2.0).getCurrentScalarValue(2.0) == 3  # inclusive stop
+    assert cmtj.stepDriver(1, 2, 1.0, 2.0).getCurrentScalarValue(2.5) == 1
+    assert cmtj.pulseDriver(0, 1, 1.0, 0.25).getCurrentScalarValue(3.1) == 1
+    assert cmtj.pulseDriver(0, 1, 1.0, 0.25).getCurrentScalarValue(3.3) == 0
+    tr = cmtj.trapezoidDriver(0, 10, 1.0, 1.0, 2.0)
+    assert [tr.getCurrentScalarValue(t) for t in (0.5, 1.5, 2.5, 4.5, 6)] == [0, 5, 10, 5, 0]
+    assert cmtj.gaussianImpulseDriver(0, 2, 1.0, 0.5).getCurrentScalarValue(1.0) == 2
+    assert cmtj.posSineDriver(0, -2, 1, 0).getCurrentScalarValue(0.25) == 2
+    assert cmtj.NullDriver().getCurrentScalarValue(1.0) == 0
+    with pytest.raises(RuntimeError, match="Start time cannot be later than stop time"):
+        cmtj.stepDriver(0, 1, 2.0, 1.0)
+
+
+def test_custom_driver_contract():
+    driver = ScalarDriver.getCustomDriver(lambda t: math.sqrt(t))
+    assert driver.getCurrentScalarValue(1e-9) == math.sqrt(1e-9)
+
+    def faulty(t):
+        raise ValueError("Intentional exception")
+
+    with pytest.raises(RuntimeError):
+        ScalarDriver.getCustomDriver(faulty).getCurrentScalarValue(1e-9)
+
+    def no_arg():
+        return 0.0
+
+    with pytest.raises(RuntimeError):
+        ScalarDriver.getCustomDriver(no_arg)
+
+
+def test_sanity_errors():
+    with pytest.raises(ValueError, match="Layers must have unique ids!"):
+        Junction([_layer("free"), _layer("free")])
+    with pytest.raises(ValueError, match="Passed a zero length Layer vector!"):
+        Junction([])
+    with pytest.raises(ValueError, match="must have a pinning"):
+        Junction([_layer()], 100, 200)
+    with pytest.raises(ValueError, match="supports only bilayers"):
+        Junction([_layer("a"), _layer("b"), _layer("c")], 100, 200)
+    with pytest.raises(ValueError, match="must be of the same size"):
+        Junction([_layer("a")], [1, 2], [1], [1], [1], [1], [1], [1])
+    with pytest.raises(RuntimeError, match="zero vector"):
+        _layer(mag=CVector(0, 0, 0))
+
+
+def test_junction_setters_and_errors():
+    l = _layer()
+    l.setReferenceLayer(CVector(1, 0, 0))
+    j = Junction([l], 100, 200)
+    assert j.Rtag == "R"
+    with pytest.raises(RuntimeError, match="Failed to find a layer with a given id: nope!"):
+        j.setLayerAnisotropyDriver("nope", constantDriver(1))
+    with pytest.raises(RuntimeError, match="Failed to find a layer with a given id nope!"):
+        j.getLayer("nope")
+    j2 = Junction([_layer("a"), _layer("b")], 100, 200)
+    assert j2.Rtag == "R_a_b"
+    j2.setIECDriver("b", "a", constantDriver(1e-3))  # order irrelevant
+    with pytest.raises(RuntimeError, match="Failed to match the layer order"):
+        j2.setIECDriver("a", "c", constantDriver(1e-3))
+    j2.setLayerMagnetisation("a", CVector(0, 3, 4))
+    assert j2.getLayerMagnetisation("a") == CVector(0, 0.6, 0.8)
+    assert j2.getMagnetoresistance()[0] == 100 + ((200 - 100) / 2.0) * (1.0 - 0.8)
+    assert Junction([_layer("a")]).getLayerIds() == ["a"]
+    with pytest.raises(RuntimeError, match="not supported for this structure"):
+        Junction([_layer("a")]).getMagnetoresistance()
+
+
+def test_layer_copy_semantics():
+    l = _layer()
+    j = Junction([l])
+    l.setMagnetisation(CVector(1, 0, 0))
+    assert j.getLayerMagnetisation("free") == CVector(0, 0, 1)
+    assert _layer(mag=CVector(0, 0, 0.5)).mag == CVector(0, 0, 0.5)  # ctor keeps |m| != 1
+
+
+def test_sot_layer_misuse():
+    layer = Layer.createSOTLayer(id="free", mag=CVector(0, 0, 1), anis=CVector(0, 0, 1), Ms=1, thickness=2e-9,
+                                 cellSurface=1e-18, demagTensor=[CVector(0, 0, 0)] * 3, damping=0.01)
+    with pytest.raises(RuntimeError):
+        layer.setFieldLikeTorqueDriver(constantDriver(0.1))
+    with pytest.raises(RuntimeError):
+        layer.setDampingLikeTorqueDriver(constantDriver(0.1))
+    stt = Layer.createSTTLayer(id="s", mag=CVector(0, 0, 1), anis=CVector(0, 0, 1), Ms=1, thickness=2e-9,
+                               cellSurface=1e-18, demagTensor=[CVector(0, 0, 0)] * 3)
+    with pytest.raises(RuntimeError, match="includeSTT"):
+        stt.setFieldLikeTorqueDriver(constantDriver(0.1))
+
+
+def test_reference_layers():
+    layer = _layer()
+    layer.setReferenceLayer(CVector(1, 0, 0))
+    assert layer.getReferenceLayer() == CVector(1, 0, 0)
+    layer.setSecondaryReferenceLayer(CVector(0, 1, 0))
+    assert layer.getSecondaryReferenceLayer() == CVector(0, 1, 0)
+    fresh = _layer()
+    with pytest.raises(RuntimeError, match="Cannot set fixed polarisation layer to 0"):
+        fresh.setReferenceLayer(cmtj.Reference.fixed)
+
+
+def test_constants_runtime_change():
+    pc = cmtj.constants.PhysicalConstants
+    try:
+        assert pc.gyromagnetic_ratio() == 220880.0
+        pc.set_gyromagnetic_ratio(300000.0)
+        assert pc.gyromagnetic_ratio() == 300000.0
+        pc.set_boltzmann_constant(1.5e-23)
+        assert pc.boltzmann_constant() == 1.5e-23
+    finally:
+        pc.resetToDefaults()
+    assert pc.gyromagnetic_ratio() == 220880.0
+    assert pc.hbar() == 6.62607015e-34 / (2.0 * math.pi)
+
+
+def test_enums_exported():
+    assert cmtj.RK4 == cmtj.SolverMode.RK4 and cmtj.EulerHeun == 0 and cmtj.Heun == 3
+    assert cmtj.xaxis == cmtj.Axis.xaxis and cmtj.fixed == cmtj.Reference.fixed
+    assert int(cmtj.custom) == 100
+
+
+def test_run_plan_matches_reference_truncation():
+    from cmtj_gb300.engine import plan_run
+    p = plan_run(10e-9, 1e-13, 1e-13)
+    assert p.total_iterations == int(10e-9 / 1e-13) and p.write_every == 1
+    p = plan_run(4e-9, 1e-13, 1e-12)
+    assert p.write_every == int(1e-12 / 1e-13)
+    with pytest.raises(RuntimeError, match="cannot be larger than write frequency"):
+        plan_run(1e-9, 1e-12, 1e-13)
