@@ -1,0 +1,422 @@
+"""Benchmark of the macrospin hot path on one GB300.
+
+Workload (value, e2e): batched FP32 PIMM -- 262,144 independent 2-layer
+junctions (512 fields over +-600 kA/m along x x 512 seeded draws of
+Ku(free) ~ U[1e5, 6e5] J/m^3 and J ~ U[-1e-4, 1e-4] J/m^2), a 1 ps
+1 kA/m Oersted step along x, 5 ns at dt = 1e-13 s (50,000 RK4 steps), the
+Ms*t-weighted m_x logged every 1 ps, and a 4096-point device FFT of each
+junction's last 4096 samples.  One step = one pass of that whole batch.
+
+Metric: layer-steps/s of the FP32 batched form (one layer-step = one
+integration step of one layer), beside the FP64 plain form (the reference's
+arithmetic on the GPU, one launch per solve and one launch per batch), the
+FP32-vs-FP64 max|dm| on a sample of the same junctions, and the reference's
+CPU path (the oracle restatement, bit-identical to the reference) on the
+host cores.
+
+    python bench.py [--steps K] [--warmup W] [--gpus N] [--impl reference]
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+N_H, N_DRAW = 512, 512
+DT = 1e-13
+TOTAL = 5e-9
+LOG_EVERY = 10       # 1 ps
+N_FFT = 4096
+MAX_FREQ = 80e9      # PIMM_procedure default max_frequency (procedures.py:52)
+
+METRIC = "layer-steps/s FP32-batched vs FP64-plain @max|Δm|≤1e-4; p50/p99 request latency"
+UNIT = "layer-steps/s"
+WORKLOAD = ("batched FP32 PIMM: 262144 2-layer MTJs (512 H x 512 seeded Ku/J draws), 1 ps 1 kA/m Oersted "
+            "step, 5 ns @ dt=1e-13 (RK4), m_x mix logged every 1 ps, 4096-pt device FFT")
+
+
+def dist_info():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed
+    region (every 200 ms)."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) == 7:
+                self.rows.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows for k in range(4) if r[3 + k].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def flops_per_layer_step():
+    """FLOPs of one layer-step of the config-1 junction, counted by running
+    the oracle (the reference's arithmetic) on a counting scalar type."""
+    import cases  # noqa: F401
+    import oracle_harness
+    import cmtj_gb300 as cm
+    j, _ = __import__("cases").config0_point(cm, hx=-3e5, total=1e-11)
+    j.setLayerOerstedFieldDriver("all", cm.AxialDriver(cm.stepDriver(0, 1e3, 0, 1e-12), cm.NullDriver(),
+                                                        cm.NullDriver()))
+    steps = 200
+    c = oracle_harness.count_flops(j, steps * DT, DT, DT * LOG_EVERY)
+    return float(c.sum()) / (steps * 2), [int(x) for x in c]
+
+
+def build_workload(n_h=N_H, n_draw=N_DRAW):
+    from cmtj_gb300 import batch, sweeps
+    spec, n_steps = sweeps.pimm_config(n_h=n_h, n_draw=n_draw, dt=DT, total=TOTAL)
+    low = batch.lower(spec, DT, n_steps)
+    return spec, low, n_steps
+
+
+def fft_bins():
+    freqs = np.fft.fftfreq(N_FFT, DT * LOG_EVERY)[: N_FFT // 2]
+    hi = int(np.searchsorted(freqs, MAX_FREQ, side="right"))
+    return 1, hi
+
+
+def run_reference_arm(args):
+    """The reference's CPU path (oracle restatement, bit-identical to the
+    reference build; the reference itself does not build on the GPU machine)
+    on all host cores, on bounded samples of the same workload."""
+    import oracle_harness
+    from cmtj_gb300 import _lower, sweeps
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    n = cores * 2
+    steps = 2000
+    spec, _ = sweeps.pimm_config(n_h=n, n_draw=1, dt=DT, total=TOTAL)
+    js = spec_to_junctions(spec)
+    vals = []
+    for it in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        oracle_harness.run_oracle(js, steps * DT, DT, DT * LOG_EVERY, threads=cores)
+        el = time.perf_counter() - t0
+        if it >= args.warmup:
+            vals.append(n * steps * 2 / el)
+    v = float(np.median(vals))
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * n * steps * 2 / v, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": WORKLOAD, "sample": "%d junctions x %d steps per step" % (n, steps)},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": "%d config-1 junctions x %d RK4 steps, one oracle pass per step" % (n, steps)},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def spec_to_junctions(spec):
+    """Junction objects equal to the first rows of a pimm_config spec."""
+    import cmtj_gb300 as cm
+    import cases
+    out = []
+    for k in range(spec.n):
+        j, _ = cases.config0_point(cm, hx=float(spec.Hc[k, 0, 0]), total=1e-9)
+        j.setLayerAnisotropyDriver("free", cm.constantDriver(float(spec.K[k, 0])))
+        j.setIECDriver("free", "ref", cm.constantDriver(float(spec.Jt[k, 0])))
+        j.setLayerOerstedFieldDriver("all", cm.AxialDriver(cm.stepDriver(0, 1e3, 0, 1e-12), cm.NullDriver(),
+                                                            cm.NullDriver()))
+        out.append(j)
+    return out
+
+
+def cpu_baseline(budget_s=12.0):
+    import oracle_harness
+    from cmtj_gb300 import sweeps
+    cores = os.cpu_count() or 1
+    n = cores * 4
+    steps = 1000
+    spec, _ = sweeps.pimm_config(n_h=n, n_draw=1, dt=DT, total=TOTAL)
+    js = spec_to_junctions(spec)
+    t0 = time.perf_counter()
+    oracle_harness.run_oracle(js, steps * DT, DT, DT * LOG_EVERY, threads=cores)
+    el = time.perf_counter() - t0
+    rate = n * steps * 2 / el
+    # scale the sample up to about budget_s of CPU work
+    steps2 = int(min(50000, max(steps, steps * budget_s / max(el, 1e-3))))
+    js = spec_to_junctions(spec)
+    t0 = time.perf_counter()
+    oracle_harness.run_oracle(js, steps2 * DT, DT, DT * LOG_EVERY, threads=cores)
+    el = time.perf_counter() - t0
+    rate = n * steps2 * 2 / el
+    return {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "%d config-1 junctions x %d RK4 steps on %d threads (%.1f s)" % (n, steps2, cores, el)}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--small", action="store_true", help="8192-junction workload (profiling)")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference_arm(args)
+        return
+
+    import torch
+    from cmtj_gb300 import _abi, batch, engine
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    lib = engine.require_gpu()
+    stream = torch.cuda.current_stream()
+
+    n_h, n_draw = (64, 128) if args.small else (N_H, N_DRAW)
+    spec, low, n_steps = build_workload(n_h, n_draw)
+    n = spec.n
+    layer_steps = float(n) * n_steps * 2
+    run = batch.BatchRun(low, DT, batch.SolverMode.RK4, batch.LOG_MIX, LOG_EVERY, log_axis=0)
+    samples = int(run.samples[0])
+    row_stride = int(run.log_pad[0])
+    b_lo, b_hi = fft_bins()
+    d_spec = torch.empty((n, b_hi - b_lo), dtype=torch.float32, device="cuda")
+    state0 = torch.zeros_like(run.d_s)
+
+    def spectrum():
+        rc = lib.cmtj_spectrum_f32(engine.ptr(run.d_log), row_stride, n, samples, N_FFT, b_lo, b_hi,
+                                   engine.ptr(d_spec), engine.stream_ptr())
+        _abi.check(rc, lib)
+
+    def one_step():
+        run.d_s.copy_(state0)
+        run.launch()
+        spectrum()
+
+    # --- device-resident timing (value)
+    for _ in range(args.warmup):
+        one_step()
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2 * args.steps + 2)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    kern_ms = []
+    fft_ms = []
+    with ClockSampler(local) as clk:
+        t_start = torch.cuda.Event(enable_timing=True)
+        t_end = torch.cuda.Event(enable_timing=True)
+        t_start.record(stream)
+        for k in range(args.steps):
+            run.d_s.copy_(state0)
+            ev[2 * k].record(stream)
+            run.launch()
+            ev[2 * k + 1].record(stream)
+            spectrum()
+            e = torch.cuda.Event(enable_timing=True)
+            e.record(stream)
+            fft_ms.append(e)
+        t_end.record(stream)
+        torch.cuda.synchronize()
+    elapsed = t_start.elapsed_time(t_end) / 1e3
+    if world > 1:
+        t = torch.tensor([elapsed], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        elapsed = float(t.item())
+    kern_ms = [ev[2 * k].elapsed_time(ev[2 * k + 1]) for k in range(args.steps)]
+    fft_only = [ev[2 * k + 1].elapsed_time(fft_ms[k]) for k in range(args.steps)]
+    value = world * layer_steps * args.steps / elapsed
+    clocks = clk.summary()
+
+    st = run.state()
+    ok = bool(np.all(st["status"] == 0) and np.all(st["step"] == n_steps))
+
+    # --- end to end through the C ABI with host buffers (pinned): H2D of
+    # the junction/layer records, the batched run, the device FFT, D2H of
+    # the spectra and final states
+    h_j = torch.from_numpy(low.junctions.view(np.uint8).copy()).pin_memory()
+    h_l = torch.from_numpy(low.layers.view(np.uint8).copy()).pin_memory()
+    h_spec = torch.empty(d_spec.shape, dtype=torch.float32).pin_memory()
+    h_state = torch.empty(run.d_s.shape, dtype=run.d_s.dtype).pin_memory()
+
+    def e2e_step():
+        run.d_j.copy_(h_j, non_blocking=True)
+        run.d_l.copy_(h_l, non_blocking=True)
+        run.d_s.copy_(state0)
+        run.launch()
+        spectrum()
+        h_spec.copy_(d_spec, non_blocking=True)
+        h_state.copy_(run.d_s, non_blocking=True)
+
+    for _ in range(max(1, args.warmup // 2)):
+        e2e_step()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for _ in range(args.steps):
+        e2e_step()
+    b.record(stream)
+    torch.cuda.synchronize()
+    e2e_s = a.elapsed_time(b) / 1e3
+    if world > 1:
+        t = torch.tensor([e2e_s], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = {"value": world * layer_steps * args.steps / e2e_s, "unit": UNIT,
+           "h2d_bytes_per_step": int(h_j.numel() + h_l.numel()),
+           "d2h_bytes_per_step": int(h_spec.numel() * 4 + h_state.numel())}
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "junctions_per_gpu": n, "layers": 2, "steps_per_junction": n_steps,
+                       "parallelism": "replicas" if world > 1 else "single",
+                       "l2": "inputs and logs (5.2 GB) larger than L2", "all_ok": ok},
+            "e2e": e2e, "clocks": clocks,
+            "gpu_launches": args.steps * 2}
+
+    if rank == 0 and not args.small:
+        extra = measure_rest(run, low, spec, n_steps, kern_ms, fft_only, lib)
+        line.update(extra)
+        f64 = line["fp64_plain"]
+        f64["fp32_over_fp64_per_solve"] = value / f64["per_solve_launch_layer_steps_per_s"]
+        f64["fp32_over_fp64_batched"] = value / f64["batched_launch_layer_steps_per_s"]
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def measure_rest(run, low, spec, n_steps, kern_ms, fft_ms, lib):
+    """Roofline, FP64 plain comparisons, FP32-vs-FP64 accuracy, CPU baseline."""
+    import torch
+    from cmtj_gb300 import batch, engine
+    out = {}
+    # roofline of the dominant kernel (the FP32 batch integrator)
+    fpls, fcount = flops_per_layer_step()
+    n = spec.n
+    kavg = float(np.mean(kern_ms)) / 1e3
+    achieved = fpls * n * n_steps * 2 / kavg / 1e12
+    from cmtj_gb300 import build as cbuild
+    import ctypes
+    probe = ctypes.CDLL(cbuild.build_probe())
+    probe.cmtj_probe_fp32_peak.restype = ctypes.c_double
+    probe.cmtj_probe_fp32_peak.argtypes = [ctypes.c_int]
+    peak = probe.cmtj_probe_fp32_peak(5) / 1e12
+    out["roofline"] = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                       "frac": achieved / peak, "traffic": None,
+                       "flop_per_layer_step": fpls, "flop_breakdown_add_mul_div_sqrt_trans": fcount,
+                       "peak_source": "measured FP32 FMA probe on this GPU (MEASURED_PEAKS.json has no FP32 figure)",
+                       "kernel_ms_avg": kavg * 1e3, "fft_ms_avg": float(np.mean(fft_ms))}
+
+    # FP64 plain form and accuracy on a sample of the same junctions
+    rows = np.arange(0, n, max(1, n // 256))[:256]
+    plan = engine.plan_run(n_steps * DT, DT, DT * LOG_EVERY)
+    from cmtj_gb300.core import SolverMode
+    # one launch per solve (2 solves of 2000 steps, 1 thread each)
+    solo = spec_to_junctions_rows(spec, rows[:2])
+    plan_s = engine.plan_run(2000 * DT, DT, DT * LOG_EVERY)
+    engine.run_junctions([spec_to_junctions_rows(spec, rows[:1])[0]], engine.plan_run(10 * DT, DT, DT),
+                         SolverMode.RK4)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for j in solo:
+        engine.run_junctions([j], plan_s, SolverMode.RK4)
+    torch.cuda.synchronize()
+    el = time.perf_counter() - t0
+    fp64_solo = len(solo) * 2000 * 2 / el
+    # one launch for the 256 sampled solves over the full duration
+    js = spec_to_junctions_rows(spec, rows)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    engine.run_junctions(js, plan, SolverMode.RK4)
+    torch.cuda.synchronize()
+    el = time.perf_counter() - t0
+    fp64_batch = len(rows) * n_steps * 2 / el
+    # FP32 vs FP64 on those junctions: final m and the logged m_x mix
+    st = run.state()
+    m32 = st["m"][rows, :2, :].astype(np.float64)
+    m64 = np.stack([[[l.mag.x, l.mag.y, l.mag.z] for l in j.layers] for j in js])
+    dm_final = float(np.max(np.abs(m32 - m64)))
+    log32 = run.d_log.cpu().numpy()
+    dmix = 0.0
+    for q, k in enumerate(rows):
+        lg = js[q].getLogArrays()
+        w = spec.mix_w[k, :2]
+        mix64 = w[0] * lg["free_mx"] + w[1] * lg["ref_mx"]
+        mix32 = run.log_of(int(k), log32)[:, 0]
+        dmix = max(dmix, float(np.max(np.abs(mix32 - mix64))))
+    out["fp64_plain"] = {"per_solve_launch_layer_steps_per_s": fp64_solo,
+                         "batched_launch_layer_steps_per_s": fp64_batch,
+                         "sample": "2 solo launches x 2000 steps; one launch of %d junctions x %d steps"
+                                   % (len(rows), n_steps)}
+    out["accuracy"] = {"max_abs_dm_final_vs_fp64": dm_final, "max_abs_dmix_logged_vs_fp64": dmix,
+                       "tolerance": 1e-4, "sample_junctions": 256, "pass": max(dm_final, dmix) <= 1e-4}
+    out["cpu_baseline"] = cpu_baseline()
+    return out
+
+
+def spec_to_junctions_rows(spec, rows):
+    """Junction objects for the given rows of the PIMM spec."""
+    import cmtj_gb300 as cm
+    import cases
+    out = []
+    for k in rows:
+        j, _ = cases.config0_point(cm, hx=float(spec.Hc[k, 0, 0]), total=1e-9)
+        j.setLayerAnisotropyDriver("free", cm.constantDriver(float(spec.K[k, 0])))
+        j.setIECDriver("free", "ref", cm.constantDriver(float(spec.Jt[k, 0])))
+        j.setLayerOerstedFieldDriver("all", cm.AxialDriver(cm.stepDriver(0, 1e3, 0, 1e-12), cm.NullDriver(),
+                                                            cm.NullDriver()))
+        out.append(j)
+    return out
+
+
+if __name__ == "__main__":
+    main()

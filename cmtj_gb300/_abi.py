@@ -99,6 +99,9 @@ PROTOTYPES = {
     "cmtj_log_width": (ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
     "cmtj_struct_sizes": (ctypes.c_int, [_P, _I32]),
     "cmtj_run_simulation_f64": (ctypes.c_int, [_P, _I32, _P, _P, _P, _P, _P, _P]),
+    "cmtj_batch_run_f32": (ctypes.c_int, [_P, _P, _P, _P, _I32, _I32, _I32, _P, _P, _P, _I32, _P]),
+    "cmtj_batch_variant_f32": (ctypes.c_int, [_I32, _I32, _I32]),
+    "cmtj_spectrum_f32": (ctypes.c_int, [_P, ctypes.c_int64, _I32, _I32, _I32, _I32, _I32, _P, _P]),
 }
 
 _lib = None
@@ -130,10 +133,13 @@ def load(path=None):
 
 
 def check_layout(lib):
-    n = len(STRUCT_SIZES)
+    from .batch import STRUCT_SIZES_F32
+    sizes = dict(STRUCT_SIZES)
+    sizes.update(STRUCT_SIZES_F32)
+    n = len(sizes)
     buf = (ctypes.c_int32 * n)()
     lib.cmtj_struct_sizes(ctypes.cast(buf, _P), n)
-    for (name, size), got in zip(STRUCT_SIZES.items(), buf):
+    for (name, size), got in zip(sizes.items(), buf):
         if size != got:
             raise RuntimeError("ABI mismatch for %s: numpy %d bytes, library %d bytes" % (name, size, got))
     if lib.cmtj_abi_version() != 1:

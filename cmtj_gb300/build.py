@@ -23,7 +23,16 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + INCLUD
 UNITS = {
     "abi.cu": [],
     "plain_f64.cu": ["--fmad=false"],
+    "batch_f32.cu": [],
+    "batch_f32_l1.cu": [],
+    "batch_f32_l2.cu": [],
+    "batch_f32_l3.cu": [],
+    "batch_f32_l4.cu": [],
+    "reduce.cu": [],
 }
+# measurement-only probe library (FP32 FMA throughput), not the product
+PROBE_UNITS = {"probe_peak.cu": []}
+PROBE_LIB = os.path.join(BUILD, "libcmtj_probe.so")
 
 
 def _nvcc():
@@ -46,13 +55,15 @@ def _stale(target, deps):
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build(verbose=False, extra_flags=()):
+def build(verbose=False, extra_flags=(), units=None, lib=None):
+    units = UNITS if units is None else units
+    lib = LIB if lib is None else lib
     os.makedirs(BUILD, exist_ok=True)
     nvcc = _nvcc()
     hdrs = _headers() + [os.path.abspath(__file__)]
     objs = []
     jobs = []
-    for unit, flags in UNITS.items():
+    for unit, flags in units.items():
         src = os.path.join(CSRC, unit)
         obj = os.path.join(BUILD, unit.replace(".cu", ".o"))
         objs.append(obj)
@@ -71,13 +82,18 @@ def build(verbose=False, extra_flags=()):
 
     with concurrent.futures.ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
         list(ex.map(run, jobs))
-    if jobs or _stale(LIB, objs):
-        cmd = [nvcc, *ARCH, "-shared", "-o", LIB + ".tmp", *objs]
+    if jobs or _stale(lib, objs):
+        cmd = [nvcc, *ARCH, "-shared", "-o", lib + ".tmp", *objs]
         run(cmd)
-        os.replace(LIB + ".tmp", LIB)
-    return LIB
+        os.replace(lib + ".tmp", lib)
+    return lib
+
+
+def build_probe(verbose=False):
+    return build(verbose=verbose, units=PROBE_UNITS, lib=PROBE_LIB)
 
 
 if __name__ == "__main__":
     extra = sys.argv[1:]
     print(build(verbose=True, extra_flags=extra))
+    print(build_probe(verbose=True))

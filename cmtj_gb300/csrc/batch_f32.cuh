@@ -1,0 +1,664 @@
+// FP32 batched form: persistent, work-stealing macrospin integrator.
+//
+// Each thread owns one junction at a time: its magnetisations, RK4
+// accumulators, driver waves and reductions live in registers.  Layers are
+// unrolled at compile time (L = 1..4), the solver and the set of active
+// field/torque terms (FEAT) are template parameters, so a partition of
+// uniform junctions runs straight-line FP32 FMA code.  When a junction
+// ends, its lane takes the next one from a warp-aggregated atomic ticket,
+// so uneven durations keep every lane busy until the queue drains.
+//
+// Arithmetic (core/junction.hpp:580-831, 1017-1041, 1709-1815 of the
+// reference) is restated with constants folded on the host: the field terms
+// arrive pre-divided by Ms, Ms*t and mu0 (cmtj_f32_layer_t), |m| is
+// renormalised with rsqrt every step, driver time enters through integer
+// step counts and Q0.64 phases (no FP32 time accumulator).
+//
+// Logs are staged per thread in shared memory and written to global memory
+// with cp.async.bulk (TMA bulk copy, shared::cta -> global), one copy per
+// completed tile of log_tile samples.
+#pragma once
+#include "common.cuh"
+#include "philox.cuh"
+
+namespace cmtjf {
+
+struct F3 {
+  float x, y, z;
+};
+__device__ __forceinline__ F3 f3(float x, float y, float z) {
+  F3 r;
+  r.x = x;
+  r.y = y;
+  r.z = z;
+  return r;
+}
+__device__ __forceinline__ F3 operator+(F3 a, F3 b) { return f3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ F3 operator-(F3 a, F3 b) { return f3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ F3 operator*(F3 a, float s) { return f3(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ F3 fma3(F3 a, float s, F3 b) { return f3(fmaf(a.x, s, b.x), fmaf(a.y, s, b.y), fmaf(a.z, s, b.z)); }
+__device__ __forceinline__ float dot(F3 a, F3 b) { return fmaf(a.x, b.x, fmaf(a.y, b.y, a.z * b.z)); }
+__device__ __forceinline__ F3 cross(F3 a, F3 b) {
+  return f3(fmaf(a.y, b.z, -a.z * b.y), fmaf(a.z, b.x, -a.x * b.z), fmaf(a.x, b.y, -a.y * b.x));
+}
+__device__ __forceinline__ F3 ld3(const float *p) { return f3(p[0], p[1], p[2]); }
+__device__ __forceinline__ F3 renorm(F3 m) { return m * rsqrtf(dot(m, m)); }
+__device__ __forceinline__ F3 matvec(const float *t, F3 m) {
+  return f3(fmaf(t[0], m.x, fmaf(t[1], m.y, t[2] * m.z)), fmaf(t[3], m.x, fmaf(t[4], m.y, t[5] * m.z)),
+            fmaf(t[6], m.x, fmaf(t[7], m.y, t[8] * m.z)));
+}
+
+// Neumaier compensated accumulation.
+__device__ __forceinline__ void kadd(float &s, float &c, float v) {
+  const float t = s + v;
+  c += (fabsf(s) >= fabsf(v)) ? ((s - t) + v) : ((v - t) + s);
+  s = t;
+}
+
+template <int FEAT> struct Feat {
+  static constexpr bool full_demag = (FEAT & CMTJ_FEAT_FULL_DEMAG) != 0;
+  static constexpr bool dipole = (FEAT & CMTJ_FEAT_DIPOLE) != 0;
+  static constexpr bool idmi = (FEAT & CMTJ_FEAT_IDMI) != 0;
+  static constexpr bool k2 = (FEAT & CMTJ_FEAT_K2) != 0;
+  static constexpr bool stt = (FEAT & CMTJ_FEAT_STT) != 0;
+  static constexpr bool sot = (FEAT & CMTJ_FEAT_SOT) != 0;
+  static constexpr bool waves = (FEAT & CMTJ_FEAT_WAVES) != 0;
+  static constexpr bool swaves = (FEAT & CMTJ_FEAT_SCALAR_WAVES) != 0;
+  static constexpr bool twaves = waves && (stt || sot);  // current / torque waves
+};
+
+// Per-layer constants held in registers for the life of a junction.
+template <int FEAT> struct LayerP {
+  F3 a;
+  float kc, k2c;
+  float N[9];
+  float Db[9], Dt[9];
+  F3 h0;
+  float jb, jt, j2b, j2t;
+  F3 dmib, dmit;
+  float gam, alpha;
+  F3 ref, ref2;
+  int rtype, flags;
+  float sttc, sttp, sttl, sttb, sttk, i0, fl0, dl0, fl20, dl20;
+  float sigc, t0;
+  uint32_t seed_lo, seed_hi;
+  uint64_t nstep0;
+
+  __device__ __forceinline__ void load(const cmtj_f32_layer_t &r) {
+    using F = Feat<FEAT>;
+    a = ld3(r.anis);
+    kc = r.kc;
+    k2c = F::k2 ? r.k2c : 0.f;
+    if (F::full_demag) {
+#pragma unroll
+      for (int q = 0; q < 9; ++q) N[q] = r.demag[q];
+    } else {
+      N[0] = r.demag[0];
+      N[4] = r.demag[4];
+      N[8] = r.demag[8];
+    }
+    if (F::dipole) {
+#pragma unroll
+      for (int q = 0; q < 9; ++q) {
+        Db[q] = r.dip_b[q];
+        Dt[q] = r.dip_t[q];
+      }
+    }
+    h0 = ld3(r.h0);
+    jb = r.jb;
+    jt = r.jt;
+    j2b = r.j2b;
+    j2t = r.j2t;
+    if (F::idmi) {
+      dmib = ld3(r.dmi_b);
+      dmit = ld3(r.dmi_t);
+    }
+    gam = r.gam;
+    alpha = r.alpha;
+    rtype = r.ref_type;
+    flags = r.flags;
+    if (F::stt || F::sot) {
+      ref = ld3(r.ref);
+      ref2 = ld3(r.ref2);
+      sttc = r.stt_c;
+      sttp = r.stt_p;
+      sttl = r.stt_l;
+      sttb = r.stt_beta;
+      sttk = r.stt_kappa;
+      i0 = r.i0;
+      fl0 = r.fl0;
+      dl0 = r.dl0;
+      fl20 = r.fl20;
+      dl20 = r.dl20;
+    }
+    sigc = r.sig_c;
+    t0 = r.t0;
+    seed_lo = r.seed_lo;
+    seed_hi = r.seed_hi;
+    nstep0 = ((uint64_t)r.noise_step_hi << 32) | r.noise_step_lo;
+  }
+};
+
+// Time-dependent additions to one layer's terms at one stage time.  Only
+// the targets the variant supports are kept (the host routes any other wave
+// to a variant that has them), so unused fields cost no registers.
+template <int FEAT> struct Delta {
+  using F = Feat<FEAT>;
+  F3 dH;
+  float dK, dK2, dJb, dJt, dJ2b, dJ2t, dI, dFL, dDL, dFL2, dDL2, dT;
+  __device__ __forceinline__ void clear() {
+    dH = f3(0.f, 0.f, 0.f);
+    dK = dK2 = dJb = dJt = dJ2b = dJ2t = dI = dFL = dDL = dFL2 = dDL2 = dT = 0.f;
+  }
+  __device__ __forceinline__ void add(int target, float v) {
+    if (target == CMTJ_TGT_HX) dH.x += v;
+    else if (target == CMTJ_TGT_HY) dH.y += v;
+    else if (target == CMTJ_TGT_HZ) dH.z += v;
+    else if (F::twaves && target == CMTJ_TGT_I) dI += v;
+    else if (F::twaves && F::sot && target == CMTJ_TGT_FL) dFL += v;
+    else if (F::twaves && F::sot && target == CMTJ_TGT_DL) dDL += v;
+    else if (F::twaves && F::sot && target == CMTJ_TGT_FL2) dFL2 += v;
+    else if (F::twaves && F::sot && target == CMTJ_TGT_DL2) dDL2 += v;
+    else if (F::swaves) {
+      switch (target) {
+      case CMTJ_TGT_K: dK += v; break;
+      case CMTJ_TGT_K2: dK2 += v; break;
+      case CMTJ_TGT_JB: dJb += v; break;
+      case CMTJ_TGT_JT: dJt += v; break;
+      case CMTJ_TGT_J2B: dJ2b += v; break;
+      case CMTJ_TGT_J2T: dJ2t += v; break;
+      case CMTJ_TGT_T: dT += v; break;
+      default: break;
+      }
+    }
+  }
+};
+
+// One time-dependent driver in registers.
+template <int L> struct WaveR {
+  int target, kind;
+  float amp[L];
+  float p0, p1, p2;
+  uint32_t thr32;
+  int32_t i0;
+  uint64_t ph0, dph, dphh;
+  uint32_t on0, off0, on1, off1, on2, off2;
+
+  __device__ __forceinline__ void load(const cmtj_wave_t &w) {
+    target = w.target;
+    kind = w.kind;
+#pragma unroll
+    for (int l = 0; l < L; ++l) amp[l] = ((w.layer_mask >> l) & 1) ? w.amp : 0.f;
+    p0 = w.p0;
+    p1 = w.p1;
+    p2 = w.p2;
+    thr32 = w.thr32;
+    i0 = w.i0;
+    ph0 = w.ph0;
+    dph = w.dph;
+    dphh = w.dph_half;
+    on0 = w.on[0];
+    off0 = w.off[0];
+    on1 = w.on[1];
+    off1 = w.off[1];
+    on2 = w.on[2];
+    off2 = w.off[2];
+  }
+
+  // Unit waveform at step i, stage s (0: t, 1: t + dt/2, 2: t + dt).
+  __device__ __forceinline__ float unit(uint32_t i, int s, float dtf) const {
+    switch (kind) {
+    case CMTJ_WAVE_SINE:
+    case CMTJ_WAVE_POSINE:
+    case CMTJ_WAVE_HALFSINE: {
+      const uint64_t ph = ph0 + (uint64_t)i * dph + (s == 0 ? 0ull : (s == 1 ? dphh : dph));
+      const float x = (float)(uint32_t)(ph >> 40) * 5.9604644775390625e-08f;  // 2^-24
+      const float v = sinpif(2.0f * x);
+      if (kind == CMTJ_WAVE_POSINE) return fabsf(v);
+      if (kind == CMTJ_WAVE_HALFSINE) return (p0 * v <= 0.f) ? v : 0.f;
+      return v;
+    }
+    case CMTJ_WAVE_PULSE: {
+      const uint64_t ph = ph0 + (uint64_t)i * dph + (s == 0 ? 0ull : (s == 1 ? dphh : dph));
+      return ((uint32_t)(ph >> 32) <= thr32) ? 1.f : 0.f;
+    }
+    case CMTJ_WAVE_STEP: {
+      const uint32_t on = s == 0 ? on0 : (s == 1 ? on1 : on2);
+      const uint32_t off = s == 0 ? off0 : (s == 1 ? off1 : off2);
+      return (i >= on && i <= off) ? 1.f : 0.f;
+    }
+    default: {
+      const float tau = fmaf((float)((int32_t)i - i0), dtf, fmaf((float)s, 0.5f * dtf, p2));
+      if (kind == CMTJ_WAVE_TRAPEZOID) {
+        if (tau < 0.f) return 0.f;
+        if (tau <= p0) return tau / p0;
+        if (tau <= p0 + p1) return 1.f;
+        if (tau <= 2.f * p0 + p1) return 1.f - (tau - (p0 + p1)) / p0;
+        return 0.f;
+      }
+      if (kind == CMTJ_WAVE_GAUSSIMPULSE) {
+        const float u = tau * p0;
+        return __expf(-0.5f * u * u);
+      }
+      return 0.5f * (1.f + erff(tau * p0));  // GAUSSSTEP
+    }
+    }
+  }
+};
+
+// Effective field + LL torque of one layer (junction.hpp:580-815).
+template <int FEAT, bool HB, bool HT>
+__device__ __forceinline__ F3 rhs(const LayerP<FEAT> &P, F3 m, F3 mb, F3 mt, const Delta<FEAT> &d) {
+  using F = Feat<FEAT>;
+  F3 H = F::waves ? P.h0 + d.dH : P.h0;
+  const float da = dot(P.a, m);
+  float ka = F::swaves ? P.kc + d.dK : P.kc;
+  if (F::k2) ka = fmaf(F::swaves ? P.k2c + d.dK2 : P.k2c, da * da, ka);
+  H = fma3(P.a, ka * da, H);
+  if (HB) {
+    const float cb = fmaf(F::swaves ? P.j2b + d.dJ2b : P.j2b, dot(mb, m), F::swaves ? P.jb + d.dJb : P.jb);
+    H = fma3(mb, cb, H);
+    if (F::idmi) H = H + cross(mb, P.dmib);
+    if (F::dipole) H = H - matvec(P.Db, mb);
+  }
+  if (HT) {
+    const float ct = fmaf(F::swaves ? P.j2t + d.dJ2t : P.j2t, dot(mt, m), F::swaves ? P.jt + d.dJt : P.jt);
+    H = fma3(mt, ct, H);
+    if (F::idmi) H = H + cross(mt, P.dmit);
+    if (F::dipole) H = H - matvec(P.Dt, mt);
+  }
+  if (F::full_demag) {
+    H = H - matvec(P.N, m);
+  } else {
+    H = f3(fmaf(-P.N[0], m.x, H.x), fmaf(-P.N[4], m.y, H.y), fmaf(-P.N[8], m.z, H.z));
+  }
+  const F3 mxH = cross(m, H);
+  F3 acc = fma3(cross(m, mxH), P.alpha, mxH);
+  if (F::stt || F::sot) {
+    F3 p = P.ref;
+    if (P.rtype == CMTJ_REF_TOP) p = HT ? mt : f3(0.f, 0.f, 0.f);
+    else if (P.rtype == CMTJ_REF_BOTTOM) p = HB ? mb : f3(0.f, 0.f, 0.f);
+    else if (P.rtype == CMTJ_REF_NONE) p = f3(0.f, 0.f, 0.f);
+    if (F::stt && (P.flags & CMTJ_F32_STT)) {
+      const float I = F::twaves ? P.i0 + d.dI : P.i0;
+      const float mp = dot(m, p);
+      float eta;
+      if (P.flags & CMTJ_F32_ALT_STT) {
+        eta = __fdividef(P.sttp, fmaf(P.sttl, mp, 1.f));
+      } else {
+        const float l2 = P.sttl * P.sttl;
+        eta = __fdividef(P.sttp * l2, fmaf(l2 - 1.f, mp, l2 + 1.f));
+      }
+      const float s = P.sttc * I * eta;
+      const F3 fl = cross(m, p);
+      const F3 dl = cross(m, fl);
+      // gam * dmdt already carries -gamma/(1+alpha^2); sttc carries 1/(1+alpha^2).
+      return fma3(fl, s * P.sttb, fma3(dl, -s * P.sttk, acc * P.gam));
+    }
+    if (F::sot && (P.flags & CMTJ_F32_SOT)) {
+      float hfl, hdl, hfl2 = 0.f, hdl2 = 0.f;
+      if (P.flags & CMTJ_F32_SOT_STATIC) {
+        const float I = F::twaves ? P.i0 + d.dI : P.i0;
+        hfl = P.fl0 * I;
+        hdl = P.dl0 * I;
+      } else {
+        hfl = F::twaves ? P.fl0 + d.dFL : P.fl0;
+        hdl = F::twaves ? P.dl0 + d.dDL : P.dl0;
+        hfl2 = F::twaves ? P.fl20 + d.dFL2 : P.fl20;
+        hdl2 = F::twaves ? P.dl20 + d.dDL2 : P.dl20;
+      }
+      const F3 cp = cross(m, p);
+      acc = fma3(cp, fmaf(-P.alpha, hdl, hfl), acc);
+      acc = fma3(cross(m, cp), fmaf(P.alpha, hfl, hdl), acc);
+      const F3 cs = cross(m, P.ref2);
+      acc = fma3(cs, fmaf(-P.alpha, hdl2, hfl2), acc);
+      acc = fma3(cross(m, cs), fmaf(P.alpha, hfl2, hdl2), acc);
+    }
+  }
+  return acc * P.gam;
+}
+
+// stochasticTorque (junction.hpp:824-831).
+template <int FEAT>
+__device__ __forceinline__ F3 stoch(const LayerP<FEAT> &P, F3 m, F3 dW) {
+  const F3 th = cross(m, dW);
+  return fma3(cross(m, th), P.alpha, th) * P.gam;
+}
+
+struct Args {
+  const cmtj_f32_junction_t *J;
+  const cmtj_f32_layer_t *Ly;
+  cmtj_f32_state_t *S;
+  const int32_t *order;
+  int32_t n;
+  cmtj_f32_params_t p;
+  float *log;
+  uint32_t *ticket;
+};
+
+__device__ __forceinline__ void bulk_store(float *gdst, const float *ssrc, uint32_t bytes) {
+  // Generic-proxy writes to shared memory must be visible to the async proxy.
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  const uint32_t s = (uint32_t)__cvta_generic_to_shared(ssrc);
+  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(gdst), "r"(s), "r"(bytes)
+               : "memory");
+  asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+__device__ __forceinline__ void bulk_wait_read() {
+  asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+}
+
+// Resistance of one junction: CLASSIC R = Rp + (Rap - Rp)/2 (1 - cos)
+// (junction.hpp:1865-1867, cos against layer 1 or the layer-0 reference),
+// STRIP Rx = 1 / sum_l 1/(Rx0 + AMR_X mx^2 + SMR_X my^2) (1835-1857), SERIES
+// Rx = sum_l (Rx0 + AMR_X mx^2 + SMR_X my^2) (cmtj/utils/resistance.py:121-150).
+template <int L>
+__device__ __forceinline__ float resistance(int mr, const F3 *m, F3 refL1, float Rp, float dR, const float *rx0,
+                                            const float *amx, const float *smx) {
+  if (mr == CMTJ_MR_CLASSIC) return fmaf(dR, 1.f - dot(m[0], L > 1 ? m[L - 1 > 0 ? 1 : 0] : refL1), Rp);
+  float acc = 0.f;
+  if (mr == CMTJ_MR_SERIES) {
+#pragma unroll
+    for (int l = 0; l < L; ++l) acc += fmaf(amx[l], m[l].x * m[l].x, fmaf(smx[l], m[l].y * m[l].y, rx0[l]));
+    return acc;
+  }
+#pragma unroll
+  for (int l = 0; l < L; ++l) acc += 1.f / fmaf(amx[l], m[l].x * m[l].x, fmaf(smx[l], m[l].y * m[l].y, rx0[l]));
+  return 1.f / acc;
+}
+
+template <int L> __device__ __forceinline__ int log_channels(int mode) {
+  return mode == CMTJ_LOG_M ? 3 * L : (mode == CMTJ_LOG_NONE ? 0 : 1);
+}
+
+template <int L, int SOLVER, int FEAT, int NW>
+__global__ void __launch_bounds__(128) k_batch(Args A) {
+  using F = Feat<FEAT>;
+  extern __shared__ __align__(16) float smem[];
+  const int lane = threadIdx.x & 31;
+  const cmtj_f32_params_t &p = A.p;
+  const float dtf = (float)p.dt;
+  const float sqdt = (float)sqrt(p.dt);
+  const int C = log_channels<L>(p.log_mode);
+  const uint32_t T = p.log_tile;
+  float *tile = smem + (size_t)threadIdx.x * T * (C > 0 ? C : 1);
+
+  // junction-lifetime registers
+  LayerP<FEAT> P[L];
+  WaveR<L> W[NW > 0 ? NW : 1];
+  int nw = 0;
+  F3 m[L];
+  int32_t jid = -1;
+  bool retired = false;
+  uint32_t step = 0, end = 0, stop_all = 0, n_logged = 0, tcount = 0, n_red = 0, win = 0;
+  int mr = 0;
+  float Rp = 0.f, dR = 0.f;
+  float rx0[L], amx[L], smx[L], mixw[L];
+  uint64_t vph0 = 0, vdph = 0;
+  float rs = 0.f, rc = 0.f, vs = 0.f, vc = 0.f;
+  float *logrow = nullptr;
+  F3 refL1 = f3(0.f, 0.f, 0.f);
+
+  for (;;) {
+    // ---- refill lanes that have no junction (warp-aggregated ticket)
+    const bool need = (jid < 0) && !retired;
+    const unsigned needmask = __ballot_sync(0xffffffffu, need);
+    if (needmask) {
+      const int leader = __ffs(needmask) - 1;
+      uint32_t base = 0;
+      if (lane == leader) base = atomicAdd(A.ticket, (uint32_t)__popc(needmask));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (need) {
+        const uint32_t k = base + __popc(needmask & ((1u << lane) - 1u));
+        if (k >= (uint32_t)A.n) {
+          retired = true;
+        } else {
+          jid = A.order[k];
+          const cmtj_f32_junction_t &J = A.J[jid];
+          const cmtj_f32_state_t &S = A.S[jid];
+          if (J.n_layers != L) {
+            // wrong partition: never read past this junction's layers
+            A.S[jid].status = CMTJ_STATUS_BAD_INPUT;
+            jid = -1;
+          } else {
+#pragma unroll
+            for (int l = 0; l < L; ++l) P[l].load(A.Ly[J.layer_offset + l]);
+            if (F::waves) {
+              nw = J.n_waves < NW ? J.n_waves : NW;
+#pragma unroll
+              for (int w = 0; w < NW; ++w)
+                if (w < nw) W[w].load(J.waves[w]);
+            }
+            step = S.step;
+            if (step == 0) {
+#pragma unroll
+              for (int l = 0; l < L; ++l) m[l] = ld3(A.Ly[J.layer_offset + l].m);
+            } else {
+#pragma unroll
+              for (int l = 0; l < L; ++l) m[l] = ld3(S.m[l]);
+            }
+            end = J.n_steps;
+            stop_all = (end - step > p.chunk_steps) ? step + p.chunk_steps : end;
+            n_logged = S.n_logged;
+            n_red = S.n_red;
+            rs = S.r_sum;
+            rc = S.r_c;
+            vs = S.v_sum;
+            vc = S.v_c;
+            win = J.win_start;
+            mr = J.mr_mode;
+            Rp = J.Rp;
+            dR = (J.Rap - J.Rp) * 0.5f;
+#pragma unroll
+            for (int l = 0; l < L; ++l) {
+              rx0[l] = J.Rx0[l];
+              amx[l] = J.AMR_X[l];
+              smx[l] = J.SMR_X[l];
+              mixw[l] = J.mix_w[l];
+            }
+            refL1 = ld3(A.Ly[J.layer_offset].ref);
+            vph0 = J.vsd_ph0;
+            vdph = J.vsd_dph;
+            tcount = 0;
+            logrow = A.log + (size_t)J.log_offset * 4u;
+          }
+        }
+      }
+    }
+    // leave only when every lane has drained the queue
+    if (__ballot_sync(0xffffffffu, !retired) == 0) break;
+    if (jid < 0) continue;
+
+    // ---- run a burst of steps
+    const uint32_t burst_end = (stop_all - step > 64u) ? step + 64u : stop_all;
+    for (; step < burst_end; ++step) {
+      if (SOLVER == CMTJ_RK4) {
+        // neighbours frozen at their start-of-step values (junction.hpp:1682-1707)
+        F3 acc[L], kp[L];
+        Delta<FEAT> d[L];
+#pragma unroll
+        for (int st = 0; st < 4; ++st) {
+          const int s = st == 0 ? 0 : (st == 3 ? 2 : 1);
+          if (F::waves && st != 2) {
+#pragma unroll
+            for (int l = 0; l < L; ++l) d[l].clear();
+#pragma unroll
+            for (int w = 0; w < NW; ++w) {
+              if (w < nw) {
+                const float u = W[w].unit(step, s, dtf);
+#pragma unroll
+                for (int l = 0; l < L; ++l) d[l].add(W[w].target, W[w].amp[l] * u);
+              }
+            }
+          } else if (!F::waves && st == 0) {
+#pragma unroll
+            for (int l = 0; l < L; ++l) d[l].clear();
+          }
+          const float c = st == 0 ? 0.f : (st == 3 ? 1.f : 0.5f);
+#pragma unroll
+          for (int l = 0; l < L; ++l) {
+            const F3 ms = st == 0 ? m[l] : fma3(kp[l], c, m[l]);
+            const F3 mb = l > 0 ? m[l - 1] : f3(0.f, 0.f, 0.f);
+            const F3 mt = l < L - 1 ? m[l + 1] : f3(0.f, 0.f, 0.f);
+            F3 k;
+            if (l == 0 && L == 1) k = rhs<FEAT, false, false>(P[l], ms, mb, mt, d[l]);
+            else if (l == 0) k = rhs<FEAT, false, true>(P[l], ms, mb, mt, d[l]);
+            else if (l == L - 1) k = rhs<FEAT, true, false>(P[l], ms, mb, mt, d[l]);
+            else k = rhs<FEAT, true, true>(P[l], ms, mb, mt, d[l]);
+            k = k * dtf;
+            kp[l] = k;
+            if (st == 0) acc[l] = k;
+            else if (st == 3) acc[l] = acc[l] + k;
+            else acc[l] = fma3(k, 2.f, acc[l]);
+          }
+        }
+#pragma unroll
+        for (int l = 0; l < L; ++l) m[l] = renorm(fma3(acc[l], 1.f / 6.f, m[l]));
+      } else {
+        // Euler-Heun (1709-1754) and Heun (1756-1815), neighbours un-updated
+        Delta<FEAT> d[L];
+#pragma unroll
+        for (int l = 0; l < L; ++l) d[l].clear();
+        if (F::waves) {
+#pragma unroll
+          for (int w = 0; w < NW; ++w) {
+            if (w < nw) {
+              const float u = W[w].unit(step, 0, dtf);
+#pragma unroll
+              for (int l = 0; l < L; ++l) d[l].add(W[w].target, W[w].amp[l] * u);
+            }
+          }
+        }
+        F3 f[L], g[L], dW[L], mn[L];
+#pragma unroll
+        for (int l = 0; l < L; ++l) {
+          const float T0 = F::swaves ? P[l].t0 + d[l].dT : P[l].t0;
+          const float sigma = sqrtf(fmaxf(P[l].sigc * T0, 0.f));
+          if (sigma > 0.f) {
+            float g0, g1, g2;
+            cmtj_gaussian3_f32(P[l].seed_lo, P[l].seed_hi, P[l].nstep0 + step, g0, g1, g2);
+            dW[l] = f3(g0, g1, g2) * sigma;
+          } else {
+            dW[l] = f3(0.f, 0.f, 0.f);
+          }
+          const F3 mb = l > 0 ? m[l - 1] : f3(0.f, 0.f, 0.f);
+          const F3 mt = l < L - 1 ? m[l + 1] : f3(0.f, 0.f, 0.f);
+          if (l == 0 && L == 1) f[l] = rhs<FEAT, false, false>(P[l], m[l], mb, mt, d[l]);
+          else if (l == 0) f[l] = rhs<FEAT, false, true>(P[l], m[l], mb, mt, d[l]);
+          else if (l == L - 1) f[l] = rhs<FEAT, true, false>(P[l], m[l], mb, mt, d[l]);
+          else f[l] = rhs<FEAT, true, true>(P[l], m[l], mb, mt, d[l]);
+          g[l] = stoch<FEAT>(P[l], m[l], dW[l]);
+        }
+        if (SOLVER == CMTJ_EULER_HEUN) {
+#pragma unroll
+          for (int l = 0; l < L; ++l) {
+            const F3 mN = fma3(g[l], sqdt, m[l]);
+            const F3 g2 = stoch<FEAT>(P[l], mN, dW[l]);
+            mn[l] = fma3(g[l] + g2, 0.5f * sqdt, fma3(f[l], dtf, m[l]));
+          }
+#pragma unroll
+          for (int l = 0; l < L; ++l) m[l] = renorm(mn[l]);
+        } else {
+#pragma unroll
+          for (int l = 0; l < L; ++l) mn[l] = fma3(g[l], sqdt, fma3(f[l], dtf, m[l]));
+          if (F::waves) {
+#pragma unroll
+            for (int l = 0; l < L; ++l) d[l].clear();
+#pragma unroll
+            for (int w = 0; w < NW; ++w) {
+              if (w < nw) {
+                const float u = W[w].unit(step, 2, dtf);
+#pragma unroll
+                for (int l = 0; l < L; ++l) d[l].add(W[w].target, W[w].amp[l] * u);
+              }
+            }
+          }
+#pragma unroll
+          for (int l = 0; l < L; ++l) {
+            const F3 mb = l > 0 ? mn[l - 1] : f3(0.f, 0.f, 0.f);
+            const F3 mt = l < L - 1 ? mn[l + 1] : f3(0.f, 0.f, 0.f);
+            F3 f2;
+            if (l == 0 && L == 1) f2 = rhs<FEAT, false, false>(P[l], mn[l], mb, mt, d[l]);
+            else if (l == 0) f2 = rhs<FEAT, false, true>(P[l], mn[l], mb, mt, d[l]);
+            else if (l == L - 1) f2 = rhs<FEAT, true, false>(P[l], mn[l], mb, mt, d[l]);
+            else f2 = rhs<FEAT, true, true>(P[l], mn[l], mb, mt, d[l]);
+            const F3 g2 = stoch<FEAT>(P[l], mn[l], dW[l]);
+            m[l] = renorm(fma3(g[l] + g2, 0.5f * sqdt, fma3(f[l] + f2, 0.5f * dtf, m[l])));
+          }
+        }
+      }
+
+      // ---- reductions: R and I(t) R(t) from win_start on
+      if (p.red_every && step >= win && (step - win) % p.red_every == 0) {
+        const float R = resistance<L>(mr, m, refL1, Rp, dR, rx0, amx, smx);
+        kadd(rs, rc, R);
+        if (vdph) {
+          const uint64_t ph = vph0 + (uint64_t)step * vdph;
+          const float I = sinpif(2.0f * ((float)(uint32_t)(ph >> 40) * 5.9604644775390625e-08f));
+          kadd(vs, vc, I * R);
+        }
+        ++n_red;
+      }
+      // ---- log (i % log_every == 0, like logLayerParams at 1978-1980)
+      if (C > 0 && step % p.log_every == 0) {
+        if (tcount == 0) bulk_wait_read();
+        float *dst = tile + tcount * C;
+        if (p.log_mode == CMTJ_LOG_M) {
+#pragma unroll
+          for (int l = 0; l < L; ++l) {
+            dst[3 * l] = m[l].x;
+            dst[3 * l + 1] = m[l].y;
+            dst[3 * l + 2] = m[l].z;
+          }
+        } else if (p.log_mode == CMTJ_LOG_MIX) {
+          float v = 0.f;
+#pragma unroll
+          for (int l = 0; l < L; ++l)
+            v = fmaf(mixw[l], p.log_axis == 0 ? m[l].x : (p.log_axis == 1 ? m[l].y : m[l].z), v);
+          dst[0] = v;
+        } else {
+          const float R = resistance<L>(mr, m, refL1, Rp, dR, rx0, amx, smx);
+          dst[0] = R;
+        }
+        ++tcount;
+        ++n_logged;
+        if (tcount == T) {
+          bulk_store(logrow + (size_t)(n_logged - T) * C, tile, T * C * 4u);
+          tcount = 0;
+        }
+      }
+    }
+
+    if (step == stop_all) {
+      // ---- junction (or chunk) done: flush the partial tile, save state
+      if (tcount > 0) {
+        const uint32_t t4 = (tcount + 3u) & ~3u;
+        bulk_store(logrow + (size_t)(n_logged - tcount) * C, tile, t4 * C * 4u);
+        tcount = 0;
+      }
+      cmtj_f32_state_t &S = A.S[jid];
+#pragma unroll
+      for (int l = 0; l < L; ++l) {
+        S.m[l][0] = m[l].x;
+        S.m[l][1] = m[l].y;
+        S.m[l][2] = m[l].z;
+      }
+      bool bad = false;
+#pragma unroll
+      for (int l = 0; l < L; ++l) bad |= isnan(m[l].x);
+      S.step = step;
+      S.status = bad ? CMTJ_STATUS_NAN : CMTJ_STATUS_OK;
+      S.n_logged = n_logged;
+      S.n_red = n_red;
+      S.r_sum = rs;
+      S.r_c = rc;
+      S.v_sum = vs;
+      S.v_c = vc;
+      jid = -1;
+    }
+  }
+  // Bulk stores still reading shared memory must finish before the CTA exits.
+  bulk_wait_read();
+}
+
+}  // namespace cmtjf

@@ -1,0 +1,9 @@
+// FP32 batched kernel variants for junctions with 1 layer(s).
+#include "batch_variants.cuh"
+
+static const CmtjBatchVariant kVariants[] = {CMTJ_BATCH_VARIANTS(CMTJ_VARIANT_ENTRY, 1)};
+
+int cmtj_batch_variants_l1(const CmtjBatchVariant **out) {
+  *out = kVariants;
+  return (int)(sizeof(kVariants) / sizeof(kVariants[0]));
+}

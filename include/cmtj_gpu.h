@@ -95,7 +95,10 @@ enum cmtj_reference { CMTJ_REF_NONE = 0, CMTJ_REF_FIXED = 1, CMTJ_REF_TOP = 2, C
 /* SolverMode (junction.hpp:143). */
 enum cmtj_solver { CMTJ_EULER_HEUN = 0, CMTJ_RK4 = 1, CMTJ_DORMAND_PRINCE = 2, CMTJ_HEUN = 3 };
 /* Junction MRmode (junction.hpp:1144). */
-enum cmtj_mr_mode { CMTJ_MR_NONE = 0, CMTJ_MR_CLASSIC = 1, CMTJ_MR_STRIP = 2 };
+enum cmtj_mr_mode { CMTJ_MR_NONE = 0, CMTJ_MR_CLASSIC = 1, CMTJ_MR_STRIP = 2,
+                   /* FP32 form only: Rx = sum_l Rx0 + AMR_X mx^2 + SMR_X my^2, the
+                    * series formula of cmtj/utils/resistance.py:121-150 */
+                   CMTJ_MR_SERIES = 3 };
 
 /* One Layer<double> (junction.hpp:145-258), as the solver needs it. */
 typedef struct cmtj_layer {
@@ -169,9 +172,11 @@ int cmtj_abi_version(void);
 const char *cmtj_last_error(void);
 /* Device properties the host planner needs: SM count and compute capability. */
 int cmtj_device_info(int device, int32_t *sm_count, int32_t *cc_major, int32_t *cc_minor);
-/* sizeof of the structs above, in this order: cmtj_driver_t, cmtj_layer_t,
- * cmtj_junction_t, cmtj_constants_t, cmtj_sim_params_t (n <= 5 entries);
- * lets a binding check its mirror of the layout. */
+/* sizeof of the structs of this header, in this order: cmtj_driver_t,
+ * cmtj_layer_t, cmtj_junction_t, cmtj_constants_t, cmtj_sim_params_t,
+ * cmtj_wave_t, cmtj_f32_layer_t, cmtj_f32_junction_t, cmtj_f32_state_t,
+ * cmtj_f32_params_t (the first n <= 10); lets a binding check its mirror of
+ * the layout. */
 int cmtj_struct_sizes(int32_t *sizes, int32_t n);
 
 /* ---------------------------------------------------------------------- */
@@ -190,6 +195,188 @@ int cmtj_run_simulation_f64(const cmtj_junction_t *d_junctions, int32_t n_juncti
                             cmtj_layer_t *d_layers, const double *d_tables,
                             const cmtj_sim_params_t *p, double *d_log,
                             uint32_t *d_status, void *stream);
+
+/* ---------------------------------------------------------------------- */
+/* FP32 batched form.                                                      */
+/* ---------------------------------------------------------------------- */
+/* Many independent junctions (1-4 layers each, uneven durations and driver
+ * sets) in one persistent launch.  The host lowers each junction into the
+ * records below: constant drivers are folded into per-layer coefficients
+ * (already divided by Ms, Ms*t, mu0 as the field terms need), and each
+ * time-dependent driver becomes one cmtj_wave_t.  m, fields and torques are
+ * FP32 with |m| renormalised every step; driver time enters through integer
+ * step counts and 64-bit fixed-point phases, so no FP32 time variable ever
+ * accumulates rounding. */
+
+/* Wave kinds: the time-dependent part of a ScalarDriver (drivers.hpp:262-305). */
+enum cmtj_wave_kind {
+  CMTJ_WAVE_SINE = 2, CMTJ_WAVE_STEP = 3, CMTJ_WAVE_POSINE = 4, CMTJ_WAVE_HALFSINE = 5,
+  CMTJ_WAVE_PULSE = 1, CMTJ_WAVE_TRAPEZOID = 6, CMTJ_WAVE_GAUSSIMPULSE = 7, CMTJ_WAVE_GAUSSSTEP = 8
+};
+/* Wave targets: which term of the field/torque the wave adds to. */
+enum cmtj_wave_target {
+  CMTJ_TGT_HX = 0, CMTJ_TGT_HY = 1, CMTJ_TGT_HZ = 2,   /* Hext+Hoe+Hdmi+Hres sum (A/m)      */
+  CMTJ_TGT_K = 3,                                       /* 2K/Ms                             */
+  CMTJ_TGT_K2 = 4,                                      /* 4K2/Ms                            */
+  CMTJ_TGT_JB = 5, CMTJ_TGT_JT = 6,                     /* J/(Ms t) bottom / top             */
+  CMTJ_TGT_J2B = 7, CMTJ_TGT_J2T = 8,                   /* 2 J2/(Ms t) bottom / top          */
+  CMTJ_TGT_I = 9,                                       /* current density (STT, static SOT) */
+  CMTJ_TGT_FL = 10, CMTJ_TGT_DL = 11, CMTJ_TGT_FL2 = 12, CMTJ_TGT_DL2 = 13, /* dynamic SOT   */
+  CMTJ_TGT_T = 14,                                      /* temperature (K)                   */
+  CMTJ_NUM_TGT = 15
+};
+
+/* One time-dependent driver.  Time is t_s = i*dt + s*dt/2 for step i and
+ * RK stage s in {0, 1, 2}.
+ *   SINE/POSINE/HALFSINE: phase (cycles, Q0.64) = ph0 + i*dph + s*dph_half;
+ *                         value = amp * sin(2 pi phase)
+ *   PULSE:                phase (Q0.64 of t/period) as above; on while
+ *                         phase <= cycle (thr32 compares the top 32 bits)
+ *   STEP:                 on while i in [on[s], off[s]] (inclusive; the host
+ *                         found these by evaluating the reference's FP64
+ *                         comparisons)
+ *   TRAPEZOID/GAUSS*:     tau = t - t0 = (i - i0)*dt + s*dt/2 + r0           */
+typedef struct cmtj_wave {
+  int32_t target, kind;
+  float amp;              /* amplitude, scaled like the target term            */
+  float p0, p1, p2;       /* TRAPEZOID: edge, steady, r0; GAUSSIMPULSE: 1/sigma, -, r0;
+                              GAUSSSTEP: 1/(sqrt2 sigma), -, r0                  */
+  uint32_t thr32;         /* PULSE duty threshold (Q0.32)                      */
+  int32_t i0;             /* TRAPEZOID/GAUSS*: step index nearest t0            */
+  uint64_t ph0, dph, dph_half;  /* SINE family / PULSE (Q0.64 cycles)           */
+  uint32_t on[3], off[3]; /* STEP: inclusive step-index window per stage        */
+  int32_t layer_mask;     /* bit l: the wave drives layer l                     */
+  int32_t reserved;
+} cmtj_wave_t;            /* 88 bytes */
+
+#define CMTJ_MAX_WAVES 4  /* distinct time-dependent drivers per junction     */
+
+/* Layer record of the FP32 form.  Field terms (junction.hpp:580-701) become:
+ *   Hanis = anis * (kc * (anis.m)),  Hanis2 = anis * (k2c * (anis.m)^3)
+ *   Hdemag = demag . m,  Hdipole = dip_b . m_bottom + dip_t . m_top
+ *   Hiec = m_b * (jb + j2b (m_b.m)) + m_t * (jt + j2t (m_t.m))
+ *   Hidmi = m_b x dmi_b + m_t x dmi_t          (= -(D x m_c)/(Ms t))
+ *   H = h0 + waves + Hanis + Hanis2 + Hiec + Hidmi - Hdemag - Hdipole
+ * and the torque (716-815): dm/dt = gam (m x H + alpha m x (m x H)) + STT/SOT. */
+typedef struct cmtj_f32_layer {
+  float m[3];             /* initial m, as stored (not renormalised)           */
+  float anis[3];
+  float kc, k2c;          /* 2K/Ms, 4K2/Ms (constant parts)                    */
+  float demag[9];         /* N * Ms/mu0                                        */
+  float dip_b[9], dip_t[9];
+  float h0[3];            /* constant part of Hext + Hoe + Hdmi + Hres         */
+  float jb, jt, j2b, j2t; /* J/(Ms t), 2 J2/(Ms t) constant parts              */
+  float dmi_b[3], dmi_t[3];
+  float gam, alpha;       /* -gamma/(1+alpha^2), alpha                         */
+  float ref[3], ref2[3];
+  int32_t ref_type;       /* enum cmtj_reference                               */
+  int32_t flags;          /* CMTJ_F32_STT | _SOT | _SOT_STATIC | _ALT_STT      */
+  float stt_c;            /* gamma*hbar/(e Ms t (1+alpha^2))                   */
+  float stt_p, stt_l, stt_beta, stt_kappa; /* P, lambda, beta, kappa           */
+  float i0;               /* constant current density                          */
+  float fl0, dl0, fl20, dl20; /* SOT: dynamic constants, or static torques/A   */
+  float sig_c;            /* 2 alpha kB / (Ms V gamma): sigma = sqrt(sig_c*T)  */
+  float t0;               /* constant temperature                              */
+  uint32_t seed_lo, seed_hi;
+  uint32_t noise_step_lo, noise_step_hi;
+} cmtj_f32_layer_t;
+
+#define CMTJ_F32_STT 1
+#define CMTJ_F32_SOT 2
+#define CMTJ_F32_SOT_STATIC 4
+#define CMTJ_F32_ALT_STT 8
+
+/* Junction header of the FP32 form. */
+typedef struct cmtj_f32_junction {
+  int32_t n_layers, mr_mode;
+  int32_t layer_offset;   /* first layer in the cmtj_f32_layer_t array         */
+  uint32_t n_steps;       /* iterations of this junction                      */
+  uint32_t win_start;     /* first step included in the on-device reductions */
+  uint32_t log_offset;    /* start of this junction's log row, in 16-byte
+                             granules (units of 4 floats) of the log buffer  */
+  float Rp, Rap;
+  float Rx0[CMTJ_MAX_LAYERS_F32], Ry0[CMTJ_MAX_LAYERS_F32];
+  float AMR_X[CMTJ_MAX_LAYERS_F32], AMR_Y[CMTJ_MAX_LAYERS_F32];
+  float SMR_X[CMTJ_MAX_LAYERS_F32], SMR_Y[CMTJ_MAX_LAYERS_F32];
+  float AHE[CMTJ_MAX_LAYERS_F32];
+  float mix_w[CMTJ_MAX_LAYERS_F32]; /* weights of the mixed log channel        */
+  uint64_t vsd_ph0, vsd_dph;        /* I(t) = sin(2 pi (vsd_ph0 + i vsd_dph))  */
+  int32_t n_waves;
+  int32_t reserved;
+  cmtj_wave_t waves[CMTJ_MAX_WAVES];
+} cmtj_f32_junction_t;
+
+/* Per-junction resumable state and on-device reductions (FP32 form). */
+typedef struct cmtj_f32_state {
+  float m[CMTJ_MAX_LAYERS_F32][3];
+  uint32_t step;          /* next iteration to run                             */
+  uint32_t status;        /* CMTJ_STATUS_*                                     */
+  uint32_t n_logged;      /* log samples written so far                        */
+  uint32_t n_red;         /* samples in the reductions                         */
+  float r_sum, r_c;       /* compensated (Neumaier) sum of R                   */
+  float v_sum, v_c;       /* compensated sum of I(t) * R(t)                    */
+} cmtj_f32_state_t;
+
+/* What the kernel logs every log_every steps (from step 0, like the
+ * reference's i % writeEvery == 0). */
+enum cmtj_log_mode {
+  CMTJ_LOG_NONE = 0,
+  CMTJ_LOG_M = 1,         /* all components of every layer: 3*n_layers floats  */
+  CMTJ_LOG_MIX = 2,       /* sum_l mix_w[l] * m_l[log_axis]: 1 float           */
+  CMTJ_LOG_R = 3          /* R (classic) or Rx (strip): 1 float                */
+};
+
+typedef struct cmtj_f32_params {
+  double dt;              /* time step (s)                                     */
+  uint32_t chunk_steps;   /* max iterations per junction in this launch        */
+  int32_t solver;         /* CMTJ_RK4, CMTJ_EULER_HEUN or CMTJ_HEUN            */
+  int32_t log_mode, log_axis;
+  uint32_t log_every;     /* 0: no log                                         */
+  uint32_t log_tile;      /* samples staged per thread before a bulk store     */
+  uint32_t red_every;     /* reduction cadence in steps (0: none)              */
+  int32_t reserved;
+} cmtj_f32_params_t;
+
+/* Kernel variant of a batch partition: n_layers (1-4), solver, and the
+ * CMTJ_FEAT_* terms its junctions use.  A variant that was not compiled
+ * falls back to the generic one of the same layer count and solver. */
+#define CMTJ_FEAT_FULL_DEMAG 1
+#define CMTJ_FEAT_DIPOLE 2
+#define CMTJ_FEAT_IDMI 4
+#define CMTJ_FEAT_K2 8
+#define CMTJ_FEAT_STT 16
+#define CMTJ_FEAT_SOT 32
+#define CMTJ_FEAT_WAVES 64         /* waves on the field (HX, HY, HZ) and, with
+                                      STT or SOT, on I / FL / DL / FL2 / DL2      */
+#define CMTJ_FEAT_SCALAR_WAVES 128 /* waves on K, K2, J*, T                      */
+#define CMTJ_FEAT_ALL 255
+
+/* Runs every junction of one partition (all with n_layers layers and the
+ * same solver) for up to p->chunk_steps iterations, resuming from d_state
+ * (state.step == 0 starts from the record).  Junctions are taken from
+ * d_order[0..n) through a work-stealing ticket in d_ticket (one uint32,
+ * zeroed by this call on `stream`).
+ *   d_log  one row of ceil4(samples) * channels floats per junction,
+ *          starting at float 4 * log_offset (16-byte aligned).
+ *   grid_blocks <= 0 picks one persistent wave of the device.              */
+int cmtj_batch_run_f32(const cmtj_f32_junction_t *d_junctions, const cmtj_f32_layer_t *d_layers,
+                       cmtj_f32_state_t *d_state, const int32_t *d_order, int32_t n, int32_t n_layers,
+                       int32_t features, const cmtj_f32_params_t *p, float *d_log, uint32_t *d_ticket,
+                       int32_t grid_blocks, void *stream);
+
+/* Feature set actually compiled for (n_layers, solver, features): the
+ * variant cmtj_batch_run_f32 will run. */
+int cmtj_batch_variant_f32(int32_t n_layers, int32_t solver, int32_t features);
+
+/* ---------------------------------------------------------------------- */
+/* On-device reductions.                                                   */
+/* ---------------------------------------------------------------------- */
+/* compute_spectrum_strip (cmtj/utils/procedures.py:28-39): for each of
+ * n_rows log rows (row r starts at d_series + r*row_stride and holds
+ * series_len samples), |FFT| of its last n_fft samples (n_fft a power of two,
+ * <= 8192), bins [bin_lo, bin_hi) written to d_out[r*(bin_hi-bin_lo) ...]. */
+int cmtj_spectrum_f32(const float *d_series, int64_t row_stride, int32_t n_rows, int32_t series_len,
+                      int32_t n_fft, int32_t bin_lo, int32_t bin_hi, float *d_out, void *stream);
 
 #ifdef __cplusplus
 }

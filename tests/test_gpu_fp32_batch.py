@@ -1,0 +1,54 @@
+"""FP32 batched form against the reference (golden FP64 logs) and the FP64
+plain form: max|dm| <= 1e-4 over the logged trajectory (the FP32 accuracy
+bound of the batched form)."""
+import numpy as np
+import pytest
+
+import cases
+import cmtj_gb300
+from cmtj_gb300 import batch
+from test_oracle_pin import load_golden
+
+TOL_M_F32 = 1e-4
+
+# cases the FP32 form accepts (drivers_zoo has 7 distinct time-dependent
+# drivers, custom_driver uses Python callbacks: FP64 plain form only)
+F32_CASES = ["config0_point", "sto", "sot_strip", "tri_layer", "vsd_sine", "energies_k2", "alt_stt_bottom",
+             "heun_det", "euler_heun_det"]
+
+
+def _golden_m(name, j):
+    g, _ = load_golden(name)
+    return np.stack([np.stack([g[l.id + "_m" + a] for a in "xyz"], axis=1) for l in j.layers], axis=1)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", F32_CASES)
+def test_fp32_batch_matches_reference(gpu_lib, name):
+    j, runs = cases.DETERMINISTIC[name](cmtj_gb300)
+    assert len(runs) == 1
+    r = dict(runs[0])
+    r.pop("calculateEnergies", None)
+    _, logs = batch.simulate_junctions_f32([j], **r)
+    ref = _golden_m(name, j)
+    got = logs[0]
+    assert got.shape == ref.shape, (got.shape, ref.shape)
+    err = float(np.max(np.abs(got - ref)))
+    assert err <= TOL_M_F32, (name, err)
+
+
+@pytest.mark.gpu
+def test_fp32_batch_mixed_layers_alone_equals_in_mix(gpu_lib):
+    """Uneven batch (1-3 layers, different durations): each junction's
+    trajectory is bit-identical alone and inside the mix."""
+    js = []
+    for k in range(24):
+        name = ["config0_point", "sto", "tri_layer", "vsd_sine"][k % 4]
+        js.append(cases.DETERMINISTIC[name](cmtj_gb300)[0])
+    run, logs = batch.simulate_junctions_f32(js, 3e-10, 1e-13, 1e-12)
+    for k in (0, 1, 2, 3, 13):
+        _, solo = batch.simulate_junctions_f32([js[k]], 3e-10, 1e-13, 1e-12)
+        assert np.array_equal(solo[0], logs[k]), k
+    st = run.state()
+    assert np.all(st["status"] == 0)
+    assert np.all(st["step"] == 3000)
