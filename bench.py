@@ -39,8 +39,25 @@ MAX_FREQ = 80e9      # PIMM_procedure default max_frequency (procedures.py:52)
 
 METRIC = "layer-steps/s FP32-batched vs FP64-plain @max|Δm|≤1e-4; p50/p99 request latency"
 UNIT = "layer-steps/s"
-WORKLOAD = ("batched FP32 PIMM: 262144 2-layer MTJs (512 H x 512 seeded Ku/J draws), 1 ps 1 kA/m Oersted "
-            "step, 5 ns @ dt=1e-13 (RK4), m_x mix logged every 1 ps, 4096-pt device FFT")
+RELAX_STEPS = 50000  # 5 ns at alpha = 1: static equilibrium before the ringing run (untimed setup)
+WORKLOAD = ("batched FP32 PIMM: 262144 2-layer MTJs (512 H x 512 seeded Ku/J draws) from their relaxed "
+            "equilibrium, 1 ps 1 kA/m Oersted step, 5 ns @ dt=1e-13 (RK4), m_x mix logged every 1 ps, "
+            "4096-pt device FFT")
+
+
+def fp32_flops_per_layer_step(n_layers=2, waves_per_junction=1):
+    """FP32 operations per layer-step of the batched RK4 integrator for the
+    PIMM junction (FMA = 2, rsqrt = 1), counted from its formulation:
+    per right-hand side and layer: field sum h0 + wave 3, anisotropy
+    a*(kc*(a.m)) 12, diagonal demag 6, LL torque gam*(mxH + alpha mx(mxH)) 27,
+    IEC per neighbour m_n*(j + j2 (m_n.m)) 13; per layer-step: 4 RHS, stage
+    states 18, k*dt 12, RK4 accumulation 15, update 6, renormalisation 9;
+    per step: each wave adds amp*u to every layer at 3 stage times (2 each)."""
+    nb = 2.0 * (n_layers - 1) / n_layers
+    rhs = 3 + 12 + 6 + 27 + 13 * nb
+    rk4 = 4 * rhs + 18 + 12 + 15 + 6 + 9
+    waves = 3 * waves_per_junction * n_layers * 2 / n_layers
+    return rk4 + waves
 
 
 def dist_info():
@@ -110,9 +127,11 @@ def flops_per_layer_step():
     return float(c.sum()) / (steps * 2), [int(x) for x in c]
 
 
-def build_workload(n_h=N_H, n_draw=N_DRAW):
+def build_workload(n_h=N_H, n_draw=N_DRAW, total=TOTAL, relax=True):
     from cmtj_gb300 import batch, sweeps
-    spec, n_steps = sweeps.pimm_config(n_h=n_h, n_draw=n_draw, dt=DT, total=TOTAL)
+    spec, n_steps = sweeps.pimm_config(n_h=n_h, n_draw=n_draw, dt=DT, total=total)
+    if relax:
+        batch.relax(spec, DT, RELAX_STEPS, alpha=1.0)
     low = batch.lower(spec, DT, n_steps)
     return spec, low, n_steps
 
@@ -200,7 +219,8 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--small", action="store_true", help="8192-junction workload (profiling)")
+    ap.add_argument("--profile", action="store_true",
+                    help="262144 junctions x 2000 steps, no extra measurements (for ncu captures)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference_arm(args)
@@ -216,19 +236,23 @@ def main():
     lib = engine.require_gpu()
     stream = torch.cuda.current_stream()
 
-    n_h, n_draw = (64, 128) if args.small else (N_H, N_DRAW)
-    spec, low, n_steps = build_workload(n_h, n_draw)
+    if args.profile:
+        spec, low, n_steps = build_workload(N_H, N_DRAW, total=2000 * DT, relax=False)
+    else:
+        spec, low, n_steps = build_workload(N_H, N_DRAW)
     n = spec.n
     layer_steps = float(n) * n_steps * 2
     run = batch.BatchRun(low, DT, batch.SolverMode.RK4, batch.LOG_MIX, LOG_EVERY, log_axis=0)
     samples = int(run.samples[0])
+    n_fft = min(N_FFT, 1 << int(np.log2(samples)))
     row_stride = int(run.log_pad[0])
     b_lo, b_hi = fft_bins()
+    b_hi = min(b_hi, n_fft // 2)
     d_spec = torch.empty((n, b_hi - b_lo), dtype=torch.float32, device="cuda")
     state0 = torch.zeros_like(run.d_s)
 
     def spectrum():
-        rc = lib.cmtj_spectrum_f32(engine.ptr(run.d_log), row_stride, n, samples, N_FFT, b_lo, b_hi,
+        rc = lib.cmtj_spectrum_f32(engine.ptr(run.d_log), row_stride, n, samples, n_fft, b_lo, b_hi,
                                    engine.ptr(d_spec), engine.stream_ptr())
         _abi.check(rc, lib)
 
@@ -322,7 +346,7 @@ def main():
             "e2e": e2e, "clocks": clocks,
             "gpu_launches": args.steps * 2}
 
-    if rank == 0 and not args.small:
+    if rank == 0 and not args.profile:
         extra = measure_rest(run, low, spec, n_steps, kern_ms, fft_only, lib)
         line.update(extra)
         f64 = line["fp64_plain"]
@@ -340,7 +364,8 @@ def measure_rest(run, low, spec, n_steps, kern_ms, fft_ms, lib):
     from cmtj_gb300 import batch, engine
     out = {}
     # roofline of the dominant kernel (the FP32 batch integrator)
-    fpls, fcount = flops_per_layer_step()
+    ref_fpls, fcount = flops_per_layer_step()
+    fpls = fp32_flops_per_layer_step(2, 1)
     n = spec.n
     kavg = float(np.mean(kern_ms)) / 1e3
     achieved = fpls * n * n_steps * 2 / kavg / 1e12
@@ -352,7 +377,9 @@ def measure_rest(run, low, spec, n_steps, kern_ms, fft_ms, lib):
     peak = probe.cmtj_probe_fp32_peak(5) / 1e12
     out["roofline"] = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                        "frac": achieved / peak, "traffic": None,
-                       "flop_per_layer_step": fpls, "flop_breakdown_add_mul_div_sqrt_trans": fcount,
+                       "flop_per_layer_step": fpls,
+                       "reference_flop_per_layer_step": ref_fpls,
+                       "reference_flop_breakdown_add_mul_div_sqrt_trans": fcount,
                        "peak_source": "measured FP32 FMA probe on this GPU (MEASURED_PEAKS.json has no FP32 figure)",
                        "kernel_ms_avg": kavg * 1e3, "fft_ms_avg": float(np.mean(fft_ms))}
 
@@ -404,12 +431,15 @@ def measure_rest(run, low, spec, n_steps, kern_ms, fft_ms, lib):
 
 
 def spec_to_junctions_rows(spec, rows):
-    """Junction objects for the given rows of the PIMM spec."""
+    """Junction objects for the given rows of the PIMM spec, starting from
+    the spec's m0 exactly (no renormalisation)."""
     import cmtj_gb300 as cm
     import cases
     out = []
     for k in rows:
         j, _ = cases.config0_point(cm, hx=float(spec.Hc[k, 0, 0]), total=1e-9)
+        for l in range(2):
+            j.layers[l].mag = cm.CVector(*spec.m0[k, l])
         j.setLayerAnisotropyDriver("free", cm.constantDriver(float(spec.K[k, 0])))
         j.setIECDriver("free", "ref", cm.constantDriver(float(spec.Jt[k, 0])))
         j.setLayerOerstedFieldDriver("all", cm.AxialDriver(cm.stepDriver(0, 1e3, 0, 1e-12), cm.NullDriver(),

@@ -633,3 +633,27 @@ def simulate_junctions_f32(junctions, totalTime, timeStep=1e-13, writeFrequency=
     log = run.d_log.cpu().numpy()
     out = [run.log_of(k, log).reshape(-1, junctions[k].layerNo, 3) for k in range(len(junctions))]
     return run, out
+
+
+def relax(spec, time_step, n_steps, alpha=1.0):
+    """Bring every junction of `spec` close to its static equilibrium: run
+    the FP32 form for n_steps with damping `alpha`, no time-dependent
+    drivers and no thermal field, then store the final m as spec.m0 (the
+    warm start PIMM_procedure gets by sweeping H, procedures.py:114-141).
+    Returns the relaxed m [n, 4, 3]."""
+    import copy as _copy
+    sp = _copy.copy(spec)
+    sp.alpha = np.where(spec.alpha > 0, alpha, alpha)
+    sp.temperature = np.zeros_like(spec.temperature)
+    sp.wave_table = None
+    sp.wave_count = None
+    sp.waves = []
+    sp.wave_drivers = [[] for _ in range(spec.n)]
+    low = lower(sp, time_step, n_steps)
+    run = BatchRun(low, time_step, SolverMode.RK4, LOG_NONE, 0)
+    run.launch()
+    m = run.state()["m"].astype(np.float64)
+    L = spec.n_layers
+    mask = np.arange(4)[None, :] < L[:, None]
+    spec.m0 = np.where(mask[..., None], m, spec.m0)
+    return spec.m0

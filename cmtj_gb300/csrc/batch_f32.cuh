@@ -391,6 +391,7 @@ __global__ void __launch_bounds__(128) k_batch(Args A) {
   int32_t jid = -1;
   bool retired = false;
   uint32_t step = 0, end = 0, stop_all = 0, n_logged = 0, tcount = 0, n_red = 0, win = 0;
+  uint32_t log_cd = 0, red_cd = 0;  // steps until the next log / reduction sample
   int mr = 0;
   float Rp = 0.f, dR = 0.f;
   float rx0[L], amx[L], smx[L], mixw[L];
@@ -461,6 +462,11 @@ __global__ void __launch_bounds__(128) k_batch(Args A) {
             vdph = J.vsd_dph;
             tcount = 0;
             logrow = A.log + (size_t)J.log_offset * 4u;
+            // countdowns to the next sample: log at step % log_every == 0,
+            // reductions at (step - win) % red_every == 0 for step >= win
+            log_cd = p.log_every ? (p.log_every - step % p.log_every) % p.log_every : 0xffffffffu;
+            red_cd = !p.red_every ? 0xffffffffu
+                     : (step >= win ? (p.red_every - (step - win) % p.red_every) % p.red_every : win - step);
           }
         }
       }
@@ -589,7 +595,9 @@ __global__ void __launch_bounds__(128) k_batch(Args A) {
       }
 
       // ---- reductions: R and I(t) R(t) from win_start on
-      if (p.red_every && step >= win && (step - win) % p.red_every == 0) {
+      const bool red_now = red_cd == 0;
+      red_cd = red_now ? p.red_every - 1 : red_cd - 1;
+      if (red_now) {
         const float R = resistance<L>(mr, m, refL1, Rp, dR, rx0, amx, smx);
         kadd(rs, rc, R);
         if (vdph) {
@@ -600,7 +608,9 @@ __global__ void __launch_bounds__(128) k_batch(Args A) {
         ++n_red;
       }
       // ---- log (i % log_every == 0, like logLayerParams at 1978-1980)
-      if (C > 0 && step % p.log_every == 0) {
+      const bool log_now = log_cd == 0;
+      log_cd = log_now ? p.log_every - 1 : log_cd - 1;
+      if (C > 0 && log_now) {
         if (tcount == 0) bulk_wait_read();
         float *dst = tile + tcount * C;
         if (p.log_mode == CMTJ_LOG_M) {
