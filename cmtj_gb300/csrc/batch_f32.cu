@@ -1,5 +1,7 @@
 // Host side of the FP32 batched form: variant choice, persistent grid size,
 // ticket reset and launch.
+#include <mutex>
+
 #include "batch_variants.cuh"
 
 namespace {
@@ -100,4 +102,69 @@ extern "C" int cmtj_batch_run_f32(const cmtj_f32_junction_t *d_junctions, const 
   void *args[] = {&a};
   CMTJ_CUDA_TRY(cudaLaunchKernel(v->fn, dim3(blocks), dim3(threads), args, smem, s));
   return CMTJ_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant.
+//
+// Some callers cannot call cudaMalloc: code that runs while a CUDA graph is
+// being captured in relaxed or global mode, real-time or signal-handler
+// threads that must not take the driver's allocation locks, and hosts that
+// hand a plugin all of its memory up front (a fixed arena) and forbid it any
+// allocation of its own.  cmtj_batch_run_f32 needs one uint32 work-stealing
+// ticket in global memory, which its caller allocates.  This variant keeps
+// its tickets in the library's own device memory instead: the file-scope
+// array below, CMTJ_NOALLOC_TICKET_SLOTS (64) tickets of 4 bytes, 256 bytes
+// that every GPU which loads the library holds until the process exits.
+// ---------------------------------------------------------------------------
+static __device__ __align__(256) uint32_t g_noalloc_tickets[CMTJ_NOALLOC_TICKET_SLOTS];
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+uint32_t *g_noalloc_ptr[kMaxDevices] = {nullptr};
+
+// Device address of g_noalloc_tickets on the current device, resolved once
+// per device with that device current.  In host code the array's name is
+// only a host-side stand-in for the symbol, never a device address.
+int noalloc_tickets(uint32_t **out) {
+  int dev = 0;
+  CMTJ_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) {
+    cmtj_set_error("cmtj_batch_run_f32_noalloc: device ordinal %d beyond %d", dev, kMaxDevices);
+    return CMTJ_ERR_LIMIT;
+  }
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_ptr[dev]) {
+    void *ptr = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_tickets);
+    if (e != cudaSuccess || !ptr) {
+      cmtj_set_error("cmtj_batch_run_f32_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
+      return CMTJ_ERR_CUDA;
+    }
+    g_noalloc_ptr[dev] = static_cast<uint32_t *>(ptr);
+  }
+  *out = g_noalloc_ptr[dev];
+  return CMTJ_OK;
+}
+}  // namespace
+
+extern "C" int cmtj_batch_run_f32_noalloc(const cmtj_f32_junction_t *d_junctions, const cmtj_f32_layer_t *d_layers,
+                                          cmtj_f32_state_t *d_state, const int32_t *d_order, int32_t n,
+                                          int32_t n_layers, int32_t features, const cmtj_f32_params_t *p,
+                                          float *d_log, int32_t ticket_slot, int32_t grid_blocks, void *stream) {
+  if (ticket_slot < 0 || ticket_slot >= CMTJ_NOALLOC_TICKET_SLOTS) {
+    cmtj_set_error("cmtj_batch_run_f32_noalloc: ticket_slot %d is outside [0, %d): the library holds %d "
+                   "static tickets",
+                   ticket_slot, CMTJ_NOALLOC_TICKET_SLOTS, CMTJ_NOALLOC_TICKET_SLOTS);
+    return CMTJ_ERR_LIMIT;
+  }
+  uint32_t *tickets = nullptr;
+  const int rc = noalloc_tickets(&tickets);
+  if (rc != CMTJ_OK) return rc;
+  // cmtj_batch_run_f32 zeroes the ticket on `stream` before its launch
+  // (cudaMemsetAsync, no allocation), so the slot's previous contents never
+  // leak into this call.
+  return cmtj_batch_run_f32(d_junctions, d_layers, d_state, d_order, n, n_layers, features, p, d_log,
+                            tickets + ticket_slot, grid_blocks, stream);
 }

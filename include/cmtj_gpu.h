@@ -368,6 +368,25 @@ int cmtj_batch_run_f32(const cmtj_f32_junction_t *d_junctions, const cmtj_f32_la
  * variant cmtj_batch_run_f32 will run. */
 int cmtj_batch_variant_f32(int32_t n_layers, int32_t solver, int32_t features);
 
+/* No counterpart in the reference: an allocation-free form of
+ * cmtj_batch_run_f32 for callers that cannot call cudaMalloc (code running
+ * under CUDA graph capture, real-time threads that must not take the
+ * driver's allocation locks, hosts that give a plugin a fixed memory arena).
+ * Same arguments and results, except that the work-stealing ticket lives in
+ * a static device array inside the library, CMTJ_NOALLOC_TICKET_SLOTS
+ * tickets (256 bytes per GPU, held until the process exits), chosen by
+ * ticket_slot; a slot outside [0, CMTJ_NOALLOC_TICKET_SLOTS) returns
+ * CMTJ_ERR_LIMIT.  The caller still passes every input and output buffer.
+ * The first call on a device resolves the array's device address
+ * (cudaGetSymbolAddress) with that device current, so make it before any
+ * stream capture.  Each call zeroes its slot on `stream` before launching;
+ * calls that overlap on the GPU and use the same slot race on its ticket. */
+#define CMTJ_NOALLOC_TICKET_SLOTS 64
+int cmtj_batch_run_f32_noalloc(const cmtj_f32_junction_t *d_junctions, const cmtj_f32_layer_t *d_layers,
+                               cmtj_f32_state_t *d_state, const int32_t *d_order, int32_t n, int32_t n_layers,
+                               int32_t features, const cmtj_f32_params_t *p, float *d_log, int32_t ticket_slot,
+                               int32_t grid_blocks, void *stream);
+
 /* ---------------------------------------------------------------------- */
 /* On-device reductions.                                                   */
 /* ---------------------------------------------------------------------- */
