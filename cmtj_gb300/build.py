@@ -23,6 +23,7 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + INCLUD
 UNITS = {
     "abi.cu": [],
     "plain_f64.cu": ["--fmad=false"],
+    "stack_f64.cu": ["--fmad=false"],
     "batch_f32.cu": [],
     "batch_f32_l1.cu": [],
     "batch_f32_l2.cu": [],

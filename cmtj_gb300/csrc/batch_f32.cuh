@@ -177,7 +177,9 @@ template <int FEAT> struct Delta {
 // One time-dependent driver in registers.
 template <int L> struct WaveR {
   int target, kind;
+  bool field;   // targets HX/HY/HZ: added as hdir[l] * u, no target dispatch
   float amp[L];
+  F3 hdir[L];
   float p0, p1, p2;
   uint32_t thr32;
   int32_t i0;
@@ -187,8 +189,13 @@ template <int L> struct WaveR {
   __device__ __forceinline__ void load(const cmtj_wave_t &w) {
     target = w.target;
     kind = w.kind;
+    field = target <= CMTJ_TGT_HZ;
 #pragma unroll
-    for (int l = 0; l < L; ++l) amp[l] = ((w.layer_mask >> l) & 1) ? w.amp : 0.f;
+    for (int l = 0; l < L; ++l) {
+      amp[l] = ((w.layer_mask >> l) & 1) ? w.amp : 0.f;
+      hdir[l] = f3(target == CMTJ_TGT_HX ? amp[l] : 0.f, target == CMTJ_TGT_HY ? amp[l] : 0.f,
+                   target == CMTJ_TGT_HZ ? amp[l] : 0.f);
+    }
     p0 = w.p0;
     p1 = w.p1;
     p2 = w.p2;
@@ -245,6 +252,22 @@ template <int L> struct WaveR {
     }
   }
 };
+
+// Adds wave w's value at (step, stage) to every layer's deltas.  Variants
+// without scalar or torque waves only ever see field waves (the host routes
+// others elsewhere), so they take the branch-free field path.
+template <int L, int FEAT>
+__device__ __forceinline__ void add_wave(const WaveR<L> &w, uint32_t step, int s, float dtf, Delta<FEAT> *d) {
+  using F = Feat<FEAT>;
+  const float u = w.unit(step, s, dtf);
+  if (!(F::swaves || F::twaves) || w.field) {
+#pragma unroll
+    for (int l = 0; l < L; ++l) d[l].dH = fma3(w.hdir[l], u, d[l].dH);
+  } else {
+#pragma unroll
+    for (int l = 0; l < L; ++l) d[l].add(w.target, w.amp[l] * u);
+  }
+}
 
 // Effective field + LL torque of one layer (junction.hpp:580-815).
 template <int FEAT, bool HB, bool HT>
@@ -353,17 +376,22 @@ __device__ __forceinline__ void bulk_wait_read() {
 // STRIP Rx = 1 / sum_l 1/(Rx0 + AMR_X mx^2 + SMR_X my^2) (1835-1857), SERIES
 // Rx = sum_l (Rx0 + AMR_X mx^2 + SMR_X my^2) (cmtj/utils/resistance.py:121-150).
 template <int L>
-__device__ __forceinline__ float resistance(int mr, const F3 *m, F3 refL1, float Rp, float dR, const float *rx0,
-                                            const float *amx, const float *smx) {
-  if (mr == CMTJ_MR_CLASSIC) return fmaf(dR, 1.f - dot(m[0], L > 1 ? m[L - 1 > 0 ? 1 : 0] : refL1), Rp);
+__device__ __forceinline__ float resistance(const cmtj_f32_junction_t *J, const float *ref0, const F3 *m) {
+  const int mr = J->mr_mode;
+  if (mr == CMTJ_MR_CLASSIC) {
+    const F3 other = L > 1 ? m[L > 1 ? 1 : 0] : ld3(ref0);
+    return fmaf((J->Rap - J->Rp) * 0.5f, 1.f - dot(m[0], other), J->Rp);
+  }
   float acc = 0.f;
   if (mr == CMTJ_MR_SERIES) {
 #pragma unroll
-    for (int l = 0; l < L; ++l) acc += fmaf(amx[l], m[l].x * m[l].x, fmaf(smx[l], m[l].y * m[l].y, rx0[l]));
+    for (int l = 0; l < L; ++l)
+      acc += fmaf(J->AMR_X[l], m[l].x * m[l].x, fmaf(J->SMR_X[l], m[l].y * m[l].y, J->Rx0[l]));
     return acc;
   }
 #pragma unroll
-  for (int l = 0; l < L; ++l) acc += 1.f / fmaf(amx[l], m[l].x * m[l].x, fmaf(smx[l], m[l].y * m[l].y, rx0[l]));
+  for (int l = 0; l < L; ++l)
+    acc += 1.f / fmaf(J->AMR_X[l], m[l].x * m[l].x, fmaf(J->SMR_X[l], m[l].y * m[l].y, J->Rx0[l]));
   return 1.f / acc;
 }
 
@@ -371,8 +399,14 @@ template <int L> __device__ __forceinline__ int log_channels(int mode) {
   return mode == CMTJ_LOG_M ? 3 * L : (mode == CMTJ_LOG_NONE ? 0 : 1);
 }
 
+// Resident CTAs of 128 threads per SM the specialised variants are built
+// for (register cap); the catch-all CMTJ_FEAT_ALL variants take what they need.
+#ifndef CMTJ_BATCH_MINB
+#define CMTJ_BATCH_MINB 4
+#endif
+
 template <int L, int SOLVER, int FEAT, int NW>
-__global__ void __launch_bounds__(128) k_batch(Args A) {
+__global__ void __launch_bounds__(128, (FEAT == CMTJ_FEAT_ALL) ? 1 : CMTJ_BATCH_MINB) k_batch(Args A) {
   using F = Feat<FEAT>;
   extern __shared__ __align__(16) float smem[];
   const int lane = threadIdx.x & 31;
@@ -392,13 +426,12 @@ __global__ void __launch_bounds__(128) k_batch(Args A) {
   bool retired = false;
   uint32_t step = 0, end = 0, stop_all = 0, n_logged = 0, tcount = 0, n_red = 0, win = 0;
   uint32_t log_cd = 0, red_cd = 0;  // steps until the next log / reduction sample
-  int mr = 0;
-  float Rp = 0.f, dR = 0.f;
-  float rx0[L], amx[L], smx[L], mixw[L];
-  uint64_t vph0 = 0, vdph = 0;
+  // junction constants used only when logging or reducing stay in the
+  // record (read through L1 when needed), not in registers
+  const cmtj_f32_junction_t *Jp = nullptr;
+  const float *ref0 = nullptr;
   float rs = 0.f, rc = 0.f, vs = 0.f, vc = 0.f;
   float *logrow = nullptr;
-  F3 refL1 = f3(0.f, 0.f, 0.f);
 
   for (;;) {
     // ---- refill lanes that have no junction (warp-aggregated ticket)
@@ -447,19 +480,8 @@ __global__ void __launch_bounds__(128) k_batch(Args A) {
             vs = S.v_sum;
             vc = S.v_c;
             win = J.win_start;
-            mr = J.mr_mode;
-            Rp = J.Rp;
-            dR = (J.Rap - J.Rp) * 0.5f;
-#pragma unroll
-            for (int l = 0; l < L; ++l) {
-              rx0[l] = J.Rx0[l];
-              amx[l] = J.AMR_X[l];
-              smx[l] = J.SMR_X[l];
-              mixw[l] = J.mix_w[l];
-            }
-            refL1 = ld3(A.Ly[J.layer_offset].ref);
-            vph0 = J.vsd_ph0;
-            vdph = J.vsd_dph;
+            Jp = &J;
+            ref0 = A.Ly[J.layer_offset].ref;
             tcount = 0;
             logrow = A.log + (size_t)J.log_offset * 4u;
             // countdowns to the next sample: log at step % log_every == 0,
@@ -489,13 +511,8 @@ __global__ void __launch_bounds__(128) k_batch(Args A) {
 #pragma unroll
             for (int l = 0; l < L; ++l) d[l].clear();
 #pragma unroll
-            for (int w = 0; w < NW; ++w) {
-              if (w < nw) {
-                const float u = W[w].unit(step, s, dtf);
-#pragma unroll
-                for (int l = 0; l < L; ++l) d[l].add(W[w].target, W[w].amp[l] * u);
-              }
-            }
+            for (int w = 0; w < NW; ++w)
+              if (w < nw) add_wave<L, FEAT>(W[w], step, s, dtf, d);
           } else if (!F::waves && st == 0) {
 #pragma unroll
             for (int l = 0; l < L; ++l) d[l].clear();
@@ -527,13 +544,8 @@ __global__ void __launch_bounds__(128) k_batch(Args A) {
         for (int l = 0; l < L; ++l) d[l].clear();
         if (F::waves) {
 #pragma unroll
-          for (int w = 0; w < NW; ++w) {
-            if (w < nw) {
-              const float u = W[w].unit(step, 0, dtf);
-#pragma unroll
-              for (int l = 0; l < L; ++l) d[l].add(W[w].target, W[w].amp[l] * u);
-            }
-          }
+          for (int w = 0; w < NW; ++w)
+            if (w < nw) add_wave<L, FEAT>(W[w], step, 0, dtf, d);
         }
         F3 f[L], g[L], dW[L], mn[L];
 #pragma unroll
@@ -571,13 +583,8 @@ __global__ void __launch_bounds__(128) k_batch(Args A) {
 #pragma unroll
             for (int l = 0; l < L; ++l) d[l].clear();
 #pragma unroll
-            for (int w = 0; w < NW; ++w) {
-              if (w < nw) {
-                const float u = W[w].unit(step, 2, dtf);
-#pragma unroll
-                for (int l = 0; l < L; ++l) d[l].add(W[w].target, W[w].amp[l] * u);
-              }
-            }
+            for (int w = 0; w < NW; ++w)
+              if (w < nw) add_wave<L, FEAT>(W[w], step, 2, dtf, d);
           }
 #pragma unroll
           for (int l = 0; l < L; ++l) {
@@ -598,10 +605,11 @@ __global__ void __launch_bounds__(128) k_batch(Args A) {
       const bool red_now = red_cd == 0;
       red_cd = red_now ? p.red_every - 1 : red_cd - 1;
       if (red_now) {
-        const float R = resistance<L>(mr, m, refL1, Rp, dR, rx0, amx, smx);
+        const float R = resistance<L>(Jp, ref0, m);
         kadd(rs, rc, R);
+        const uint64_t vdph = Jp->vsd_dph;
         if (vdph) {
-          const uint64_t ph = vph0 + (uint64_t)step * vdph;
+          const uint64_t ph = Jp->vsd_ph0 + (uint64_t)step * vdph;
           const float I = sinpif(2.0f * ((float)(uint32_t)(ph >> 40) * 5.9604644775390625e-08f));
           kadd(vs, vc, I * R);
         }
@@ -624,11 +632,10 @@ __global__ void __launch_bounds__(128) k_batch(Args A) {
           float v = 0.f;
 #pragma unroll
           for (int l = 0; l < L; ++l)
-            v = fmaf(mixw[l], p.log_axis == 0 ? m[l].x : (p.log_axis == 1 ? m[l].y : m[l].z), v);
+            v = fmaf(Jp->mix_w[l], p.log_axis == 0 ? m[l].x : (p.log_axis == 1 ? m[l].y : m[l].z), v);
           dst[0] = v;
         } else {
-          const float R = resistance<L>(mr, m, refL1, Rp, dR, rx0, amx, smx);
-          dst[0] = R;
+          dst[0] = resistance<L>(Jp, ref0, m);
         }
         ++tcount;
         ++n_logged;

@@ -12,228 +12,11 @@
 // The state of a junction (m of every layer, side values for the energy
 // log) lives in the thread's registers / local memory; layer parameters
 // and drivers are read from the caller's cmtj_layer_t array through L1.
-#include "common.cuh"
-#include "philox.cuh"
+#include "plain_f64.cuh"
+
+using namespace cmtjd;
 
 namespace {
-
-struct D3 {
-  double x, y, z;
-};
-__device__ __forceinline__ D3 d3(double x, double y, double z) {
-  D3 r;
-  r.x = x;
-  r.y = y;
-  r.z = z;
-  return r;
-}
-__device__ __forceinline__ D3 zero3() { return d3(0.0, 0.0, 0.0); }
-__device__ __forceinline__ D3 operator+(const D3 &a, const D3 &b) { return d3(a.x + b.x, a.y + b.y, a.z + b.z); }
-__device__ __forceinline__ D3 operator-(const D3 &a, const D3 &b) { return d3(a.x - b.x, a.y - b.y, a.z - b.z); }
-__device__ __forceinline__ D3 operator*(const D3 &a, double s) { return d3(a.x * s, a.y * s, a.z * s); }
-__device__ __forceinline__ D3 operator/(const D3 &a, double s) { return d3(a.x / s, a.y / s, a.z / s); }
-__device__ __forceinline__ D3 smul(double s, const D3 &a) { return d3(s * a.x, s * a.y, s * a.z); }
-__device__ __forceinline__ double dot(const D3 &a, const D3 &b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
-__device__ __forceinline__ D3 cross(const D3 &a, const D3 &b) {
-  return d3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
-}
-__device__ __forceinline__ D3 load3(const double *p) { return d3(p[0], p[1], p[2]); }
-
-// CVector::normalize (cvector.hpp:185-192); pow(v, 2) is v*v.
-__device__ __forceinline__ D3 normalized(const D3 &v) {
-  const double mag = sqrt(v.x * v.x + v.y * v.y + v.z * v.z);
-  if (mag != 0) return d3(v.x / mag, v.y / mag, v.z / mag);
-  return v;
-}
-
-// calculate_tensor_interaction (junction.hpp:54-72).
-__device__ __forceinline__ D3 tensor_mul(const D3 &m, const double *t, double Ms, double mu0) {
-  const D3 r = d3(t[0] * m.x + t[1] * m.y + t[2] * m.z, t[3] * m.x + t[4] * m.y + t[5] * m.z,
-                  t[6] * m.x + t[7] * m.y + t[8] * m.z);
-  return r * (Ms / mu0);
-}
-
-// x^3 rounded once: x*x is split exactly into hi + lo (FMA error-free
-// product), then (hi + lo) * x is formed with one final rounding.  This is
-// what a correctly rounded pow(x, 3.0) returns, up to rare ties.
-__device__ __forceinline__ double cube_rn(double x) {
-  const double ph = x * x;
-  const double pl = fma(x, x, -ph);
-  const double th = ph * x;
-  const double tl = fma(ph, x, -th) + pl * x;
-  return th + tl;
-}
-
-struct DriverCtx {
-  const double *tables;
-  uint32_t step;
-  int stage;  // 0: t, 1: t + dt/2, 2: t + dt
-};
-
-// ScalarDriver::getCurrentScalarValue (drivers.hpp:262-305).
-__device__ double drv(const cmtj_driver_t &d, double time, const DriverCtx &dc) {
-  const int u = d.update;
-  double rv = d.constantValue;
-  if (u == CMTJ_DRV_CONSTANT) return rv;
-  if (u == CMTJ_DRV_PULSE) {
-    const int n = (int)(time / d.period);
-    const double dT = d.cycle * d.period;
-    const double nT = n * d.period;
-    if (nT <= time && time <= (nT + dT)) rv = rv + d.amplitude;
-  } else if (u == CMTJ_DRV_SINE) {
-    rv = rv + d.amplitude * sin(2 * M_PI * time * d.frequency + d.phase);
-  } else if (u == CMTJ_DRV_POSINE) {
-    rv = rv + fabs(d.amplitude * sin(2 * M_PI * time * d.frequency + d.phase));
-  } else if (u == CMTJ_DRV_HALFSINE) {
-    const double tamp = d.amplitude * sin(2 * M_PI * time * d.frequency + d.phase);
-    if (tamp <= 0) rv = rv + tamp;
-  } else if (u == CMTJ_DRV_STEP) {
-    if (time >= d.timeStart && time <= d.timeStop) rv = rv + d.amplitude;
-  } else if (u == CMTJ_DRV_TRAPEZOID) {
-    const double ts = d.timeStart, e = d.edgeTime, s = d.steadyTime, a = d.amplitude;
-    double add = 0.0;
-    if (time < ts) add = 0.0;
-    else if (time <= ts + e) add = (a / e) * (time - ts);
-    else if (time <= ts + e + s) add = a;
-    else if (time <= ts + 2 * e + s) add = a - (a / e) * (time - (ts + e + s));
-    rv = rv + add;
-  } else if (u == CMTJ_DRV_GAUSSIMPULSE) {
-    const double dtt = time - d.timeStart;
-    rv = rv + d.amplitude * exp(-(dtt * dtt) / (2 * (d.edgeTime * d.edgeTime)));
-  } else if (u == CMTJ_DRV_GAUSSSTEP) {
-    rv = rv + 0.5 * d.amplitude * (1 + erf((time - d.timeStart) / (sqrt(2.0) * d.edgeTime)));
-  } else if (u == CMTJ_DRV_TABLE) {
-    return dc.tables[d.table_offset + (int64_t)dc.step * 3 + dc.stage];
-  }
-  return rv;
-}
-
-__device__ __forceinline__ D3 axial(const cmtj_layer_t &L, int slot, double t, const DriverCtx &dc) {
-  return d3(drv(L.drv[slot], t, dc), drv(L.drv[slot + 1], t, dc), drv(L.drv[slot + 2], t, dc));
-}
-
-// Values the reference keeps on the Layer as side effects of the last field
-// evaluation and logs with calculateEnergies (junction.hpp:1589-1613).
-struct Side {
-  double K, K2, Jb, Jt, I;
-  D3 Hext, Hiec, Hanis, Hdemag, Hfl, Hdl;
-};
-
-// calculateHeff + solveLLG (junction.hpp:580-815, 855-864).
-__device__ D3 rhs(const cmtj_layer_t &L, const cmtj_constants_t &c, double time, const D3 &m, const D3 &bottom,
-                  const D3 &top, const DriverCtx &dc, Side *side) {
-  const double mu0 = c.mu0;
-  const double Ms = L.Ms;
-  // --- calculateHeff (580-622)
-  const D3 Hdipole = tensor_mul(bottom, L.dipole_bottom, Ms, mu0) + tensor_mul(top, L.dipole_top, Ms, mu0);
-  const D3 Hext = axial(L, CMTJ_SLOT_HEXT, time, dc);
-  const D3 Hoe = axial(L, CMTJ_SLOT_HOE, time, dc);
-  const D3 Hdemag = tensor_mul(m, L.demag, Ms, mu0);
-  const double Jb = drv(L.drv[CMTJ_SLOT_IEC_BOTTOM], time, dc);
-  const double Jt = drv(L.drv[CMTJ_SLOT_IEC_TOP], time, dc);
-  const double J2b = drv(L.drv[CMTJ_SLOT_IECQ_BOTTOM], time, dc);
-  const double J2t = drv(L.drv[CMTJ_SLOT_IECQ_TOP], time, dc);
-  const double Mst = Ms * L.thickness;
-  const D3 Hiec = (bottom * (Jb + 2 * J2b * dot(bottom, m))) / Mst + (top * (Jt + 2 * J2t * dot(top, m))) / Mst;
-  const D3 Db = axial(L, CMTJ_SLOT_IDMI_BOTTOM, time, dc);
-  const D3 Dt = axial(L, CMTJ_SLOT_IDMI_TOP, time, dc);
-  const D3 Hidmi = smul(-1.0, cross(Db, bottom)) / Mst + smul(-1.0, cross(Dt, top)) / Mst;
-  const D3 anis = load3(L.anis);
-  const double K = drv(L.drv[CMTJ_SLOT_ANIS], time, dc);
-  const D3 Hanis = anis * ((2 * K) * dot(anis, m) / Ms);
-  const D3 Hdmi = axial(L, CMTJ_SLOT_HDMI, time, dc);
-  const D3 Hres = axial(L, CMTJ_SLOT_HRES, time, dc);
-  const double K2 = drv(L.drv[CMTJ_SLOT_ANIS2], time, dc);
-  const D3 Hanis2 = anis * ((4 * K2) * cube_rn(dot(anis, m)) / Ms);
-  const D3 Hfluct = zero3();
-  const D3 H = Hext + Hanis + Hanis2 + Hiec + Hidmi + Hoe + Hdmi + Hfluct - Hdemag - Hdipole + Hres;
-  if (side) {
-    side->K = K;
-    side->K2 = K2;
-    side->Jb = Jb;
-    side->Jt = Jt;
-    side->Hext = Hext;
-    side->Hiec = Hiec;
-    side->Hanis = Hanis;
-    side->Hdemag = Hdemag;
-  }
-  // --- solveLLG (716-815)
-  const double GYRO = c.gyro;
-  const double damping = L.damping;
-  const D3 prod = cross(m, H);
-  const D3 prod2 = cross(m, prod);
-  const double convTerm = 1 / (1 + damping * damping);
-  const D3 dmdt = prod + prod2 * damping;
-  D3 reference = zero3();
-  if (L.referenceType == CMTJ_REF_FIXED) reference = load3(L.ref);
-  else if (L.referenceType == CMTJ_REF_TOP) reference = top;
-  else if (L.referenceType == CMTJ_REF_BOTTOM) reference = bottom;
-  if (L.includeSTT) {
-    const double I = drv(L.drv[CMTJ_SLOT_CURRENT], time, dc);
-    if (side) side->I = I;
-    const double aJ = c.hbar * I / (c.echarge * L.Ms * L.thickness);
-    double eta = 0;
-    if (L.alternativeSTT) {
-      eta = (L.spinPolarisation) / (1 + L.slonczewski * dot(m, reference));
-    } else {
-      const double slonSq = L.slonczewski * L.slonczewski;
-      eta = (L.spinPolarisation * slonSq) / (slonSq + 1 + (slonSq - 1) * dot(m, reference));
-    }
-    const double sttTerm = GYRO * aJ * eta;
-    const D3 fieldLike = cross(m, reference);
-    const D3 dampingLike = cross(m, fieldLike);
-    return (dmdt * -GYRO + dampingLike * -sttTerm * L.kappa + fieldLike * sttTerm * L.beta) * convTerm;
-  } else if (L.includeSOT) {
-    double Hdl = 0, Hfl = 0, Hdl2 = 0, Hfl2 = 0;
-    if (L.dynamicSOT) {
-      Hdl = drv(L.drv[CMTJ_SLOT_DL], time, dc);
-      Hfl = drv(L.drv[CMTJ_SLOT_FL], time, dc);
-      Hdl2 = drv(L.drv[CMTJ_SLOT_DL2], time, dc);
-      Hfl2 = drv(L.drv[CMTJ_SLOT_FL2], time, dc);
-    } else {
-      const double I = drv(L.drv[CMTJ_SLOT_CURRENT], time, dc);
-      if (side) side->I = I;
-      Hdl = L.dampingLikeTorque * I;
-      Hfl = L.fieldLikeTorque * I;
-    }
-    const D3 ref2 = load3(L.ref2);
-    if (side) {
-      side->Hfl = reference * (Hfl - damping * Hdl);
-      side->Hdl = reference * (Hdl + damping * Hfl);
-    }
-    const D3 cm_p = cross(m, reference);
-    const D3 ccm_p = cross(m, cm_p);
-    const D3 cm_s = cross(m, ref2);
-    const D3 ccm_s = cross(m, cm_s);
-    const D3 flp = cm_p * (Hfl - damping * Hdl);
-    const D3 dlp = ccm_p * (Hdl + damping * Hfl);
-    const D3 fls = cm_s * (Hfl2 - damping * Hdl2);
-    const D3 dls = ccm_s * (Hdl2 + damping * Hfl2);
-    return (dmdt + flp + dlp + fls + dls) * -GYRO * convTerm;
-  }
-  return dmdt * -GYRO * convTerm;
-}
-
-// stochasticTorque (junction.hpp:824-831).
-__device__ __forceinline__ D3 stoch_torque(const cmtj_layer_t &L, const cmtj_constants_t &c, const D3 &m,
-                                           const D3 &dW) {
-  const double convTerm = -c.gyro / (1. + L.damping * L.damping);
-  const D3 th = cross(m, dW);
-  const D3 th2 = cross(m, th);
-  return (th + th2 * L.damping) * convTerm;
-}
-
-// getStochasticLangevinVector (junction.hpp:1111-1128).
-__device__ __forceinline__ D3 langevin(const cmtj_layer_t &L, const cmtj_constants_t &c, double time,
-                                       uint32_t i, const DriverCtx &dc) {
-  if (!L.temperatureSet) return zero3();
-  const double temp = drv(L.drv[CMTJ_SLOT_TEMPERATURE], time, dc);
-  const double mainFactor = (2 * L.damping * c.kB * temp) / (L.Ms * L.cellVolume * c.gyro);
-  const double sigma = sqrt(mainFactor);
-  double g0, g1, g2;
-  cmtj_gaussian3_f64(L.seed_lo, L.seed_hi, L.noise_step + i, g0, g1, g2);
-  return d3(g0, g1, g2) * sigma;
-}
 
 __global__ void __launch_bounds__(64) k_run_simulation_f64(const cmtj_junction_t *__restrict__ junctions,
                                                            int32_t n_junctions, cmtj_layer_t *layers,
@@ -249,7 +32,6 @@ __global__ void __launch_bounds__(64) k_run_simulation_f64(const cmtj_junction_t
     return;
   }
   cmtj_layer_t *Ls = layers + J.layer_offset;
-  const cmtj_constants_t c = p.c;
   const double dt = p.time_step;
 
   D3 mag[CMTJ_MAX_LAYERS];
@@ -263,123 +45,14 @@ __global__ void __launch_bounds__(64) k_run_simulation_f64(const cmtj_junction_t
   const bool energies = p.calculate_energies != 0;
   uint32_t row = 0, code = CMTJ_STATUS_OK;
   double *out = log + (size_t)j * p.n_log * p.log_width;
-
   for (uint32_t i = 0; i < p.total_iterations; ++i) {
     const double t = (double)i * dt;
-    if (p.solver == CMTJ_RK4) {
-      // runSingleLayerSolver / runMultiLayerSolver (1668-1707): neighbours
-      // frozen at their start-of-step values for all four stages.
-      work[0] = zero3();
-      work[n + 1] = zero3();
-      for (int l = 0; l < n; ++l) work[l + 1] = mag[l];
-      bool nan_seen = false;
-      for (int l = 0; l < n; ++l) {
-        const cmtj_layer_t &L = Ls[l];
-        const D3 bottom = work[l], top = work[l + 2];
-        DriverCtx d0 = {tables, i, 0}, d1 = {tables, i, 1}, d2 = {tables, i, 2};
-        // Layer::rk4_step (1017-1041)
-        D3 m_t = mag[l];
-        const D3 k1 = rhs(L, c, t, m_t, bottom, top, d0, nullptr) * dt;
-        const D3 k2 = rhs(L, c, t + 0.5 * dt, m_t + k1 * 0.5, bottom, top, d1, nullptr) * dt;
-        const D3 k3 = rhs(L, c, t + 0.5 * dt, m_t + k2 * 0.5, bottom, top, d1, nullptr) * dt;
-        const D3 k4 = rhs(L, c, t + dt, m_t + k3, bottom, top, d2, energies ? &side[l] : nullptr) * dt;
-        m_t = m_t + (k1 + (k2 * 2.0) + (k3 * 2.0) + k4) / 6.0;
-        mag[l] = normalized(m_t);
-        if (isnan(mag[l].x)) {
-          nan_seen = true;
-          break;
-        }
-      }
-      if (nan_seen) {
-        code = CMTJ_STATUS_NAN;
-        break;
-      }
-    } else if (p.solver == CMTJ_EULER_HEUN) {
-      // eulerHeunSolverStep (1709-1754)
-      for (int l = 0; l < n; ++l) {
-        const cmtj_layer_t &L = Ls[l];
-        DriverCtx d0 = {tables, i, 0};
-        const D3 dW = langevin(L, c, t, i, d0);
-        const D3 bottom = (l == 0) ? zero3() : mag[l - 1];
-        const D3 top = (l == n - 1) ? zero3() : mag[l + 1];
-        const D3 f = rhs(L, c, t, mag[l], bottom, top, d0, energies ? &side[l] : nullptr);
-        const D3 g = stoch_torque(L, c, mag[l], dW);
-        const D3 mNext = mag[l] + g * sqrt(dt);
-        const D3 g2 = stoch_torque(L, c, mNext, dW);
-        work[l] = mag[l] + f * dt + smul(0.5, g + g2) * sqrt(dt);
-      }
-      for (int l = 0; l < n; ++l) mag[l] = normalized(work[l]);
-    } else {
-      // heunSolverStep (1756-1815)
-      D3 fn[CMTJ_MAX_LAYERS], gn[CMTJ_MAX_LAYERS], dW[CMTJ_MAX_LAYERS];
-      for (int l = 0; l < n; ++l) {
-        const cmtj_layer_t &L = Ls[l];
-        DriverCtx d0 = {tables, i, 0};
-        const D3 bottom = (l == 0) ? zero3() : mag[l - 1];
-        const D3 top = (l == n - 1) ? zero3() : mag[l + 1];
-        fn[l] = rhs(L, c, t, mag[l], bottom, top, d0, nullptr);
-        dW[l] = langevin(L, c, t, i, d0);
-        gn[l] = stoch_torque(L, c, mag[l], dW[l]);
-        work[l] = mag[l] + fn[l] * dt + gn[l] * sqrt(dt);
-      }
-      for (int l = 0; l < n; ++l) {
-        const cmtj_layer_t &L = Ls[l];
-        DriverCtx d2 = {tables, i, 2};
-        const D3 bottom = (l == 0) ? zero3() : work[l - 1];
-        const D3 top = (l == n - 1) ? zero3() : work[l + 1];
-        const D3 f2 = rhs(L, c, t + dt, work[l], bottom, top, d2, energies ? &side[l] : nullptr);
-        const D3 g2 = stoch_torque(L, c, work[l], dW[l]);
-        mag[l] = mag[l] + smul(0.5 * dt, fn[l] + f2) + smul(0.5, gn[l] + g2) * sqrt(dt);
-        mag[l] = normalized(mag[l]);
-      }
+    if (!junction_step(n, Ls, mag, work, side, i, t, p, tables, nullptr, false)) {
+      code = CMTJ_STATUS_NAN;
+      break;
     }
-
     if (!(i % p.write_every)) {
-      // logLayerParams (1580-1636)
-      double *r = out + (size_t)row * p.log_width;
-      int col = 0;
-      for (int l = 0; l < n; ++l) {
-        if (energies) {
-          const Side &s = side[l];
-          r[col++] = s.K;
-          r[col++] = s.K2;
-          r[col++] = s.Jb;
-          r[col++] = s.Jt;
-          r[col++] = s.I;
-          const D3 v[7] = {s.Hext, s.Hiec, s.Hanis, s.Hdemag, zero3(), s.Hfl, s.Hdl};
-          for (int q = 0; q < 7; ++q) {
-            r[col++] = v[q].x;
-            r[col++] = v[q].y;
-            r[col++] = v[q].z;
-          }
-        }
-        r[col++] = mag[l].x;
-        r[col++] = mag[l].y;
-        r[col++] = mag[l].z;
-      }
-      double r0 = 0.0, r1 = 0.0, r2 = 0.0;
-      if (J.mr_mode == CMTJ_MR_CLASSIC && n == 1) {
-        const double cosT = dot(mag[0], load3(Ls[0].ref));
-        r0 = J.Rp + (((J.Rap - J.Rp) / 2.0) * (1.0 - cosT));
-      } else if (J.mr_mode == CMTJ_MR_CLASSIC && n > 1) {
-        const double cosT = dot(mag[0], mag[1]);
-        r0 = J.Rp + (((J.Rap - J.Rp) / 2.0) * (1.0 - cosT));
-      } else if (J.mr_mode == CMTJ_MR_STRIP) {
-        // stripMagnetoResistance (1835-1857)
-        double Rx_acc = 0.0, Ry_acc = 0.0;
-        for (int l = 0; l < n; ++l) {
-          const double Rx = J.Rx0[l] + J.AMR_X[l] * (mag[l].x * mag[l].x) + J.SMR_X[l] * (mag[l].y * mag[l].y);
-          const double Ry = J.Ry0[l] + 0.5 * J.AHE[l] * mag[l].z + (J.AMR_Y[l] + J.SMR_Y[l]) * mag[l].x * mag[l].y;
-          Rx_acc = Rx_acc + 1. / Rx;
-          Ry_acc = Ry_acc + 1. / Ry;
-        }
-        r0 = 1 / Rx_acc;
-        r1 = 1 / Ry_acc;
-      }
-      r[col++] = r0;
-      r[col++] = r1;
-      r[col++] = r2;
-      r[col++] = t;
+      log_row(out + (size_t)row * p.log_width, J, n, Ls, mag, side, t, energies);
       ++row;
     }
   }

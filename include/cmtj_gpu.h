@@ -175,8 +175,8 @@ int cmtj_device_info(int device, int32_t *sm_count, int32_t *cc_major, int32_t *
 /* sizeof of the structs of this header, in this order: cmtj_driver_t,
  * cmtj_layer_t, cmtj_junction_t, cmtj_constants_t, cmtj_sim_params_t,
  * cmtj_wave_t, cmtj_f32_layer_t, cmtj_f32_junction_t, cmtj_f32_state_t,
- * cmtj_f32_params_t (the first n <= 10); lets a binding check its mirror of
- * the layout. */
+ * cmtj_f32_params_t, cmtj_stack_t (the first n <= 11); lets a binding check
+ * its mirror of the layout. */
 int cmtj_struct_sizes(int32_t *sizes, int32_t n);
 
 /* ---------------------------------------------------------------------- */
@@ -195,6 +195,37 @@ int cmtj_run_simulation_f64(const cmtj_junction_t *d_junctions, int32_t n_juncti
                             cmtj_layer_t *d_layers, const double *d_tables,
                             const cmtj_sim_params_t *p, double *d_log,
                             uint32_t *d_status, void *stream);
+
+/* ---------------------------------------------------------------------- */
+/* Electrically coupled stacks (core/stack.hpp), FP64 plain form.          */
+/* ---------------------------------------------------------------------- */
+enum cmtj_stack_kind { CMTJ_STACK_SERIES = 0, CMTJ_STACK_PARALLEL = 1 };
+
+/* One SeriesStack / ParallelStack (stack.hpp:16-480). */
+typedef struct cmtj_stack {
+  int32_t first_junction;    /* its junctions: [first, first + n_junctions) */
+  int32_t n_junctions;       /* 2 .. 256                                     */
+  int32_t kind;              /* enum cmtj_stack_kind                          */
+  int32_t use_kcl;           /* runSimulationKCL (1) or NonKCL (0)            */
+  int32_t delayed;           /* non-KCL: coupling from frozen magnetisations  */
+  int32_t single_layer_runner; /* last junction has one layer (RK4): every
+                                  junction steps only its layer 0 (stack.hpp:48-57) */
+  int32_t coupling_offset, n_coupling; /* 1 value, or n_junctions-1 values  */
+  double phase_offset;
+  double pol[3];             /* polarisation when not a 2-layer stack        */
+  cmtj_driver_t current;     /* the coupled current driver                    */
+} cmtj_stack_t;
+
+/* Stack::runSimulation (stack.hpp:311-423) for n_stacks stacks, one CTA
+ * each.  d_top_bottom[2*j] / [2*j+1]: index (within junction j) of the
+ * topId layer and of the bottomId layer (-1: use cmtj_stack_t.pol).
+ * Junction logs as cmtj_run_simulation_f64; the stack log is
+ * [n_stacks][p->n_log][stack_width] doubles per row: Resistance,
+ * I_0..I_{N-1}, C_0_1..C_{N-2}_{N-1}, time (stack_width >= 2*max_junctions+1). */
+int cmtj_run_stack_f64(const cmtj_stack_t *d_stacks, int32_t n_stacks, const double *d_couplings,
+                       const cmtj_junction_t *d_junctions, const int32_t *d_top_bottom, cmtj_layer_t *d_layers,
+                       const double *d_tables, const cmtj_sim_params_t *p, double *d_log, double *d_stack_log,
+                       int32_t stack_width, int32_t max_junctions, uint32_t *d_status, void *stream);
 
 /* ---------------------------------------------------------------------- */
 /* FP32 batched form.                                                      */

@@ -267,3 +267,96 @@ def run_case(cm, name):
         m = j.getLayerMagnetisation(lid)
         mags[lid] = (m.x, m.y, m.z)
     return j, log, mags
+
+
+# --------------------------------------------------------------------------
+# Stacks (core/stack.hpp): STT junctions so that the coupled current moves m.
+# --------------------------------------------------------------------------
+def _stt_junction(cm, Ms, K, mag, anis, P=0.5):
+    l1 = cm.Layer.createSTTLayer("free", mag=_v(cm, mag), anis=_v(cm, anis), Ms=Ms, thickness=2e-9,
+                                 cellSurface=SURFACE, demagTensor=_demag(cm, DEMAG_Z), damping=0.02,
+                                 SlonczewskiSpacerLayerParameter=1.0, beta=0.1, spinPolarisation=P)
+    l1.setReferenceLayer(_v(cm, (1, 0, 0)))
+    j = cm.Junction([l1], 100, 200)
+    j.setLayerAnisotropyDriver("free", cm.constantDriver(K))
+    j.setLayerExternalFieldDriver("all", cm.AxialDriver(5e3, 1e3, 0))
+    return j
+
+
+def _stt_bilayer(cm, Ms, K, mag):
+    l1 = cm.Layer.createSTTLayer("free", mag=_v(cm, mag), anis=_v(cm, (1, 0, 0)), Ms=Ms, thickness=2e-9,
+                                 cellSurface=SURFACE, demagTensor=_demag(cm, DEMAG_Z), damping=0.02,
+                                 SlonczewskiSpacerLayerParameter=1.0, beta=0.0, spinPolarisation=0.4)
+    l1.setReferenceLayer(cm.Reference.bottom)
+    l2 = cm.Layer("bottom", mag=_v(cm, (1, 0, 0)), anis=_v(cm, (1, 0, 0)), Ms=1.4, thickness=3e-9,
+                  cellSurface=SURFACE, demagTensor=_demag(cm, DEMAG_Z), damping=0.02)
+    j = cm.Junction([l1, l2], 100, 200)
+    j.setLayerAnisotropyDriver("free", cm.constantDriver(K))
+    j.setLayerAnisotropyDriver("bottom", cm.constantDriver(5e4))
+    j.setIECDriver("free", "bottom", cm.constantDriver(-1e-4))
+    return j
+
+
+def stack_series_kcl(cm):
+    js = [_stt_junction(cm, 1.2, 1e3, (0.1, 0.2, 1), (1, 0, 0)),
+          _stt_junction(cm, 1.0, 2e3, (0.3, 0.2, 0.9), (1, 0.1, 0.3))]
+    s = cm.stack.SeriesStack(js)
+    s.setCouplingStrength(0.3)
+    s.setCoupledCurrentDriver(cm.constantDriver(5e10))
+    return s, dict(totalTime=2e-10, timeStep=1e-13, writeFrequency=1e-12)
+
+
+def stack_parallel_nonkcl(cm):
+    js = [_stt_junction(cm, 1.2, 1e3, (0.1, 0.2, 1), (1, 0, 0)),
+          _stt_junction(cm, 1.1, 1.5e3, (0.2, 0.1, 1), (1, 0, 0)),
+          _stt_junction(cm, 1.0, 2e3, (0.3, 0.2, 0.9), (1, 0.1, 0.3))]
+    s = cm.stack.ParallelStack(js, useKCL=False, phaseOffset=0.3)
+    s.setCouplingStrength([0.1, 0.25])
+    s.setCoupledCurrentDriver(cm.sineDriver(2e10, 3e10, 2e9, 0.1))
+    return s, dict(totalTime=2e-10, timeStep=1e-13, writeFrequency=1e-12)
+
+
+def stack_series_nondelayed(cm):
+    js = [_stt_bilayer(cm, 1.2, 1e3, (0.1, 0.2, 1)), _stt_bilayer(cm, 1.0, 2e3, (0.3, 0.1, 0.9))]
+    s = cm.stack.SeriesStack(js, useKCL=False, phaseOffset=0.2)
+    s.setDelayed(False)
+    s.setCouplingStrength(0.2)
+    s.setCoupledCurrentDriver(cm.sineDriver(0, 8e10, 3e9, 0))
+    return s, dict(totalTime=2e-10, timeStep=1e-13, writeFrequency=1e-12)
+
+
+def stack_parallel_kcl_bilayer(cm):
+    js = [_stt_bilayer(cm, 1.2, 1e3, (0.1, 0.2, 1)), _stt_bilayer(cm, 1.0, 2e3, (0.3, 0.1, 0.9))]
+    s = cm.stack.ParallelStack(js)
+    s.setCouplingStrength(0.4)
+    s.setCoupledCurrentDriver(cm.stepDriver(0, 6e10, 2e-11, 1.5e-10))
+    return s, dict(totalTime=2e-10, timeStep=1e-13, writeFrequency=2e-12)
+
+
+STACKS = {
+    "stack_series_kcl": stack_series_kcl,
+    "stack_parallel_nonkcl": stack_parallel_nonkcl,
+    "stack_series_nondelayed": stack_series_nondelayed,
+    "stack_parallel_kcl_bilayer": stack_parallel_kcl_bilayer,
+}
+
+
+def run_stack_case(cm, name):
+    """Build and run a stack case; returns (stack log, [junction logs]) as
+    dicts of numpy arrays."""
+    import numpy as np
+    s, r = STACKS[name](cm)
+    s.runSimulation(**r)
+    slog = {k: np.asarray(v, dtype=np.float64) for k, v in s.getLog().items()}
+    jlogs = []
+    for q in range(len(s.junctionList) if hasattr(s, "junctionList") else 0):
+        jlogs.append({k: np.asarray(v, dtype=np.float64) for k, v in s.getLog(q).items()})
+    if not jlogs:
+        q = 0
+        while True:
+            try:
+                jlogs.append({k: np.asarray(v, dtype=np.float64) for k, v in s.getLog(q).items()})
+            except RuntimeError:
+                break
+            q += 1
+    return slog, jlogs

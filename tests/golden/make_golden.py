@@ -41,13 +41,27 @@ def save_case(cm, name):
     return path, sum(v.size for v in log.values())
 
 
+def save_stack_case(cm, name):
+    import cases
+    slog, jlogs = cases.run_stack_case(cm, name)
+    out = {"stack__" + k: v for k, v in slog.items()}
+    for q, lg in enumerate(jlogs):
+        out.update({"j%d__%s" % (q, k): v for k, v in lg.items()})
+    path = os.path.join(HERE, name + ".npz")
+    np.savez_compressed(path, **out)
+    return path, sum(v.size for v in out.values())
+
+
 def main(argv):
     import cases
     cm = reference_module()
-    names = argv or list(cases.DETERMINISTIC)
+    names = argv or (list(cases.DETERMINISTIC) + list(cases.STACKS))
     for name in names:
-        path, n = save_case(cm, name)
-        print("%-20s %8d values  %7.1f KB" % (name, n, os.path.getsize(path) / 1024))
+        if name in cases.STACKS:
+            path, n = save_stack_case(cm, name)
+        else:
+            path, n = save_case(cm, name)
+        print("%-28s %8d values  %7.1f KB" % (name, n, os.path.getsize(path) / 1024))
 
 
 if __name__ == "__main__":

@@ -193,3 +193,26 @@ def test_run_plan_matches_reference_truncation():
     assert p.write_every == int(1e-12 / 1e-13)
     with pytest.raises(RuntimeError, match="cannot be larger than write frequency"):
         plan_run(1e-9, 1e-12, 1e-13)
+
+
+def test_stack_validation():
+    """stack.hpp:123-152 and test_stack.py's error contract."""
+    from cmtj_gb300.stack import ParallelStack, SeriesStack
+    l = _layer()
+    l.setReferenceLayer(CVector(1, 0, 0))
+    j = Junction([l], 100, 200)
+    with pytest.raises(RuntimeError, match="must have at least 2 junctions"):
+        ParallelStack([j])
+    with pytest.raises(RuntimeError, match="must have at least 2 junctions"):
+        SeriesStack([])
+    with pytest.raises(RuntimeError, match="Asking for id of a non-existing junction!"):
+        ParallelStack([j, j]).getLog(2)
+    with pytest.raises(TypeError):
+        SeriesStack([j, j]).getLog(-10)
+    with pytest.raises(RuntimeError, match="non-classic"):
+        SeriesStack([Junction([_layer("a")]), Junction([_layer("b")])])
+    s = SeriesStack([j, j])
+    with pytest.raises(RuntimeError, match="size of stack size - 1"):
+        s.setCouplingStrength([0.1, 0.2])
+    with pytest.raises(RuntimeError, match="only supported for 2 layer stacks"):
+        s.setDelayed(False)
