@@ -1,0 +1,58 @@
+"""Reference switching statistics for the stochastic (sLLGS) parity test.
+
+The reference draws its thermal field from an unseeded std::mt19937
+(junction.hpp:174-175), so thermal runs can only be compared in statistics.
+This script runs the reference extension (oracle/_ref, built from the
+reference sources) on the p-bit case of tests/thermal_cases.py: n runs per
+current density, Euler-Heun, T = 300 K, and records how many ended with
+m_z < 0.  Output: tests/golden/pbit_switching.npz.
+
+    python tests/golden/make_thermal.py [runs_per_current]
+"""
+import multiprocessing as mp
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+sys.path.insert(0, ROOT)
+
+
+def _worker(args):
+    ref_path, j_density, n = args
+    sys.path.insert(0, ref_path)
+    import cmtj
+    import thermal_cases
+    switched = 0
+    for _ in range(n):
+        junc, run = thermal_cases.pbit_junction(cmtj, j_density)
+        junc.runSimulation(**run)
+        if junc.getLayerMagnetisation("free").z < 0:
+            switched += 1
+    return switched
+
+
+def main(argv):
+    from oracle.build import build_reference
+    import thermal_cases
+    ref = build_reference()
+    if ref is None:
+        raise SystemExit("reference sources not available")
+    n = int(argv[0]) if argv else 512
+    currents = thermal_cases.PBIT_CURRENTS
+    chunks = 8
+    tasks = [(ref, float(j), n // chunks) for j in currents for _ in range(chunks)]
+    with mp.get_context("spawn").Pool(os.cpu_count()) as pool:
+        res = pool.map(_worker, tasks)
+    counts = np.array(res).reshape(len(currents), chunks).sum(axis=1)
+    np.savez_compressed(os.path.join(HERE, "pbit_switching.npz"), currents=np.asarray(currents),
+                        switched=counts, runs=np.full(len(currents), (n // chunks) * chunks))
+    for j, c in zip(currents, counts):
+        print("j=%.3g  P=%.3f" % (j, c / ((n // chunks) * chunks)))
+
+
+if __name__ == "__main__":
+    main(sys.argv[1:])

@@ -1,0 +1,77 @@
+"""Stochastic (sLLGS) parity on the CPU: the oracle's Philox thermal field
+against the reference's own switching statistics (tests/golden/
+pbit_switching.npz, from the reference extension with its mt19937) within a
+3-sigma binomial bound, and the stationary m_z density against the
+Boltzmann distribution of the uniaxial macrospin."""
+import numpy as np
+
+import cmtj_gb300
+import oracle_harness
+import thermal_cases
+
+
+def load_ref():
+    g = np.load("%s/golden/pbit_switching.npz" % thermal_cases.__file__.rsplit("/", 1)[0])
+    return g["currents"], g["switched"], g["runs"]
+
+
+def binomial_ok(k1, n1, k2, n2):
+    p1, p2 = k1 / n1, k2 / n2
+    p = (k1 + k2) / (n1 + n2)
+    bound = 3 * np.sqrt(max(p * (1 - p), 1.0 / (n1 + n2)) * (1.0 / n1 + 1.0 / n2))
+    return abs(p1 - p2) <= bound, abs(p1 - p2), bound
+
+
+def seeded_pbits(cm, j_density, n, seed0):
+    out = []
+    for k in range(n):
+        j, run = thermal_cases.pbit_junction(cm, j_density)
+        j.layers[0].noise_seed = seed0 + k
+        out.append(j)
+    return out, run
+
+
+def test_oracle_switching_matches_reference_statistics():
+    cur, sw, runs = load_ref()
+    n = 1024
+    for q, jd in enumerate(cur):
+        js, run = seeded_pbits(cmtj_gb300, float(jd), n, 1000 * q + 17)
+        r = dict(run)
+        oracle_harness.run_oracle(js, r.pop("totalTime"), threads=8, **r)
+        k = sum(1 for j in js if j.getLayerMagnetisation("free").z < 0)
+        ok, d, b = binomial_ok(k, n, int(sw[q]), int(runs[q]))
+        assert ok, (jd, k / n, sw[q] / runs[q], d, b)
+
+
+def test_oracle_boltzmann_equilibrium():
+    """j = 0, barrier 1.5 kT: pooled m_z samples after 1 ns of burn-in
+    follow p(m_z) ~ exp(Ku V m_z^2 / kT) (histogram within 4 sigma)."""
+    V = 7e-17 * 1.2e-9
+    Ku = 1.5 * 1.380649e-23 * 300 / V
+    js = []
+    for k in range(128):
+        j, run = thermal_cases.pbit_junction(cmtj_gb300, 0.0, Ku=Ku)
+        j.layers[0].noise_seed = 77 + k
+        if k % 2:
+            j.setLayerMagnetisation("free", cmtj_gb300.CVector(0, 0, -1))  # both wells start populated
+        js.append(j)
+    oracle_harness.run_oracle(js, 1.2e-8, 1e-13, 2e-11, solverMode=cmtj_gb300.SolverMode.EulerHeun, threads=8)
+    mz = np.concatenate([np.asarray(j.getLogArrays()["free_mz"])[100:] for j in js])
+    check_density(mz, Ku, V)
+
+
+def check_density(mz, Ku, V, bins=10, sigmas=4.0):
+    """Histogram of |m_z| against the folded Boltzmann density.  The density
+    is even in m_z; folding removes the slow population exchange between the
+    two wells, whose few independent samples say nothing about the shape."""
+    a = np.abs(np.asarray(mz))
+    edges = np.linspace(0, 1, bins + 1)
+    h, _ = np.histogram(a, bins=edges)
+    x = np.linspace(0, 1, 20001)
+    p = 2 * thermal_cases.boltzmann_mz_density(x, Ku, V, 300.0)
+    expect = np.array([np.trapezoid(p[(x >= lo) & (x <= hi)], x[(x >= lo) & (x <= hi)])
+                       for lo, hi in zip(edges[:-1], edges[1:])]) * a.size
+    # samples are correlated in time: inflate the Poisson variance
+    corr = 8.0
+    z = (h - expect) / np.sqrt(corr * np.maximum(expect, 1.0))
+    assert np.max(np.abs(z)) < sigmas, (np.round(z, 2), h, np.round(expect))

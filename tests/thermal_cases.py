@@ -1,0 +1,38 @@
+"""Stochastic cases written against the `cmtj` API (reference or
+cmtj_gb300).
+
+p-bit: one STT free layer (Ms 1.0 T, t 1.2 nm, surface 7e-17 m^2, alpha
+0.02, zero demag, Slonczewski polarisation 0.6, reference -z), Ku chosen so
+the barrier is about 3 kT at 300 K, m from +z, a 1 ns current step, 2 ns in
+total at dt = 1e-13 with Euler-Heun.  The observable is P(m_z < 0 at the
+end) per current density."""
+import math
+
+PBIT_CURRENTS = [0.0, 2e10, 4e10, 6e10, 8e10, 1e11, 1.5e11, 3e11]
+PBIT_KU = 1.5e5
+PBIT_T = 300.0
+
+
+def pbit_junction(cm, j_density, Ku=PBIT_KU, T=PBIT_T):
+    z = cm.CVector(0, 0, 0)
+    l = cm.Layer.createSTTLayer("free", mag=cm.CVector(0, 0, 1), anis=cm.CVector(0, 0, 1), Ms=1.0,
+                                thickness=1.2e-9, cellSurface=7e-17, demagTensor=[z, z, z], damping=0.02,
+                                SlonczewskiSpacerLayerParameter=1.0, beta=0.0, spinPolarisation=0.6)
+    l.setReferenceLayer(cm.CVector(0, 0, -1))
+    j = cm.Junction([l])
+    j.setLayerAnisotropyDriver("free", cm.constantDriver(Ku))
+    j.setLayerCurrentDriver("free", cm.stepDriver(0, j_density, 0, 1e-9))
+    j.setLayerTemperatureDriver("free", cm.constantDriver(T))
+    return j, dict(totalTime=2e-9, timeStep=1e-13, writeFrequency=1e-10,
+                   solverMode=cm.SolverMode.EulerHeun)
+
+
+def boltzmann_mz_density(mz, Ku, V, T, kB=1.380649e-23):
+    """Equilibrium density of m_z for a uniaxial macrospin with zero demag
+    and no field: p(m_z) proportional to exp(Ku V m_z^2 / kB T) on [-1, 1]
+    (the sin(theta) of the solid angle is absorbed by d m_z)."""
+    import numpy as np
+    d = Ku * V / (kB * T)
+    x = np.linspace(-1, 1, 20001)
+    Z = np.trapezoid(np.exp(d * x * x), x)
+    return np.exp(d * np.asarray(mz) ** 2) / Z
