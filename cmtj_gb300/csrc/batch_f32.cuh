@@ -402,7 +402,7 @@ template <int L> __device__ __forceinline__ int log_channels(int mode) {
 // Resident CTAs of 128 threads per SM the specialised variants are built
 // for (register cap); the catch-all CMTJ_FEAT_ALL variants take what they need.
 #ifndef CMTJ_BATCH_MINB
-#define CMTJ_BATCH_MINB 4
+#define CMTJ_BATCH_MINB 5
 #endif
 
 template <int L, int SOLVER, int FEAT, int NW>
