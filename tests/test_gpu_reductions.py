@@ -1,0 +1,117 @@
+"""On-device reductions against FP64:
+
+* spin-diode mixing <I(t) R(t)> (compute.hpp:75-76 form; resistance.py:12-22
+  without the low-pass) accumulated in the FP32 batch kernel with
+  compensated sums, on uneven 1-4 layer junctions of the spin-diode sweep,
+  against the mean over the oracle's FP64 trajectory;
+* the PIMM spectrum (procedures.py:28-39): cmtj_spectrum_f32 on the FP32 log
+  against numpy's FFT of the same log (the FFT itself) and of the FP64
+  trajectory (end to end)."""
+import numpy as np
+import pytest
+
+import cmtj_gb300 as cm
+import oracle_harness
+from cmtj_gb300 import _abi, batch, engine, sweeps
+
+DT = 1e-13
+
+
+def junctions_from_spec(spec, rows, oersted=None):
+    """Junction objects for rows of a sweeps.* spec (constant parts only;
+    `oersted(k)` returns the AxialDriver of row k's time-dependent field)."""
+    out = []
+    for k in rows:
+        L = int(spec.n_layers[k])
+        layers = []
+        for l in range(L):
+            d = [cm.CVector(*spec.demag[k, l, 3 * r:3 * r + 3]) for r in range(3)]
+            ly = cm.Layer("L%d" % l, cm.CVector(*spec.m0[k, l]), cm.CVector(*spec.anis[k, l]), float(spec.Ms[k, l]),
+                          float(spec.thickness[k, l]), float(spec.surface[k, l]), d, float(spec.alpha[k, l]))
+            ly.setAnisotropyDriver(cm.constantDriver(float(spec.K[k, l])))
+            ly.setExternalFieldDriver(cm.AxialDriver(*[float(x) for x in spec.Hc[k, l]]))
+            if oersted is not None:
+                ly.setOerstedFieldDriver(oersted(k))
+            ly.mag = cm.CVector(*spec.m0[k, l])  # exact start, no renormalisation
+            layers.append(ly)
+        if spec.mr_mode[k] == 1:
+            if L == 1:
+                layers[0].setReferenceLayer(cm.CVector(*spec.ref[k, 0]))
+            j = cm.Junction(layers, float(spec.Rp[k]), float(spec.Rap[k]))
+        else:
+            j = cm.Junction(layers)
+        for l in range(L - 1):
+            j.setIECDriver("L%d" % l, "L%d" % (l + 1), cm.constantDriver(float(spec.Jt[k, l])))
+        out.append(j)
+    return out
+
+
+@pytest.mark.gpu
+def test_vsd_mixing_voltage_matches_fp64(gpu_lib):
+    spec, _ = sweeps.vsd_config(n_f=4, n_h=8, seed=9, dt=DT, amp=5e3)
+    batch.relax(spec, DT, 20000, alpha=1.0)
+    n_steps = 20000
+    low = batch.lower(spec, DT, n_steps)
+    run = batch.BatchRun(low, DT, cm.SolverMode.RK4, batch.LOG_NONE, 0, red_every=1)
+    run.launch()
+    st = run.state()
+    assert np.all(st["status"] == 0) and np.all(st["n_red"] == n_steps)
+    v32 = (st["v_sum"].astype(np.float64) + st["v_c"]) / n_steps
+    rows = list(range(spec.n))
+    js = junctions_from_spec(spec, rows, lambda k: cm.AxialDriver(cm.NullDriver(),
+                                                                     cm.sineDriver(0, 5e3, float(spec.vsd_freq[k]), 0),
+                                                                     cm.NullDriver()))
+    oracle_harness.run_oracle(js, n_steps * DT, DT, DT, threads=8)
+    for q, k in enumerate(rows):
+        lg = js[q].getLogArrays()
+        L = int(spec.n_layers[k])
+        t = lg["time"]
+        if spec.mr_mode[k] == 1:
+            R = lg["R"] if L == 1 else lg["R_L0_L1"]
+            scale = spec.Rap[k] - spec.Rp[k]
+        else:
+            R = sum(spec.strip[k, 0, l] + spec.strip[k, 2, l] * lg["L%d_mx" % l] ** 2 +
+                    spec.strip[k, 4, l] * lg["L%d_my" % l] ** 2 for l in range(L))
+            scale = sum(abs(spec.strip[k, 2, l]) + abs(spec.strip[k, 4, l]) for l in range(L))
+        I = np.sin(2 * np.pi * spec.vsd_freq[k] * t)
+        v64 = float(np.mean(I * R))
+        assert abs(v32[k] - v64) <= 1e-4 * scale, (k, L, v32[k], v64)
+
+
+@pytest.mark.gpu
+def test_pimm_spectrum_matches_numpy_and_fp64(gpu_lib):
+    spec, _ = sweeps.pimm_config(n_h=16, n_draw=1, dt=DT)
+    batch.relax(spec, DT, 30000, alpha=1.0)
+    n_steps, every, nfft = 10240, 10, 1024
+    low = batch.lower(spec, DT, n_steps)
+    run = batch.BatchRun(low, DT, cm.SolverMode.RK4, batch.LOG_MIX, every, log_axis=0)
+    run.launch()
+    lib = _abi.load()
+    t = engine.torch()
+    samples = int(run.samples[0])
+    out = t.empty((spec.n, nfft // 2 - 1), dtype=t.float32, device="cuda")
+    rc = lib.cmtj_spectrum_f32(engine.ptr(run.d_log), int(run.log_pad[0]), spec.n, samples, nfft, 1, nfft // 2,
+                               engine.ptr(out), engine.stream_ptr())
+    _abi.check(rc, lib)
+    gpu = out.cpu().numpy()
+    log = run.d_log.cpu().numpy()
+    js = junctions_from_spec(spec, range(spec.n), lambda k: cm.AxialDriver(cm.stepDriver(0, 1e3, 0, 1e-12),
+                                                                            cm.NullDriver(), cm.NullDriver()))
+    for j in js:
+        j.setLayerAnisotropyDriver("L1", cm.constantDriver(1e6))
+    oracle_harness.run_oracle(js, n_steps * DT, DT, DT * every, threads=8)
+    eps32 = np.finfo(np.float32).eps
+    for k in range(spec.n):
+        x32 = run.log_of(k, log)[:, 0].astype(np.float64)
+        ref_fft = np.abs(np.fft.fft(x32[-nfft:]))[1:nfft // 2]
+        # FP32 FFT rounding: per bin about eps * log2(N) * ||x||_2 (the DC
+        # part of x dominates ||x||, not the ringing)
+        fft_tol = 4 * eps32 * np.log2(nfft) * np.linalg.norm(x32[-nfft:])
+        assert np.max(np.abs(gpu[k] - ref_fft)) <= fft_tol, (k, np.max(np.abs(gpu[k] - ref_fft)), fft_tol)
+        lg = js[k].getLogArrays()
+        w = spec.mix_w[k, :2]
+        x64 = w[0] * lg["L0_mx"] + w[1] * lg["L1_mx"]
+        fft64 = np.abs(np.fft.fft(x64[-nfft:]))[1:nfft // 2]
+        # trajectory error (max|dm| <= 1e-4 per sample) plus FFT rounding
+        traj_tol = 1e-4 * nfft
+        assert np.max(np.abs(gpu[k] - fft64)) <= traj_tol + fft_tol, k

@@ -1,0 +1,46 @@
+"""Continuous batching (cmtj_gb300.serving): requests of mixed kinds
+(2-layer RK4, 1-layer thermal Euler-Heun, uneven 1-4-layer spin-diode with
+on-device <I R>) arrive while others run; each request's results are the
+same alone and in the mix, at any tick length (the FP32 form's tolerance
+is 1e-4; the bits agree)."""
+import numpy as np
+import pytest
+
+from cmtj_gb300 import serving
+
+
+def _trace():
+    return serving.make_trace(8, rate_hz=400.0, seed=11, min_solves=64, max_solves=512, t_min=2e-10, t_max=8e-10)
+
+
+@pytest.mark.gpu
+def test_serving_results_same_alone_and_in_mix(gpu_lib):
+    mix = _trace()
+    eng = serving.ServingEngine(hbm_budget_bytes=256 << 20, chunk_steps=500)
+    done = eng.run(mix)
+    assert all(r.done_at is not None for r in done)
+    assert all(np.all(r.state["status"] == 0) for r in done)
+    for k in (0, 3, 6):
+        alone = _trace()[k]
+        alone.arrival = 0.0
+        e2 = serving.ServingEngine(hbm_budget_bytes=64 << 20, chunk_steps=700)  # other tick length
+        e2.run([alone])
+        a, b = done[k].state, alone.state
+        assert np.array_equal(a["step"], b["step"])
+        assert float(np.max(np.abs(a["m"] - b["m"]))) <= 1e-4
+        assert np.array_equal(a["m"], b["m"]), k
+        if done[k].red_every:
+            assert np.array_equal(a["r_sum"], b["r_sum"]) and np.array_equal(a["v_sum"], b["v_sum"])
+
+
+@pytest.mark.gpu
+def test_serving_admission_waits_for_hbm_budget(gpu_lib):
+    """A pool smaller than the sum of the requests: later requests wait for
+    slots and still complete."""
+    reqs = serving.make_trace(6, rate_hz=1e6, seed=5, min_solves=200, max_solves=300, t_min=2e-10, t_max=3e-10)
+    per = serving.SlotPool.BYTES_PER_SLOT
+    eng = serving.ServingEngine(hbm_budget_bytes=per * 700, chunk_steps=1000)
+    assert eng.pool.capacity < sum(r.spec.n for r in reqs)
+    done = eng.run(reqs)
+    assert all(r.done_at is not None for r in done)
+    assert eng.pool.free == [(0, eng.pool.capacity)]
