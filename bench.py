@@ -426,7 +426,33 @@ def measure_rest(run, low, spec, n_steps, kern_ms, fft_ms, lib):
                                    % (len(rows), n_steps)}
     out["accuracy"] = {"max_abs_dm_final_vs_fp64": dm_final, "max_abs_dmix_logged_vs_fp64": dmix,
                        "tolerance": 1e-4, "sample_junctions": 256, "pass": max(dm_final, dmix) <= 1e-4}
+    out["serving"] = serving_leg(fp64_batch)
     out["cpu_baseline"] = cpu_baseline()
+    return out
+
+
+def serving_leg(fp64_rate, n_requests=200, rate_hz=200.0):
+    """Config-4 trace: Poisson arrivals at 200 req/s of requests holding
+    64-16,384 solves (log-uniform) of three kinds -- PIMM-style 2-layer RK4,
+    thermal 1-layer p-bit Euler-Heun at 300 K, uneven 1-4-layer spin-diode
+    RK4 with on-device <I R> -- each solve 2-40 ns at dt = 1e-13, served by
+    continuous batching (cmtj_gb300.serving).  Latency = completion minus
+    arrival, wall clock."""
+    from cmtj_gb300 import serving
+    reqs = serving.make_trace(n_requests, rate_hz=rate_hz, seed=3)
+    eng = serving.ServingEngine(hbm_budget_bytes=8 << 30, chunk_steps=4000)
+    t0 = time.perf_counter()
+    done = eng.run(reqs)
+    wall = time.perf_counter() - t0
+    out = serving.summary(done, wall)
+    offered = sum(r.layer_steps for r in done)
+    out.update({"trace": "%d requests, Poisson %.0f req/s, 64-16384 solves, 2-40 ns, pimm/pbit/vsd mix"
+                         % (n_requests, rate_hz),
+                "offered_layer_steps": offered,
+                "offered_over_span": offered / max(done[-1].arrival, 1e-9),
+                "ticks": eng.stats["ticks"], "host_s": eng.stats["host_s"],
+                "device_wait_s": eng.stats["device_wait_s"],
+                "fp64_plain_alone_estimate_s": offered / fp64_rate})
     return out
 
 

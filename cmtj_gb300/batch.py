@@ -31,7 +31,7 @@ TGT_HX, TGT_HY, TGT_HZ, TGT_K, TGT_K2, TGT_JB, TGT_JT, TGT_J2B, TGT_J2T = range(
 TGT_I, TGT_FL, TGT_DL, TGT_FL2, TGT_DL2, TGT_T = 9, 10, 11, 12, 13, 14
 
 FEAT_FULL_DEMAG, FEAT_DIPOLE, FEAT_IDMI, FEAT_K2 = 1, 2, 4, 8
-FEAT_STT, FEAT_SOT, FEAT_WAVES, FEAT_SCALAR_WAVES, FEAT_ALL = 16, 32, 64, 128, 255
+FEAT_STT, FEAT_SOT, FEAT_WAVES, FEAT_SCALAR_WAVES, FEAT_IEC2, FEAT_ALL = 16, 32, 64, 128, 256, 511
 
 F32_STT, F32_SOT, F32_SOT_STATIC, F32_ALT_STT = 1, 2, 4, 8
 LOG_NONE, LOG_M, LOG_MIX, LOG_R = 0, 1, 2, 3
@@ -463,6 +463,7 @@ def lower(spec, time_step, n_steps, win_start=None):
                      FEAT_DIPOLE, 0)
     feat |= np.where((((np.abs(spec.Db).sum(2) + np.abs(spec.Dt).sum(2)) > 0) & lmask).any(axis=1), FEAT_IDMI, 0)
     feat |= np.where(((spec.K2 != 0) & lmask).any(axis=1), FEAT_K2, 0)
+    feat |= np.where((((spec.J2b != 0) | (spec.J2t != 0)) & lmask).any(axis=1), FEAT_IEC2, 0)
     feat |= np.where((((spec.flags & F32_STT) != 0) & lmask).any(axis=1), FEAT_STT, 0)
     feat |= np.where((((spec.flags & F32_SOT) != 0) & lmask).any(axis=1), FEAT_SOT, 0)
     n_waves = np.zeros(n, dtype=np.int64)
@@ -473,6 +474,7 @@ def lower(spec, time_step, n_steps, win_start=None):
         used = np.arange(MAX_WAVES)[None, :] < n_waves[:, None]
         tg = spec.wave_table["target"]
         scal = np.isin(tg, [TGT_K, TGT_K2, TGT_JB, TGT_JT, TGT_J2B, TGT_J2T, TGT_T]) & used
+        feat |= np.where((np.isin(tg, [TGT_J2B, TGT_J2T]) & used).any(axis=1), FEAT_IEC2, 0)
         feat |= np.where(scal.any(axis=1), FEAT_SCALAR_WAVES, 0)
         feat |= np.where(((tg == TGT_K2) & used).any(axis=1), FEAT_K2, 0)
         feat |= np.where(n_waves > 0, FEAT_WAVES, 0)
@@ -490,6 +492,8 @@ def lower(spec, time_step, n_steps, win_start=None):
             tg = int(w["target"])
             if tg in (TGT_K, TGT_JB, TGT_JT, TGT_J2B, TGT_J2T, TGT_T):
                 feat[k] |= FEAT_SCALAR_WAVES
+            if tg in (TGT_J2B, TGT_J2T):
+                feat[k] |= FEAT_IEC2
             if tg == TGT_K2:
                 feat[k] |= FEAT_SCALAR_WAVES | FEAT_K2
         n_waves[k] = len(ws)

@@ -64,6 +64,7 @@ template <int FEAT> struct Feat {
   static constexpr bool sot = (FEAT & CMTJ_FEAT_SOT) != 0;
   static constexpr bool waves = (FEAT & CMTJ_FEAT_WAVES) != 0;
   static constexpr bool swaves = (FEAT & CMTJ_FEAT_SCALAR_WAVES) != 0;
+  static constexpr bool iec2 = (FEAT & CMTJ_FEAT_IEC2) != 0;
   static constexpr bool twaves = waves && (stt || sot);  // current / torque waves
 };
 
@@ -76,15 +77,15 @@ template <int FEAT> struct LayerP {
   F3 h0;
   float jb, jt, j2b, j2t;
   F3 dmib, dmit;
-  float gam, alpha;
+  float gam, gdt, alpha;  // -gamma/(1+alpha^2), and that times dt
   F3 ref, ref2;
   int rtype, flags;
-  float sttc, sttp, sttl, sttb, sttk, i0, fl0, dl0, fl20, dl20;
+  float sttc, sttp, sttl, sttb, sttk, i0, fl0, dl0, fl20, dl20;  // sttc carries dt
   float sigc, t0;
   uint32_t seed_lo, seed_hi;
   uint64_t nstep0;
 
-  __device__ __forceinline__ void load(const cmtj_f32_layer_t &r) {
+  __device__ __forceinline__ void load(const cmtj_f32_layer_t &r, float dtf) {
     using F = Feat<FEAT>;
     a = ld3(r.anis);
     kc = r.kc;
@@ -114,13 +115,14 @@ template <int FEAT> struct LayerP {
       dmit = ld3(r.dmi_t);
     }
     gam = r.gam;
+    gdt = r.gam * dtf;
     alpha = r.alpha;
     rtype = r.ref_type;
     flags = r.flags;
     if (F::stt || F::sot) {
       ref = ld3(r.ref);
       ref2 = ld3(r.ref2);
-      sttc = r.stt_c;
+      sttc = r.stt_c * dtf;
       sttp = r.stt_p;
       sttl = r.stt_l;
       sttb = r.stt_beta;
@@ -146,8 +148,10 @@ template <int FEAT> struct Delta {
   using F = Feat<FEAT>;
   F3 dH;
   float dK, dK2, dJb, dJt, dJ2b, dJ2t, dI, dFL, dDL, dFL2, dDL2, dT;
-  __device__ __forceinline__ void clear() {
-    dH = f3(0.f, 0.f, 0.f);
+  // dH starts at the layer's constant field h0, so the right-hand side
+  // reads the whole field from it without a separate add
+  __device__ __forceinline__ void clear(F3 h0) {
+    dH = h0;
     dK = dK2 = dJb = dJt = dJ2b = dJ2t = dI = dFL = dDL = dFL2 = dDL2 = dT = 0.f;
   }
   __device__ __forceinline__ void add(int target, float v) {
@@ -269,23 +273,26 @@ __device__ __forceinline__ void add_wave(const WaveR<L> &w, uint32_t step, int s
   }
 }
 
-// Effective field + LL torque of one layer (junction.hpp:580-815).
+// Effective field + LL torque of one layer (junction.hpp:580-815), returned
+// already multiplied by dt (the RK4 k, the Euler-Heun f dt).
 template <int FEAT, bool HB, bool HT>
 __device__ __forceinline__ F3 rhs(const LayerP<FEAT> &P, F3 m, F3 mb, F3 mt, const Delta<FEAT> &d) {
   using F = Feat<FEAT>;
-  F3 H = F::waves ? P.h0 + d.dH : P.h0;
+  F3 H = F::waves ? d.dH : P.h0;
   const float da = dot(P.a, m);
   float ka = F::swaves ? P.kc + d.dK : P.kc;
   if (F::k2) ka = fmaf(F::swaves ? P.k2c + d.dK2 : P.k2c, da * da, ka);
   H = fma3(P.a, ka * da, H);
   if (HB) {
-    const float cb = fmaf(F::swaves ? P.j2b + d.dJ2b : P.j2b, dot(mb, m), F::swaves ? P.jb + d.dJb : P.jb);
+    const float jb = F::swaves ? P.jb + d.dJb : P.jb;
+    const float cb = F::iec2 ? fmaf(F::swaves ? P.j2b + d.dJ2b : P.j2b, dot(mb, m), jb) : jb;
     H = fma3(mb, cb, H);
     if (F::idmi) H = H + cross(mb, P.dmib);
     if (F::dipole) H = H - matvec(P.Db, mb);
   }
   if (HT) {
-    const float ct = fmaf(F::swaves ? P.j2t + d.dJ2t : P.j2t, dot(mt, m), F::swaves ? P.jt + d.dJt : P.jt);
+    const float jt = F::swaves ? P.jt + d.dJt : P.jt;
+    const float ct = F::iec2 ? fmaf(F::swaves ? P.j2t + d.dJ2t : P.j2t, dot(mt, m), jt) : jt;
     H = fma3(mt, ct, H);
     if (F::idmi) H = H + cross(mt, P.dmit);
     if (F::dipole) H = H - matvec(P.Dt, mt);
@@ -315,8 +322,8 @@ __device__ __forceinline__ F3 rhs(const LayerP<FEAT> &P, F3 m, F3 mb, F3 mt, con
       const float s = P.sttc * I * eta;
       const F3 fl = cross(m, p);
       const F3 dl = cross(m, fl);
-      // gam * dmdt already carries -gamma/(1+alpha^2); sttc carries 1/(1+alpha^2).
-      return fma3(fl, s * P.sttb, fma3(dl, -s * P.sttk, acc * P.gam));
+      // gdt carries -gamma dt/(1+alpha^2); sttc carries dt/(1+alpha^2).
+      return fma3(fl, s * P.sttb, fma3(dl, -s * P.sttk, acc * P.gdt));
     }
     if (F::sot && (P.flags & CMTJ_F32_SOT)) {
       float hfl, hdl, hfl2 = 0.f, hdl2 = 0.f;
@@ -338,7 +345,7 @@ __device__ __forceinline__ F3 rhs(const LayerP<FEAT> &P, F3 m, F3 mb, F3 mt, con
       acc = fma3(cross(m, cs), fmaf(P.alpha, hfl2, hdl2), acc);
     }
   }
-  return acc * P.gam;
+  return acc * P.gdt;
 }
 
 // stochasticTorque (junction.hpp:824-831).
@@ -425,7 +432,7 @@ __global__ void __launch_bounds__(128, (FEAT == CMTJ_FEAT_ALL) ? 1 : CMTJ_BATCH_
   int32_t jid = -1;
   bool retired = false;
   uint32_t step = 0, end = 0, stop_all = 0, n_logged = 0, tcount = 0, n_red = 0, win = 0;
-  uint32_t log_cd = 0, red_cd = 0;  // steps until the next log / reduction sample
+  uint32_t next_log = 0xffffffffu, next_red = 0xffffffffu;  // next steps that log / reduce
   // junction constants used only when logging or reducing stay in the
   // record (read through L1 when needed), not in registers
   const cmtj_f32_junction_t *Jp = nullptr;
@@ -456,7 +463,7 @@ __global__ void __launch_bounds__(128, (FEAT == CMTJ_FEAT_ALL) ? 1 : CMTJ_BATCH_
             jid = -1;
           } else {
 #pragma unroll
-            for (int l = 0; l < L; ++l) P[l].load(A.Ly[J.layer_offset + l]);
+            for (int l = 0; l < L; ++l) P[l].load(A.Ly[J.layer_offset + l], dtf);
             if (F::waves) {
               nw = J.n_waves < NW ? J.n_waves : NW;
 #pragma unroll
@@ -484,11 +491,12 @@ __global__ void __launch_bounds__(128, (FEAT == CMTJ_FEAT_ALL) ? 1 : CMTJ_BATCH_
             ref0 = A.Ly[J.layer_offset].ref;
             tcount = 0;
             logrow = A.log + (size_t)J.log_offset * 4u;
-            // countdowns to the next sample: log at step % log_every == 0,
-            // reductions at (step - win) % red_every == 0 for step >= win
-            log_cd = p.log_every ? (p.log_every - step % p.log_every) % p.log_every : 0xffffffffu;
-            red_cd = !p.red_every ? 0xffffffffu
-                     : (step >= win ? (p.red_every - (step - win) % p.red_every) % p.red_every : win - step);
+            // next sampling steps: log at step % log_every == 0, reductions
+            // at (step - win) % red_every == 0 for step >= win
+            next_log = (C > 0 && p.log_every) ? step + (p.log_every - step % p.log_every) % p.log_every
+                                              : 0xffffffffu;
+            next_red = !p.red_every ? 0xffffffffu
+                       : (step >= win ? step + (p.red_every - (step - win) % p.red_every) % p.red_every : win);
           }
         }
       }
@@ -497,27 +505,32 @@ __global__ void __launch_bounds__(128, (FEAT == CMTJ_FEAT_ALL) ? 1 : CMTJ_BATCH_
     if (__ballot_sync(0xffffffffu, !retired) == 0) break;
     if (jid < 0) continue;
 
-    // ---- run a burst of steps
+    // ---- run a burst of steps, sampling only at the steps that log or
+    // reduce (the reference logs after stepping at i % writeEvery == 0)
     const uint32_t burst_end = (stop_all - step > 64u) ? step + 64u : stop_all;
-    for (; step < burst_end; ++step) {
+    while (step < burst_end) {
+      const uint32_t next_ev = next_log < next_red ? next_log : next_red;
+      const uint32_t stop = (next_ev < burst_end) ? next_ev + 1 : burst_end;
+      for (; step < stop; ++step) {
       if (SOLVER == CMTJ_RK4) {
         // neighbours frozen at their start-of-step values (junction.hpp:1682-1707)
-        F3 acc[L], kp[L];
+        F3 mnext[L], kp[L];
         Delta<FEAT> d[L];
 #pragma unroll
         for (int st = 0; st < 4; ++st) {
           const int s = st == 0 ? 0 : (st == 3 ? 2 : 1);
-          if (F::waves && st != 2) {
+          if ((F::waves && st != 2) || (!F::waves && st == 0)) {
 #pragma unroll
-            for (int l = 0; l < L; ++l) d[l].clear();
+            for (int l = 0; l < L; ++l) d[l].clear(P[l].h0);
+            if (F::waves) {
 #pragma unroll
-            for (int w = 0; w < NW; ++w)
-              if (w < nw) add_wave<L, FEAT>(W[w], step, s, dtf, d);
-          } else if (!F::waves && st == 0) {
-#pragma unroll
-            for (int l = 0; l < L; ++l) d[l].clear();
+              for (int w = 0; w < NW; ++w)
+                if (w < nw) add_wave<L, FEAT>(W[w], step, s, dtf, d);
+            }
           }
           const float c = st == 0 ? 0.f : (st == 3 ? 1.f : 0.5f);
+          // m + (k1 + 2 k2 + 2 k3 + k4)/6, accumulated as four FMAs
+          const float wgt = (st == 0 || st == 3) ? (1.f / 6.f) : (1.f / 3.f);
 #pragma unroll
           for (int l = 0; l < L; ++l) {
             const F3 ms = st == 0 ? m[l] : fma3(kp[l], c, m[l]);
@@ -528,20 +541,17 @@ __global__ void __launch_bounds__(128, (FEAT == CMTJ_FEAT_ALL) ? 1 : CMTJ_BATCH_
             else if (l == 0) k = rhs<FEAT, false, true>(P[l], ms, mb, mt, d[l]);
             else if (l == L - 1) k = rhs<FEAT, true, false>(P[l], ms, mb, mt, d[l]);
             else k = rhs<FEAT, true, true>(P[l], ms, mb, mt, d[l]);
-            k = k * dtf;
             kp[l] = k;
-            if (st == 0) acc[l] = k;
-            else if (st == 3) acc[l] = acc[l] + k;
-            else acc[l] = fma3(k, 2.f, acc[l]);
+            mnext[l] = fma3(k, wgt, st == 0 ? m[l] : mnext[l]);
           }
         }
 #pragma unroll
-        for (int l = 0; l < L; ++l) m[l] = renorm(fma3(acc[l], 1.f / 6.f, m[l]));
+        for (int l = 0; l < L; ++l) m[l] = renorm(mnext[l]);
       } else {
         // Euler-Heun (1709-1754) and Heun (1756-1815), neighbours un-updated
         Delta<FEAT> d[L];
 #pragma unroll
-        for (int l = 0; l < L; ++l) d[l].clear();
+        for (int l = 0; l < L; ++l) d[l].clear(P[l].h0);
         if (F::waves) {
 #pragma unroll
           for (int w = 0; w < NW; ++w)
@@ -572,16 +582,16 @@ __global__ void __launch_bounds__(128, (FEAT == CMTJ_FEAT_ALL) ? 1 : CMTJ_BATCH_
           for (int l = 0; l < L; ++l) {
             const F3 mN = fma3(g[l], sqdt, m[l]);
             const F3 g2 = stoch<FEAT>(P[l], mN, dW[l]);
-            mn[l] = fma3(g[l] + g2, 0.5f * sqdt, fma3(f[l], dtf, m[l]));
+            mn[l] = fma3(g[l] + g2, 0.5f * sqdt, m[l] + f[l]);
           }
 #pragma unroll
           for (int l = 0; l < L; ++l) m[l] = renorm(mn[l]);
         } else {
 #pragma unroll
-          for (int l = 0; l < L; ++l) mn[l] = fma3(g[l], sqdt, fma3(f[l], dtf, m[l]));
+          for (int l = 0; l < L; ++l) mn[l] = fma3(g[l], sqdt, m[l] + f[l]);
           if (F::waves) {
 #pragma unroll
-            for (int l = 0; l < L; ++l) d[l].clear();
+            for (int l = 0; l < L; ++l) d[l].clear(P[l].h0);
 #pragma unroll
             for (int w = 0; w < NW; ++w)
               if (w < nw) add_wave<L, FEAT>(W[w], step, 2, dtf, d);
@@ -596,29 +606,29 @@ __global__ void __launch_bounds__(128, (FEAT == CMTJ_FEAT_ALL) ? 1 : CMTJ_BATCH_
             else if (l == L - 1) f2 = rhs<FEAT, true, false>(P[l], mn[l], mb, mt, d[l]);
             else f2 = rhs<FEAT, true, true>(P[l], mn[l], mb, mt, d[l]);
             const F3 g2 = stoch<FEAT>(P[l], mn[l], dW[l]);
-            m[l] = renorm(fma3(g[l] + g2, 0.5f * sqdt, fma3(f[l] + f2, 0.5f * dtf, m[l])));
+            m[l] = renorm(fma3(g[l] + g2, 0.5f * sqdt, fma3(f[l] + f2, 0.5f, m[l])));
           }
         }
       }
+      }  // steps up to (and including) the next sampling step
+      const uint32_t last = step - 1;
 
       // ---- reductions: R and I(t) R(t) from win_start on
-      const bool red_now = red_cd == 0;
-      red_cd = red_now ? p.red_every - 1 : red_cd - 1;
-      if (red_now) {
+      if (last == next_red) {
+        next_red = (next_red > 0xffffffffu - p.red_every) ? 0xffffffffu : next_red + p.red_every;
         const float R = resistance<L>(Jp, ref0, m);
         kadd(rs, rc, R);
         const uint64_t vdph = Jp->vsd_dph;
         if (vdph) {
-          const uint64_t ph = Jp->vsd_ph0 + (uint64_t)step * vdph;
+          const uint64_t ph = Jp->vsd_ph0 + (uint64_t)last * vdph;
           const float I = sinpif(2.0f * ((float)(uint32_t)(ph >> 40) * 5.9604644775390625e-08f));
           kadd(vs, vc, I * R);
         }
         ++n_red;
       }
       // ---- log (i % log_every == 0, like logLayerParams at 1978-1980)
-      const bool log_now = log_cd == 0;
-      log_cd = log_now ? p.log_every - 1 : log_cd - 1;
-      if (C > 0 && log_now) {
+      if (last == next_log) {
+        next_log = (next_log > 0xffffffffu - p.log_every) ? 0xffffffffu : next_log + p.log_every;
         if (tcount == 0) bulk_wait_read();
         float *dst = tile + tcount * C;
         if (p.log_mode == CMTJ_LOG_M) {

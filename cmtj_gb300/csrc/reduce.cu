@@ -2,60 +2,140 @@
 //
 // cmtj_spectrum_f32 replaces the per-junction numpy/scipy post-processing of
 // PIMM_procedure (cmtj/utils/procedures.py:28-39, compute_spectrum_strip:
-// |scipy.fft.fft(m)| truncated to a frequency range): one CTA per log row
-// loads the last n_fft samples into shared memory, runs an in-place
-// radix-2 decimation-in-time FFT (bit-reversed load, log2(n_fft) butterfly
-// stages, twiddles from sincospif), and writes |X[k]| for k in [bin_lo,
-// bin_hi).  Work per row is O(n log n) FP32 in shared memory; the kernel is
-// bound by reading the log rows from HBM.
+// |scipy.fft.fft(m)| truncated to a frequency range).  One CTA of n/8
+// threads transforms one log row: a Stockham FFT (self-sorting, no bit
+// reversal) in radix-8 stages with a final radix-4 or radix-2 stage when
+// log2(n) is not a multiple of 3.  Every thread keeps its 8 points in
+// registers through a stage; stages exchange through one shared-memory
+// buffer (n complex floats), so an n = 4096 transform takes 4 stages and 8
+// CTA barriers.  The first stage reads the row straight from HBM
+// (coalesced), the last writes |X[k]| for k in [bin_lo, bin_hi).
 #include "common.cuh"
 
 namespace {
 
 constexpr int kMaxFft = 8192;
-constexpr int kFftThreads = 512;
 
-__global__ void __launch_bounds__(kFftThreads) k_spectrum(const float *__restrict__ series, int64_t row_stride,
-                                                          int32_t series_len, int32_t log2n, int32_t bin_lo,
-                                                          int32_t bin_hi, float *__restrict__ out) {
-  extern __shared__ __align__(16) float sm[];
-  const int n = 1 << log2n;
-  float *re = sm;
-  float *im = sm + n;
-  float *twc = sm + 2 * n;       // cos(2 pi k / n), k < n/2
-  float *tws = twc + n / 2;      // sin(2 pi k / n)
-  const int64_t row = blockIdx.x;
-  const float *src = series + row * row_stride + (series_len - n);
-  for (int k = threadIdx.x; k < n / 2; k += blockDim.x) {
-    float s, c;
-    sincospif(2.0f * (float)k / (float)n, &s, &c);
-    twc[k] = c;
-    tws[k] = s;
+struct C2 {
+  float r, i;
+};
+__device__ __forceinline__ C2 c2(float r, float i) {
+  C2 z;
+  z.r = r;
+  z.i = i;
+  return z;
+}
+__device__ __forceinline__ C2 cadd(C2 a, C2 b) { return c2(a.r + b.r, a.i + b.i); }
+__device__ __forceinline__ C2 csub(C2 a, C2 b) { return c2(a.r - b.r, a.i - b.i); }
+__device__ __forceinline__ C2 cmul(C2 a, C2 b) { return c2(fmaf(a.r, b.r, -a.i * b.i), fmaf(a.r, b.i, a.i * b.r)); }
+// multiplication by -i (forward-transform rotation)
+__device__ __forceinline__ C2 mul_mi(C2 a) { return c2(a.i, -a.r); }
+
+// In-register DFTs of size 2, 4, 8 (forward, e^{-2 pi i jk/R}).
+__device__ __forceinline__ void dft2(C2 &a, C2 &b) {
+  const C2 t = a;
+  a = cadd(t, b);
+  b = csub(t, b);
+}
+__device__ __forceinline__ void dft4(C2 *v) {
+  C2 a0 = v[0], a1 = v[1], a2 = v[2], a3 = v[3];
+  dft2(a0, a2);
+  dft2(a1, a3);
+  a3 = mul_mi(a3);
+  dft2(a0, a1);
+  dft2(a2, a3);
+  v[0] = a0;
+  v[1] = a2;
+  v[2] = a1;
+  v[3] = a3;
+}
+__device__ __forceinline__ void dft8(C2 *v) {
+  const float h = 0.70710678118654752f;
+  C2 e[4] = {v[0], v[2], v[4], v[6]}, o[4] = {v[1], v[3], v[5], v[7]};
+  dft4(e);
+  dft4(o);
+  // o[k] *= e^{-2 pi i k/8}
+  o[1] = c2(h * (o[1].r + o[1].i), h * (o[1].i - o[1].r));
+  o[2] = mul_mi(o[2]);
+  o[3] = c2(h * (o[3].i - o[3].r), -h * (o[3].r + o[3].i));
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    v[k] = cadd(e[k], o[k]);
+    v[k + 4] = csub(e[k], o[k]);
   }
-  for (int t = threadIdx.x; t < n; t += blockDim.x) {
-    const int r = __brev(t) >> (32 - log2n);
-    re[r] = src[t];
-    im[r] = 0.f;
+}
+
+// One Stockham stage of radix R over n points, `groups` R-point groups per
+// thread.  Group g reads x[g + r*n/R], twiddles by w^(r*k) with
+// w = e^{-2 pi i / (Ns R)}, k = g mod Ns, and writes y[(g/Ns) Ns R + k + r Ns].
+template <int R>
+__device__ __forceinline__ void stage(const float *__restrict__ src_re, const float *__restrict__ src_im,
+                                      float *dst_re, float *dst_im, int n, int Ns, bool from_global,
+                                      const float *__restrict__ grow, bool first) {
+  constexpr int G = 8 / R;
+  C2 v[G][R];
+  const int stride = n / R;
+#pragma unroll
+  for (int q = 0; q < G; ++q) {
+    const int g = threadIdx.x * G + q;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const int idx = g + r * stride;
+      v[q][r] = from_global ? c2(grow[idx], 0.f) : c2(src_re[idx], src_im[idx]);
+    }
+    const int k = g % Ns;
+    if (!first && k) {
+      float sn, cs;
+      sincospif(-2.0f * (float)k / (float)(Ns * R), &sn, &cs);
+      const C2 w1 = c2(cs, sn);
+      C2 w = w1;
+#pragma unroll
+      for (int r = 1; r < R; ++r) {
+        v[q][r] = cmul(v[q][r], w);
+        w = cmul(w, w1);
+      }
+    }
+    if (R == 8) dft8(v[q]);
+    else if (R == 4) dft4(v[q]);
+    else dft2(v[q][0], v[q][1]);
+  }
+  __syncthreads();  // everyone has read src before anyone overwrites it
+#pragma unroll
+  for (int q = 0; q < G; ++q) {
+    const int g = threadIdx.x * G + q;
+    const int k = g % Ns;
+    const int base = (g / Ns) * Ns * R + k;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      dst_re[base + r * Ns] = v[q][r].r;
+      dst_im[base + r * Ns] = v[q][r].i;
+    }
   }
   __syncthreads();
-  for (int s = 0; s < log2n; ++s) {
-    const int half = 1 << s;
-    const int tstep = n >> (s + 1);
-    for (int b = threadIdx.x; b < n / 2; b += blockDim.x) {
-      const int pos = b & (half - 1);
-      const int i = ((b >> s) << (s + 1)) + pos;
-      const int j = i + half;
-      const float wr = twc[pos * tstep], wi = -tws[pos * tstep];  // exp(-2 pi i k/n)
-      const float xr = re[j], xi = im[j];
-      const float tr = fmaf(wr, xr, -wi * xi);
-      const float ti = fmaf(wr, xi, wi * xr);
-      const float ar = re[i], ai = im[i];
-      re[i] = ar + tr;
-      im[i] = ai + ti;
-      re[j] = ar - tr;
-      im[j] = ai - ti;
+}
+
+__global__ void k_spectrum(const float *__restrict__ series, int64_t row_stride, int32_t series_len, int32_t n,
+                           int32_t bin_lo, int32_t bin_hi, float *__restrict__ out) {
+  extern __shared__ __align__(16) float sm[];
+  float *re = sm;
+  float *im = sm + n;
+  const int64_t row = blockIdx.x;
+  const float *src = series + row * row_stride + (series_len - n);
+  int Ns = 1;
+  bool first = true;
+  while (Ns < n) {
+    const int left = n / Ns;
+    if (left >= 8) {
+      stage<8>(re, im, re, im, n, Ns, first, src, first);
+      Ns *= 8;
+    } else if (left == 4) {
+      stage<4>(re, im, re, im, n, Ns, first, src, first);
+      Ns *= 4;
+    } else {
+      stage<2>(re, im, re, im, n, Ns, first, src, first);
+      Ns *= 2;
     }
-    __syncthreads();
+    first = false;
   }
   const int nb = bin_hi - bin_lo;
   float *dst = out + row * (int64_t)nb;
@@ -71,8 +151,8 @@ extern "C" int cmtj_spectrum_f32(const float *d_series, int64_t row_stride, int3
                                  int32_t n_fft, int32_t bin_lo, int32_t bin_hi, float *d_out, void *stream) {
   int log2n = 0;
   while ((1 << log2n) < n_fft) ++log2n;
-  if (n_rows < 0 || n_fft < 2 || (1 << log2n) != n_fft || n_fft > kMaxFft) {
-    cmtj_set_error("cmtj_spectrum_f32: n_fft must be a power of two in [2, %d], got %d", kMaxFft, n_fft);
+  if (n_rows < 0 || n_fft < 64 || (1 << log2n) != n_fft || n_fft > kMaxFft) {
+    cmtj_set_error("cmtj_spectrum_f32: n_fft must be a power of two in [64, %d], got %d", kMaxFft, n_fft);
     return CMTJ_ERR_ARG;
   }
   if (series_len < n_fft || row_stride < series_len || bin_lo < 0 || bin_hi > n_fft || bin_lo >= bin_hi) {
@@ -85,12 +165,12 @@ extern "C" int cmtj_spectrum_f32(const float *d_series, int64_t row_stride, int3
     cmtj_set_error("cmtj_spectrum_f32: null buffer");
     return CMTJ_ERR_ARG;
   }
-  const size_t smem = (size_t)(3 * n_fft) * sizeof(float);
+  const size_t smem = (size_t)(2 * n_fft) * sizeof(float);
   if (smem > 48 * 1024) {
     CMTJ_CUDA_TRY(cudaFuncSetAttribute(k_spectrum, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   }
-  k_spectrum<<<n_rows, kFftThreads, smem, cmtj_stream(stream)>>>(d_series, row_stride, series_len, log2n, bin_lo,
-                                                                  bin_hi, d_out);
+  k_spectrum<<<n_rows, n_fft / 8, smem, cmtj_stream(stream)>>>(d_series, row_stride, series_len, n_fft, bin_lo,
+                                                               bin_hi, d_out);
   CMTJ_LAUNCH_CHECK("k_spectrum");
   return CMTJ_OK;
 }

@@ -380,7 +380,8 @@ typedef struct cmtj_f32_params {
 #define CMTJ_FEAT_WAVES 64         /* waves on the field (HX, HY, HZ) and, with
                                       STT or SOT, on I / FL / DL / FL2 / DL2      */
 #define CMTJ_FEAT_SCALAR_WAVES 128 /* waves on K, K2, J*, T                      */
-#define CMTJ_FEAT_ALL 255
+#define CMTJ_FEAT_IEC2 256         /* quadratic (biquadratic) IEC, J2 != 0        */
+#define CMTJ_FEAT_ALL 511
 
 /* Runs every junction of one partition (all with n_layers layers and the
  * same solver) for up to p->chunk_steps iterations, resuming from d_state

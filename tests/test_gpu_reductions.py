@@ -115,3 +115,25 @@ def test_pimm_spectrum_matches_numpy_and_fp64(gpu_lib):
         # trajectory error (max|dm| <= 1e-4 per sample) plus FFT rounding
         traj_tol = 1e-4 * nfft
         assert np.max(np.abs(gpu[k] - fft64)) <= traj_tol + fft_tol, k
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("nfft", [64, 128, 256, 512, 4096, 8192])
+def test_spectrum_kernel_matches_numpy(gpu_lib, nfft):
+    """Radix-8 Stockham stages with a radix-4 or radix-2 tail: |FFT| of
+    random rows (taken from the end of longer rows) against numpy."""
+    t = engine.torch()
+    lib = _abi.load()
+    rng = np.random.default_rng(nfft)
+    rows, length, stride = 37, nfft + 13, nfft + 20
+    x = rng.standard_normal((rows, stride)).astype(np.float32) + 0.5
+    d_x = t.from_numpy(x.ravel().copy()).cuda()
+    lo, hi = 0, nfft // 2 + 1
+    out = t.empty((rows, hi - lo), dtype=t.float32, device="cuda")
+    rc = lib.cmtj_spectrum_f32(engine.ptr(d_x), stride, rows, length, nfft, lo, hi, engine.ptr(out),
+                               engine.stream_ptr())
+    _abi.check(rc, lib)
+    got = out.cpu().numpy()
+    ref = np.abs(np.fft.fft(x[:, length - nfft:length].astype(np.float64), axis=1))[:, lo:hi]
+    tol = 4 * np.finfo(np.float32).eps * np.log2(nfft) * np.linalg.norm(x[:, length - nfft:length], axis=1)
+    assert np.all(np.max(np.abs(got - ref), axis=1) <= tol)
