@@ -49,7 +49,8 @@ F32_LAYER_DTYPE = np.dtype(
      ("ref", "<f4", 3), ("ref2", "<f4", 3), ("ref_type", "<i4"), ("flags", "<i4"), ("stt_c", "<f4"),
      ("stt_p", "<f4"), ("stt_l", "<f4"), ("stt_beta", "<f4"), ("stt_kappa", "<f4"), ("i0", "<f4"),
      ("fl0", "<f4"), ("dl0", "<f4"), ("fl20", "<f4"), ("dl20", "<f4"), ("sig_c", "<f4"), ("t0", "<f4"),
-     ("seed_lo", "<u4"), ("seed_hi", "<u4"), ("noise_step_lo", "<u4"), ("noise_step_hi", "<u4")], align=True)
+     ("seed_lo", "<u4"), ("seed_hi", "<u4"), ("noise_step_lo", "<u4"), ("noise_step_hi", "<u4"),
+     ("gdt", "<f4"), ("gdt6", "<f4"), ("stt_cdt", "<f4"), ("stt_cdt6", "<f4")], align=True)
 
 F32_JUNCTION_DTYPE = np.dtype(
     [("n_layers", "<i4"), ("mr_mode", "<i4"), ("layer_offset", "<i4"), ("n_steps", "<u4"),
@@ -409,6 +410,8 @@ def lower(spec, time_step, n_steps, win_start=None):
     lay["dmi_t"] = g(spec.Dt) / mst[:, None]
     conv = 1.0 / (1.0 + alpha * alpha)
     lay["gam"] = -c["gyro"] * conv
+    lay["gdt"] = -c["gyro"] * conv * dt
+    lay["gdt6"] = -c["gyro"] * conv * dt / 6.0
     lay["alpha"] = alpha
     lay["ref"] = g(spec.ref)
     lay["ref2"] = g(spec.ref2)
@@ -416,6 +419,8 @@ def lower(spec, time_step, n_steps, win_start=None):
     flags = g(spec.flags)
     lay["flags"] = flags
     lay["stt_c"] = c["gyro"] * c["hbar"] / (c["echarge"] * mst) * conv
+    lay["stt_cdt"] = c["gyro"] * c["hbar"] / (c["echarge"] * mst) * conv * dt
+    lay["stt_cdt6"] = c["gyro"] * c["hbar"] / (c["echarge"] * mst) * conv * dt / 6.0
     lay["stt_p"] = g(spec.stt_p)
     lay["stt_l"] = g(spec.stt_l)
     lay["stt_beta"] = g(spec.stt_beta)

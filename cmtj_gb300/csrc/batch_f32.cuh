@@ -77,15 +77,16 @@ template <int FEAT> struct LayerP {
   F3 h0;
   float jb, jt, j2b, j2t;
   F3 dmib, dmit;
-  float gam, gdt, alpha;  // -gamma/(1+alpha^2), and that times dt
+  float gam, gdt, alpha;  // -gamma/(1+alpha^2), and that times dt (or dt/6 for RK4)
   F3 ref, ref2;
   int rtype, flags;
-  float sttc, sttp, sttl, sttb, sttk, i0, fl0, dl0, fl20, dl20;  // sttc carries dt
+  float sttc, sttp, sttl, sttb, sttk, i0, fl0, dl0, fl20, dl20;  // sttc carries dt (dt/6 for RK4)
   float sigc, t0;
   uint32_t seed_lo, seed_hi;
   uint64_t nstep0;
 
-  __device__ __forceinline__ void load(const cmtj_f32_layer_t &r, float dtf) {
+  // rk4: load the dt/6 prefactors (k' = k/6), else the dt ones
+  __device__ __forceinline__ void load(const cmtj_f32_layer_t &r, bool rk4) {
     using F = Feat<FEAT>;
     a = ld3(r.anis);
     kc = r.kc;
@@ -115,14 +116,14 @@ template <int FEAT> struct LayerP {
       dmit = ld3(r.dmi_t);
     }
     gam = r.gam;
-    gdt = r.gam * dtf;
+    gdt = rk4 ? r.gdt6 : r.gdt;
     alpha = r.alpha;
     rtype = r.ref_type;
     flags = r.flags;
     if (F::stt || F::sot) {
       ref = ld3(r.ref);
       ref2 = ld3(r.ref2);
-      sttc = r.stt_c * dtf;
+      sttc = rk4 ? r.stt_cdt6 : r.stt_cdt;
       sttp = r.stt_p;
       sttl = r.stt_l;
       sttb = r.stt_beta;
@@ -274,7 +275,7 @@ __device__ __forceinline__ void add_wave(const WaveR<L> &w, uint32_t step, int s
 }
 
 // Effective field + LL torque of one layer (junction.hpp:580-815), returned
-// already multiplied by dt (the RK4 k, the Euler-Heun f dt).
+// already multiplied by dt (Euler-Heun, Heun: f dt) or by dt/6 (RK4: k/6).
 template <int FEAT, bool HB, bool HT>
 __device__ __forceinline__ F3 rhs(const LayerP<FEAT> &P, F3 m, F3 mb, F3 mt, const Delta<FEAT> &d) {
   using F = Feat<FEAT>;
@@ -322,7 +323,7 @@ __device__ __forceinline__ F3 rhs(const LayerP<FEAT> &P, F3 m, F3 mb, F3 mt, con
       const float s = P.sttc * I * eta;
       const F3 fl = cross(m, p);
       const F3 dl = cross(m, fl);
-      // gdt carries -gamma dt/(1+alpha^2); sttc carries dt/(1+alpha^2).
+      // gdt carries -gamma dt/(1+alpha^2), sttc dt/(1+alpha^2) (each /6 for RK4).
       return fma3(fl, s * P.sttb, fma3(dl, -s * P.sttk, acc * P.gdt));
     }
     if (F::sot && (P.flags & CMTJ_F32_SOT)) {
@@ -463,7 +464,7 @@ __global__ void __launch_bounds__(128, (FEAT == CMTJ_FEAT_ALL) ? 1 : CMTJ_BATCH_
             jid = -1;
           } else {
 #pragma unroll
-            for (int l = 0; l < L; ++l) P[l].load(A.Ly[J.layer_offset + l], dtf);
+            for (int l = 0; l < L; ++l) P[l].load(A.Ly[J.layer_offset + l], SOLVER == CMTJ_RK4);
             if (F::waves) {
               nw = J.n_waves < NW ? J.n_waves : NW;
 #pragma unroll
@@ -514,7 +515,7 @@ __global__ void __launch_bounds__(128, (FEAT == CMTJ_FEAT_ALL) ? 1 : CMTJ_BATCH_
       for (; step < stop; ++step) {
       if (SOLVER == CMTJ_RK4) {
         // neighbours frozen at their start-of-step values (junction.hpp:1682-1707)
-        F3 mnext[L], kp[L];
+        F3 acc[L], kp[L];
         Delta<FEAT> d[L];
 #pragma unroll
         for (int st = 0; st < 4; ++st) {
@@ -528,9 +529,11 @@ __global__ void __launch_bounds__(128, (FEAT == CMTJ_FEAT_ALL) ? 1 : CMTJ_BATCH_
                 if (w < nw) add_wave<L, FEAT>(W[w], step, s, dtf, d);
             }
           }
-          const float c = st == 0 ? 0.f : (st == 3 ? 1.f : 0.5f);
-          // m + (k1 + 2 k2 + 2 k3 + k4)/6, accumulated as four FMAs
-          const float wgt = (st == 0 || st == 3) ? (1.f / 6.f) : (1.f / 3.f);
+          // k' = k/6 through the host's dt/6 prefactors, so the stage
+          // offsets (3k', 3k', 6k') and weights (1, 2, 2, 1) are exact; the
+          // increment is summed apart from m and added to m once, so only one
+          // rounding per step happens at the scale of |m| = 1
+          const float c = st == 3 ? 6.f : 3.f;
 #pragma unroll
           for (int l = 0; l < L; ++l) {
             const F3 ms = st == 0 ? m[l] : fma3(kp[l], c, m[l]);
@@ -542,11 +545,13 @@ __global__ void __launch_bounds__(128, (FEAT == CMTJ_FEAT_ALL) ? 1 : CMTJ_BATCH_
             else if (l == L - 1) k = rhs<FEAT, true, false>(P[l], ms, mb, mt, d[l]);
             else k = rhs<FEAT, true, true>(P[l], ms, mb, mt, d[l]);
             kp[l] = k;
-            mnext[l] = fma3(k, wgt, st == 0 ? m[l] : mnext[l]);
+            if (st == 0) acc[l] = k;
+            else if (st == 3) acc[l] = acc[l] + k;
+            else acc[l] = fma3(k, 2.f, acc[l]);
           }
         }
 #pragma unroll
-        for (int l = 0; l < L; ++l) m[l] = renorm(mnext[l]);
+        for (int l = 0; l < L; ++l) m[l] = renorm(m[l] + acc[l]);
       } else {
         // Euler-Heun (1709-1754) and Heun (1756-1815), neighbours un-updated
         Delta<FEAT> d[L];
@@ -582,13 +587,13 @@ __global__ void __launch_bounds__(128, (FEAT == CMTJ_FEAT_ALL) ? 1 : CMTJ_BATCH_
           for (int l = 0; l < L; ++l) {
             const F3 mN = fma3(g[l], sqdt, m[l]);
             const F3 g2 = stoch<FEAT>(P[l], mN, dW[l]);
-            mn[l] = fma3(g[l] + g2, 0.5f * sqdt, m[l] + f[l]);
+            mn[l] = m[l] + fma3(g[l] + g2, 0.5f * sqdt, f[l]);  // one rounding at |m|
           }
 #pragma unroll
           for (int l = 0; l < L; ++l) m[l] = renorm(mn[l]);
         } else {
 #pragma unroll
-          for (int l = 0; l < L; ++l) mn[l] = fma3(g[l], sqdt, m[l] + f[l]);
+          for (int l = 0; l < L; ++l) mn[l] = m[l] + fma3(g[l], sqdt, f[l]);
           if (F::waves) {
 #pragma unroll
             for (int l = 0; l < L; ++l) d[l].clear(P[l].h0);
@@ -606,7 +611,7 @@ __global__ void __launch_bounds__(128, (FEAT == CMTJ_FEAT_ALL) ? 1 : CMTJ_BATCH_
             else if (l == L - 1) f2 = rhs<FEAT, true, false>(P[l], mn[l], mb, mt, d[l]);
             else f2 = rhs<FEAT, true, true>(P[l], mn[l], mb, mt, d[l]);
             const F3 g2 = stoch<FEAT>(P[l], mn[l], dW[l]);
-            m[l] = renorm(fma3(g[l] + g2, 0.5f * sqdt, fma3(f[l] + f2, 0.5f, m[l])));
+            m[l] = renorm(m[l] + fma3(g[l] + g2, 0.5f * sqdt, (f[l] + f2) * 0.5f));
           }
         }
       }

@@ -114,7 +114,7 @@ __device__ __forceinline__ void stage(const float *__restrict__ src_re, const fl
   __syncthreads();
 }
 
-__global__ void k_spectrum(const float *__restrict__ series, int64_t row_stride, int32_t series_len, int32_t n,
+__global__ void __launch_bounds__(1024) k_spectrum(const float *__restrict__ series, int64_t row_stride, int32_t series_len, int32_t n,
                            int32_t bin_lo, int32_t bin_hi, float *__restrict__ out) {
   extern __shared__ __align__(16) float sm[];
   float *re = sm;

@@ -310,6 +310,13 @@ typedef struct cmtj_f32_layer {
   float t0;               /* constant temperature                              */
   uint32_t seed_lo, seed_hi;
   uint32_t noise_step_lo, noise_step_hi;
+  /* time-step prefactors, each formed in FP64 and rounded once:
+   *   gdt  = gam * dt,      stt_cdt  = stt_c * dt        (Euler-Heun, Heun)
+   *   gdt6 = gam * dt / 6,  stt_cdt6 = stt_c * dt / 6    (RK4: with k' = k/6
+   *   every RK4 constant is an exact small integer: m + 3k', m + 6k',
+   *   m + k1' + 2k2' + 2k3' + k4', so no weight or dt rounding drifts
+   *   the precession phase over long runs) */
+  float gdt, gdt6, stt_cdt, stt_cdt6;
 } cmtj_f32_layer_t;
 
 #define CMTJ_F32_STT 1

@@ -11,10 +11,31 @@ from test_oracle_pin import load_golden
 
 TOL_M_F32 = 1e-4
 
-# cases the FP32 form accepts (drivers_zoo has 7 distinct time-dependent
-# drivers, custom_driver uses Python callbacks: FP64 plain form only)
+# Cases the FP32 form accepts (drivers_zoo has 7 distinct time-dependent
+# drivers and custom_driver uses Python callbacks: FP64 plain form only).
+# euler_heun_det is left out: it is deterministic forward Euler on the
+# strongly coupled tri-layer, and it is ill-conditioned: a 1e-7 nudge of m0
+# moves it by 2.9e-4 (the other cases: at most 1.5e-5). Reordering its FP64
+# arithmetic moves it by 5e-6, and FP32 (in any formulation) by 5e-4, so no
+# 1e-4 comparison is meaningful for it.
 F32_CASES = ["config0_point", "sto", "sot_strip", "tri_layer", "vsd_sine", "energies_k2", "alt_stt_bottom",
-             "heun_det", "euler_heun_det"]
+             "heun_det"]
+
+
+def conditioning(name):
+    """max|dm| of the FP64 oracle when every initial m is nudged by 1e-7:
+    how far rounding at FP32 level can move the trajectory at all."""
+    import oracle_harness
+    om = oracle_harness.oracle_module()
+    base, runs = cases.DETERMINISTIC[name](om)
+    pert, _ = cases.DETERMINISTIC[name](om)
+    for l in pert.layers:
+        l.mag.x += 1e-7
+    r = dict(runs[0])
+    for j in (base, pert):
+        j.runSimulation(**r)
+    a, b = base.getLogArrays(), pert.getLogArrays()
+    return max(float(np.max(np.abs(a[k] - b[k]))) for k in a if k.endswith(("_mx", "_my", "_mz")))
 
 
 def _golden_m(name, j):
@@ -25,6 +46,7 @@ def _golden_m(name, j):
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", F32_CASES)
 def test_fp32_batch_matches_reference(gpu_lib, name):
+    assert conditioning(name) <= 3e-5, "ill-conditioned case: FP32 accuracy not testable"
     j, runs = cases.DETERMINISTIC[name](cmtj_gb300)
     assert len(runs) == 1
     r = dict(runs[0])
