@@ -47,17 +47,19 @@ WORKLOAD = ("batched FP32 PIMM: 262144 2-layer MTJs (512 H x 512 seeded Ku/J dra
 
 def fp32_flops_per_layer_step(n_layers=2, waves_per_junction=1):
     """FP32 operations per layer-step of the batched RK4 integrator for the
-    PIMM junction (FMA = 2, rsqrt = 1), counted from its formulation:
-    per right-hand side and layer: field sum h0 + wave 3, anisotropy
-    a*(kc*(a.m)) 12, diagonal demag 6, LL torque gam*(mxH + alpha mx(mxH)) 27,
-    IEC per neighbour m_n*(j + j2 (m_n.m)) 13; per layer-step: 4 RHS, stage
-    states 18, k*dt 12, RK4 accumulation 15, update 6, renormalisation 9;
-    per step: each wave adds amp*u to every layer at 3 stage times (2 each)."""
+    PIMM junction (FMA = 2, rsqrt = 1), counted from its formulation.  The
+    field terms are stored pre-multiplied by gamma dt/6, and the anisotropy
+    (axis along z) and the diagonal demag fold into one diagonal tensor M.
+    Per stage time (3 per step: t, t + dt/2, t + dt) and layer: base field
+    h0 + wave 6 per wave, + IEC neighbour 6 per neighbour.  Per RHS (4 per
+    step) and layer: M m 6, m x H 9, m x (m x H) 9, alpha FMA 6.  Per
+    layer-step: stage states 18, RK4 accumulation 15, m + increment 3,
+    renormalisation 9."""
     nb = 2.0 * (n_layers - 1) / n_layers
-    rhs = 3 + 12 + 6 + 27 + 13 * nb
-    rk4 = 4 * rhs + 18 + 12 + 15 + 6 + 9
-    waves = 3 * waves_per_junction * n_layers * 2 / n_layers
-    return rk4 + waves
+    waves_per_layer = float(waves_per_junction)
+    stage_fields = 3 * (6 * waves_per_layer + 6 * nb)
+    rhs = 6 + 9 + 9 + 6
+    return stage_fields + 4 * rhs + 18 + 15 + 3 + 9
 
 
 def dist_info():
@@ -114,12 +116,12 @@ class ClockSampler:
 
 
 def flops_per_layer_step():
-    """FLOPs of one layer-step of the config-1 junction, counted by running
+    """FLOPs of one layer-step of the 2-layer PIMM junction, counted by running
     the oracle (the reference's arithmetic) on a counting scalar type."""
     import cases  # noqa: F401
     import oracle_harness
     import cmtj_gb300 as cm
-    j, _ = __import__("cases").config0_point(cm, hx=-3e5, total=1e-11)
+    j, _ = __import__("cases").mtj_rh_point(cm, hx=-3e5, total=1e-11)
     j.setLayerOerstedFieldDriver("all", cm.AxialDriver(cm.stepDriver(0, 1e3, 0, 1e-12), cm.NullDriver(),
                                                         cm.NullDriver()))
     steps = 200
@@ -127,9 +129,12 @@ def flops_per_layer_step():
     return float(c.sum()) / (steps * 2), [int(x) for x in c]
 
 
-def build_workload(n_h=N_H, n_draw=N_DRAW, total=TOTAL, relax=True):
+def build_workload(n_h=N_H, n_draw=N_DRAW, total=TOTAL, relax=True, seed=1):
+    """The PIMM batch of one rank.  Under N ranks the job is N x 262,144
+    junctions: rank r draws its Ku/J with seed 1 + r, so ranks hold disjoint
+    shards and never exchange data."""
     from cmtj_gb300 import batch, sweeps
-    spec, n_steps = sweeps.pimm_config(n_h=n_h, n_draw=n_draw, dt=DT, total=total)
+    spec, n_steps = sweeps.pimm_config(n_h=n_h, n_draw=n_draw, seed=seed, dt=DT, total=total)
     if relax:
         batch.relax(spec, DT, RELAX_STEPS, alpha=1.0)
     low = batch.lower(spec, DT, n_steps)
@@ -152,13 +157,14 @@ def run_reference_arm(args):
     if rank != 0:
         return
     cores = os.cpu_count() or 1
-    n = cores * 2
-    steps = 2000
-    spec, _ = sweeps.pimm_config(n_h=n, n_draw=1, dt=DT, total=TOTAL)
+    n = cores * 8
+    spec, steps = sweeps.pimm_config(n_h=n, n_draw=1, dt=DT, total=TOTAL)
     js = spec_to_junctions(spec)
     vals = []
     for it in range(args.warmup + args.steps):
         t0 = time.perf_counter()
+        for j in js:
+            j.clearLog()
         oracle_harness.run_oracle(js, steps * DT, DT, DT * LOG_EVERY, threads=cores)
         el = time.perf_counter() - t0
         if it >= args.warmup:
@@ -170,7 +176,8 @@ def run_reference_arm(args):
             "impl": "reference",
             "config": {"workload": WORKLOAD, "sample": "%d junctions x %d steps per step" % (n, steps)},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": "%d config-1 junctions x %d RK4 steps, one oracle pass per step" % (n, steps)},
+                             "sample": "%d PIMM junctions x %d RK4 steps (whole 5 ns solves), one oracle pass per step"
+                                       % (n, steps)},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -181,7 +188,7 @@ def spec_to_junctions(spec):
     import cases
     out = []
     for k in range(spec.n):
-        j, _ = cases.config0_point(cm, hx=float(spec.Hc[k, 0, 0]), total=1e-9)
+        j, _ = cases.mtj_rh_point(cm, hx=float(spec.Hc[k, 0, 0]), total=1e-9)
         j.setLayerAnisotropyDriver("free", cm.constantDriver(float(spec.K[k, 0])))
         j.setIECDriver("free", "ref", cm.constantDriver(float(spec.Jt[k, 0])))
         j.setLayerOerstedFieldDriver("all", cm.AxialDriver(cm.stepDriver(0, 1e3, 0, 1e-12), cm.NullDriver(),
@@ -191,26 +198,29 @@ def spec_to_junctions(spec):
 
 
 def cpu_baseline(budget_s=12.0):
+    """The oracle (the reference's arithmetic, bit-identical on the pinned
+    cases) on all host cores: a pilot of whole 5 ns PIMM solves on 2
+    junctions per core, then as many junctions as fill about budget_s."""
     import oracle_harness
     from cmtj_gb300 import sweeps
     cores = os.cpu_count() or 1
-    n = cores * 4
-    steps = 1000
-    spec, _ = sweeps.pimm_config(n_h=n, n_draw=1, dt=DT, total=TOTAL)
+    n = cores * 2
+    spec, n_steps = sweeps.pimm_config(n_h=n, n_draw=1, dt=DT, total=TOTAL)
     js = spec_to_junctions(spec)
     t0 = time.perf_counter()
-    oracle_harness.run_oracle(js, steps * DT, DT, DT * LOG_EVERY, threads=cores)
+    oracle_harness.run_oracle(js, n_steps * DT, DT, DT * LOG_EVERY, threads=cores)
     el = time.perf_counter() - t0
-    rate = n * steps * 2 / el
-    # scale the sample up to about budget_s of CPU work
-    steps2 = int(min(50000, max(steps, steps * budget_s / max(el, 1e-3))))
+    per_junction_s = el / n
+    n2 = max(cores, int(budget_s / per_junction_s) // cores * cores)
+    spec, _ = sweeps.pimm_config(n_h=n2, n_draw=1, dt=DT, total=TOTAL)
     js = spec_to_junctions(spec)
     t0 = time.perf_counter()
-    oracle_harness.run_oracle(js, steps2 * DT, DT, DT * LOG_EVERY, threads=cores)
+    oracle_harness.run_oracle(js, n_steps * DT, DT, DT * LOG_EVERY, threads=cores)
     el = time.perf_counter() - t0
-    rate = n * steps2 * 2 / el
+    rate = n2 * n_steps * 2 / el
     return {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": "%d config-1 junctions x %d RK4 steps on %d threads (%.1f s)" % (n, steps2, cores, el)}
+            "sample": "%d PIMM junctions x %d RK4 steps (full 5 ns solves) on %d threads (%.1f s)"
+                      % (n2, n_steps, cores, el)}
 
 
 def main():
@@ -237,9 +247,9 @@ def main():
     stream = torch.cuda.current_stream()
 
     if args.profile:
-        spec, low, n_steps = build_workload(N_H, N_DRAW, total=2000 * DT, relax=False)
+        spec, low, n_steps = build_workload(N_H, N_DRAW, total=2000 * DT, relax=False, seed=1 + rank)
     else:
-        spec, low, n_steps = build_workload(N_H, N_DRAW)
+        spec, low, n_steps = build_workload(N_H, N_DRAW, seed=1 + rank)
     n = spec.n
     layer_steps = float(n) * n_steps * 2
     run = batch.BatchRun(low, DT, batch.SolverMode.RK4, batch.LOG_MIX, LOG_EVERY, log_axis=0)
@@ -341,7 +351,8 @@ def main():
             "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": WORKLOAD, "junctions_per_gpu": n, "layers": 2, "steps_per_junction": n_steps,
-                       "parallelism": "replicas" if world > 1 else "single",
+                       "parallelism": ("%d disjoint shards (rank r: draws seeded 1 + r), no data-path collective"
+                                       % world) if world > 1 else "single",
                        "l2": "inputs and logs (5.2 GB) larger than L2", "all_ok": ok},
             "e2e": e2e, "clocks": clocks,
             "gpu_launches": args.steps * 2}
@@ -372,15 +383,23 @@ def measure_rest(run, low, spec, n_steps, kern_ms, fft_ms, lib):
     from cmtj_gb300 import build as cbuild
     import ctypes
     probe = ctypes.CDLL(cbuild.build_probe())
-    probe.cmtj_probe_fp32_peak.restype = ctypes.c_double
-    probe.cmtj_probe_fp32_peak.argtypes = [ctypes.c_int]
-    peak = probe.cmtj_probe_fp32_peak(5) / 1e12
+    peaks = {}
+    for name in ("cmtj_probe_fp32_peak", "cmtj_probe_fp32x2_peak"):
+        fn = getattr(probe, name)
+        fn.restype = ctypes.c_double
+        fn.argtypes = [ctypes.c_int]
+        peaks[name] = fn(5) / 1e12
+    # the FP32 ceiling is the larger of scalar FFMA and packed FFMA2 issue
+    peak = max(peaks.values())
     out["roofline"] = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                        "frac": achieved / peak, "traffic": None,
                        "flop_per_layer_step": fpls,
                        "reference_flop_per_layer_step": ref_fpls,
                        "reference_flop_breakdown_add_mul_div_sqrt_trans": fcount,
-                       "peak_source": "measured FP32 FMA probe on this GPU (MEASURED_PEAKS.json has no FP32 figure)",
+                       "peak_source": "measured FP32 FMA probe on this GPU, best of scalar FFMA and packed FFMA2 "
+                                      "(MEASURED_PEAKS.json has no FP32 figure)",
+                       "peak_scalar_ffma": peaks["cmtj_probe_fp32_peak"],
+                       "peak_packed_ffma2": peaks["cmtj_probe_fp32x2_peak"],
                        "kernel_ms_avg": kavg * 1e3, "fft_ms_avg": float(np.mean(fft_ms))}
 
     # FP64 plain form and accuracy on a sample of the same junctions
@@ -432,7 +451,7 @@ def measure_rest(run, low, spec, n_steps, kern_ms, fft_ms, lib):
 
 
 def serving_leg(fp64_rate, n_requests=200, rate_hz=200.0):
-    """Config-4 trace: Poisson arrivals at 200 req/s of requests holding
+    """Serving trace: Poisson arrivals at 200 req/s of requests holding
     64-16,384 solves (log-uniform) of three kinds -- PIMM-style 2-layer RK4,
     thermal 1-layer p-bit Euler-Heun at 300 K, uneven 1-4-layer spin-diode
     RK4 with on-device <I R> -- each solve 2-40 ns at dt = 1e-13, served by
@@ -463,7 +482,7 @@ def spec_to_junctions_rows(spec, rows):
     import cases
     out = []
     for k in rows:
-        j, _ = cases.config0_point(cm, hx=float(spec.Hc[k, 0, 0]), total=1e-9)
+        j, _ = cases.mtj_rh_point(cm, hx=float(spec.Hc[k, 0, 0]), total=1e-9)
         for l in range(2):
             j.layers[l].mag = cm.CVector(*spec.m0[k, l])
         j.setLayerAnisotropyDriver("free", cm.constantDriver(float(spec.K[k, 0])))

@@ -32,13 +32,18 @@ EULER_HEUN, RK4, DORMAND_PRINCE, HEUN = 0, 1, 2, 3
 MR_NONE, MR_CLASSIC, MR_STRIP = 0, 1, 2
 
 CMTJ_OK, CMTJ_ERR_ARG, CMTJ_ERR_CUDA, CMTJ_ERR_RUNTIME, CMTJ_ERR_LIMIT = 0, -1, -2, -3, -4
-STATUS_OK, STATUS_NAN, STATUS_NOT_RUN = 0, 1, 2
+STATUS_OK, STATUS_NAN, STATUS_NOT_RUN, STATUS_BAD_INPUT, STATUS_DP_STALL, STATUS_LIMIT = 0, 1, 2, 3, 4, 5
 
 DRIVER_DTYPE = np.dtype(
     [("update", "<i4"), ("reserved", "<i4"), ("table_offset", "<i8"),
      ("constantValue", "<f8"), ("amplitude", "<f8"), ("frequency", "<f8"), ("phase", "<f8"),
      ("period", "<f8"), ("cycle", "<f8"), ("timeStart", "<f8"), ("timeStop", "<f8"),
      ("edgeTime", "<f8"), ("steadyTime", "<f8")], align=True)
+
+ADAPTIVE_DTYPE = np.dtype(
+    [("abs_tol", "<f8"), ("rel_tol", "<f8"), ("max_factor", "<f8"), ("min_factor", "<f8"),
+     ("safety_factor", "<f8"), ("ki", "<f8"), ("kp", "<f8"), ("kd", "<f8"), ("prev_error_ratio", "<f8"),
+     ("integral_error", "<f8"), ("use_pid_control", "<i4"), ("reserved", "<i4")], align=True)
 
 LAYER_DTYPE = np.dtype(
     [("mag", "<f8", 3), ("anis", "<f8", 3), ("ref", "<f8", 3), ("ref2", "<f8", 3),
@@ -49,7 +54,7 @@ LAYER_DTYPE = np.dtype(
      ("referenceType", "<i4"), ("includeSTT", "<i4"), ("includeSOT", "<i4"), ("dynamicSOT", "<i4"),
      ("alternativeSTT", "<i4"), ("temperatureSet", "<i4"),
      ("seed_lo", "<u4"), ("seed_hi", "<u4"), ("noise_step", "<u8"),
-     ("drv", DRIVER_DTYPE, NUM_SLOTS)], align=True)
+     ("drv", DRIVER_DTYPE, NUM_SLOTS), ("adaptive", ADAPTIVE_DTYPE)], align=True)
 
 JUNCTION_DTYPE = np.dtype(
     [("n_layers", "<i4"), ("mr_mode", "<i4"), ("layer_offset", "<i4"), ("reserved", "<i4"),
@@ -65,7 +70,8 @@ CONSTANTS_DTYPE = np.dtype(
 SIM_PARAMS_DTYPE = np.dtype(
     [("time_step", "<f8"), ("total_iterations", "<u4"), ("write_every", "<u4"), ("n_log", "<u4"),
      ("solver", "<i4"), ("calculate_energies", "<i4"), ("log_width", "<i4"),
-     ("c", CONSTANTS_DTYPE)], align=True)
+     ("c", CONSTANTS_DTYPE), ("total_time", "<f8"), ("write_frequency", "<f8"), ("max_attempts", "<u8")],
+    align=True)
 
 # Order of cmtj_struct_sizes() output.
 STRUCT_SIZES = {

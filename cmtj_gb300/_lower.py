@@ -23,19 +23,37 @@ _SOLVER_STAGES = {
 class RunPlan:
     """Junction::runSimulation arguments resolved as the reference does
     (junction.hpp:1952-1959): truncating casts of totalTime/timeStep and
-    writeFrequency/timeStep."""
+    writeFrequency/timeStep.  `adaptive` marks a Dormand-Prince run
+    (junction.hpp:1982-2045), whose log length depends on the step sizes
+    it picks: at most floor(totalTime / writeFrequency) + 2 rows."""
     time_step: float
     total_iterations: int
     write_every: int
+    total_time: float = 0.0
+    write_frequency: float = 0.0
+    adaptive: bool = False
 
     @property
     def n_log(self):
+        if self.adaptive:
+            return int(self.total_time / self.write_frequency) + 2
         if self.total_iterations == 0:
             return 0
         return (self.total_iterations + self.write_every - 1) // self.write_every
 
+    def for_solver(self, solver):
+        """This plan for `solver` (Dormand-Prince plans are adaptive)."""
+        import dataclasses
+        return dataclasses.replace(self, adaptive=SolverMode(int(solver)) == SolverMode.DormandPrince)
 
-def plan_run(totalTime, timeStep=1e-13, writeFrequency=1e-11):
+    @property
+    def max_attempts(self):
+        """Dormand-Prince step attempts before the run stops with an error:
+        100 attempts per initial step of the horizon, at least 10^6."""
+        return int(max(1e6, 100.0 * self.total_time / self.time_step))
+
+
+def plan_run(totalTime, timeStep=1e-13, writeFrequency=1e-11, solver=None):
     totalTime, timeStep, writeFrequency = float(totalTime), float(timeStep), float(writeFrequency)
     if timeStep > writeFrequency:
         raise RuntimeError("The time step cannot be larger than write frequency!")
@@ -43,7 +61,8 @@ def plan_run(totalTime, timeStep=1e-13, writeFrequency=1e-11):
     we = writeFrequency / timeStep
     if not (0 <= total < 2 ** 32) or not (1 <= we < 2 ** 32):
         raise ValueError("totalTime/timeStep and writeFrequency/timeStep must fit an unsigned 32-bit count")
-    return RunPlan(timeStep, int(total), int(we))
+    plan = RunPlan(timeStep, int(total), int(we), totalTime, writeFrequency)
+    return plan.for_solver(solver) if solver is not None else plan
 
 
 class TableBuilder:
@@ -53,12 +72,15 @@ class TableBuilder:
 
     def __init__(self, plan, solver):
         self.plan = plan
-        self.stages = _SOLVER_STAGES[SolverMode(int(solver))]
+        self.stages = _SOLVER_STAGES.get(SolverMode(int(solver)))
         self.chunks = []
         self.size = 0
         self._cache = {}
 
     def add(self, driver):
+        if self.stages is None:
+            raise RuntimeError("custom (Python) drivers cannot be sampled ahead of time at the adaptive times "
+                               "of SolverMode.DormandPrince")
         key = id(driver.callback)
         if key in self._cache:
             return self._cache[key]
@@ -129,6 +151,12 @@ def lower_layer(layer, rec, tables=None):
     rec["seed_lo"] = layer.noise_seed & 0xFFFFFFFF
     rec["seed_hi"] = (layer.noise_seed >> 32) & 0xFFFFFFFF
     rec["noise_step"] = layer.noise_step
+    ap = rec["adaptive"]
+    a = layer.adaptiveParams
+    for f in ("abs_tol", "rel_tol", "max_factor", "min_factor", "safety_factor", "ki", "kp", "kd",
+              "prev_error_ratio", "integral_error"):
+        ap[f] = getattr(a, f)
+    ap["use_pid_control"] = int(bool(a.use_pid_control))
     drv = rec["drv"]
     for name, idx in _SCALAR_INDEX.items():
         _fill_driver(drv[idx], layer.scalar[name], tables)
@@ -164,8 +192,6 @@ def validate(junctions, solver, max_layers=_abi.MAX_LAYERS):
                 raise RuntimeError("Failed to divide vector by zero!")
             if l.temperatureSet and solver in (SolverMode.EulerHeun, SolverMode.Heun) and l.cellVolume == 0.0:
                 raise RuntimeError("Cell surface cannot be 0 during temp. calculations!")
-    if solver == SolverMode.DormandPrince:
-        raise RuntimeError("SolverMode.DormandPrince is not implemented by the GPU solver")
 
 
 @dataclass
@@ -179,6 +205,7 @@ class Lowered:
 
 def lower(junctions, plan, solver, calculate_energies):
     solver = SolverMode(int(solver))
+    plan = plan.for_solver(solver)
     validate(junctions, solver)
     n_layers = sum(j.layerNo for j in junctions)
     jarr = np.zeros(len(junctions), dtype=_abi.JUNCTION_DTYPE)
@@ -204,6 +231,9 @@ def make_params(plan, solver, calculate_energies, width):
     p["solver"] = int(solver)
     p["calculate_energies"] = int(bool(calculate_energies))
     p["log_width"] = width
+    p["total_time"] = plan.total_time
+    p["write_frequency"] = plan.write_frequency
+    p["max_attempts"] = plan.max_attempts
     c = _constants.snapshot()
     for k in ("mu0", "gyro", "TtoAm", "hbar", "echarge", "kB"):
         p["c"][k] = c[k]
@@ -258,13 +288,23 @@ def apply_results(junctions, lowered, log, status, plan):
         off = int(lowered.junctions[k]["layer_offset"])
         code, rows = int(status[2 * k]), int(status[2 * k + 1])
         for i, l in enumerate(j.layers):
-            m = lowered.layers[off + i]["mag"]
+            rec = lowered.layers[off + i]
+            m = rec["mag"]
             l.mag.x, l.mag.y, l.mag.z = float(m[0]), float(m[1]), float(m[2])
             l.noise_step += plan.total_iterations
+            if plan.adaptive:
+                l.adaptiveParams.prev_error_ratio = float(rec["adaptive"]["prev_error_ratio"])
+                l.adaptiveParams.integral_error = float(rec["adaptive"]["integral_error"])
         if rows:
             j._append_log(decode_log(j, log[k, :rows], bool(lowered.params["calculate_energies"][0])), rows)
         if code == _abi.STATUS_NAN:
             nan = True
+        elif code == _abi.STATUS_DP_STALL:
+            raise RuntimeError(
+                "Dormand-Prince: a layer of a multi-layer junction rejected a step; the reference then uses the "
+                "unassigned Layer::hopt (-1) as the step and does not terminate (junction.hpp:1700-1705)")
+        elif code == _abi.STATUS_LIMIT:
+            raise RuntimeError("Dormand-Prince: no end after %d step attempts" % plan.max_attempts)
         elif code != _abi.STATUS_OK:
             raise RuntimeError("solver status %d for junction %d" % (code, k))
     if nan:

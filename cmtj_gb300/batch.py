@@ -31,7 +31,8 @@ TGT_HX, TGT_HY, TGT_HZ, TGT_K, TGT_K2, TGT_JB, TGT_JT, TGT_J2B, TGT_J2T = range(
 TGT_I, TGT_FL, TGT_DL, TGT_FL2, TGT_DL2, TGT_T = 9, 10, 11, 12, 13, 14
 
 FEAT_FULL_DEMAG, FEAT_DIPOLE, FEAT_IDMI, FEAT_K2 = 1, 2, 4, 8
-FEAT_STT, FEAT_SOT, FEAT_WAVES, FEAT_SCALAR_WAVES, FEAT_IEC2, FEAT_ALL = 16, 32, 64, 128, 256, 511
+FEAT_STT, FEAT_SOT, FEAT_WAVES, FEAT_SCALAR_WAVES, FEAT_IEC2 = 16, 32, 64, 128, 256
+FEAT_OFFAXIS, FEAT_ALL = 512, 1023
 
 F32_STT, F32_SOT, F32_SOT_STATIC, F32_ALT_STT = 1, 2, 4, 8
 LOG_NONE, LOG_M, LOG_MIX, LOG_R = 0, 1, 2, 3
@@ -253,6 +254,23 @@ class BatchSpec:
         sp.anis[:, :, 2] = 1.0
         return sp
 
+    def take(self, rows):
+        """A new BatchSpec holding rows `rows` (in that order) of this one."""
+        import dataclasses
+        rows = np.asarray(rows, dtype=np.int64)
+        out = {}
+        for f in dataclasses.fields(self):
+            v = getattr(self, f.name)
+            if f.name == "n":
+                out["n"] = len(rows)
+            elif isinstance(v, np.ndarray) and v.ndim >= 1 and v.shape[0] == self.n:
+                out[f.name] = v[rows].copy()
+            elif isinstance(v, list) and len(v) == self.n:
+                out[f.name] = [v[k] for k in rows]
+            else:
+                out[f.name] = v
+        return BatchSpec(**out)
+
     @staticmethod
     def from_junctions(junctions):
         sp = BatchSpec.empty(len(junctions))
@@ -468,6 +486,7 @@ def lower(spec, time_step, n_steps, win_start=None):
                      FEAT_DIPOLE, 0)
     feat |= np.where((((np.abs(spec.Db).sum(2) + np.abs(spec.Dt).sum(2)) > 0) & lmask).any(axis=1), FEAT_IDMI, 0)
     feat |= np.where(((spec.K2 != 0) & lmask).any(axis=1), FEAT_K2, 0)
+    feat |= np.where((((spec.anis != 0).sum(axis=2) > 1) & lmask).any(axis=1), FEAT_OFFAXIS, 0)
     feat |= np.where((((spec.J2b != 0) | (spec.J2t != 0)) & lmask).any(axis=1), FEAT_IEC2, 0)
     feat |= np.where((((spec.flags & F32_STT) != 0) & lmask).any(axis=1), FEAT_STT, 0)
     feat |= np.where((((spec.flags & F32_SOT) != 0) & lmask).any(axis=1), FEAT_SOT, 0)

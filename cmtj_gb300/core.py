@@ -998,6 +998,7 @@ class Junction:
         begin = _time.perf_counter()
         plan = engine.plan_run(totalTime, timeStep, writeFrequency)
         solver = self.getSolver(solverMode)
+        plan = plan.for_solver(solver)
         engine.run_junctions([self], plan, solver, bool(calculateEnergies))
         if verbose:
             print("Steps in simulation: %d" % plan.total_iterations)

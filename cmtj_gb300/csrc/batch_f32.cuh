@@ -66,11 +66,19 @@ template <int FEAT> struct Feat {
   static constexpr bool swaves = (FEAT & CMTJ_FEAT_SCALAR_WAVES) != 0;
   static constexpr bool iec2 = (FEAT & CMTJ_FEAT_IEC2) != 0;
   static constexpr bool twaves = waves && (stt || sot);  // current / torque waves
+  static constexpr bool offaxis = (FEAT & CMTJ_FEAT_OFFAXIS) != 0;
+  // anisotropy (constant K along a coordinate axis) + diagonal demag fold
+  // into one diagonal tensor: H += M m with M_i = 2K a_i^2/(mu0 Ms) - N_ii
+  static constexpr bool diag = !full_demag && !k2 && !swaves && !offaxis;
+  // every field term is stored pre-multiplied by the layer's gamma dt
+  // prefactor, so the torque needs no final scaling
+  static constexpr bool prescale = diag && !sot && !dipole && !idmi;
 };
 
 // Per-layer constants held in registers for the life of a junction.
 template <int FEAT> struct LayerP {
   F3 a;
+  F3 M;  // diag: the folded anisotropy + demag tensor (times gdt when prescale)
   float kc, k2c;
   float N[9];
   float Db[9], Dt[9];
@@ -134,6 +142,17 @@ template <int FEAT> struct LayerP {
       fl20 = r.fl20;
       dl20 = r.dl20;
     }
+    if (F::diag) {
+      M = f3(fmaf(kc * a.x, a.x, -N[0]), fmaf(kc * a.y, a.y, -N[4]), fmaf(kc * a.z, a.z, -N[8]));
+    }
+    if (F::prescale) {
+      M = M * gdt;
+      h0 = h0 * gdt;
+      jb *= gdt;
+      jt *= gdt;
+      j2b *= gdt;
+      j2t *= gdt;
+    }
     sigc = r.sig_c;
     t0 = r.t0;
     seed_lo = r.seed_lo;
@@ -191,15 +210,17 @@ template <int L> struct WaveR {
   uint64_t ph0, dph, dphh;
   uint32_t on0, off0, on1, off1, on2, off2;
 
-  __device__ __forceinline__ void load(const cmtj_wave_t &w) {
+  // hscale[l]: factor on layer l's field contributions (its gamma dt
+  // prefactor when the variant pre-scales fields, else 1)
+  __device__ __forceinline__ void load(const cmtj_wave_t &w, const float *hscale) {
     target = w.target;
     kind = w.kind;
     field = target <= CMTJ_TGT_HZ;
 #pragma unroll
     for (int l = 0; l < L; ++l) {
       amp[l] = ((w.layer_mask >> l) & 1) ? w.amp : 0.f;
-      hdir[l] = f3(target == CMTJ_TGT_HX ? amp[l] : 0.f, target == CMTJ_TGT_HY ? amp[l] : 0.f,
-                   target == CMTJ_TGT_HZ ? amp[l] : 0.f);
+      const float h = amp[l] * hscale[l];
+      hdir[l] = f3(target == CMTJ_TGT_HX ? h : 0.f, target == CMTJ_TGT_HY ? h : 0.f, target == CMTJ_TGT_HZ ? h : 0.f);
     }
     p0 = w.p0;
     p1 = w.p1;
@@ -274,33 +295,56 @@ __device__ __forceinline__ void add_wave(const WaveR<L> &w, uint32_t step, int s
   }
 }
 
-// Effective field + LL torque of one layer (junction.hpp:580-815), returned
-// already multiplied by dt (Euler-Heun, Heun: f dt) or by dt/6 (RK4: k/6).
+// The part of one layer's effective field that does not depend on its own
+// m (junction.hpp:590-622, 654-701): the constant + wave field, then the
+// neighbour terms (bilinear IEC, IDMI, dipole) from the neighbour
+// magnetisations mb / mt.  The RK4 runner freezes neighbours for the whole
+// step (junction.hpp:1682-1707), so this sum is formed once per stage time,
+// not once per stage.  Quadratic IEC depends on m and stays in rhs().
 template <int FEAT, bool HB, bool HT>
-__device__ __forceinline__ F3 rhs(const LayerP<FEAT> &P, F3 m, F3 mb, F3 mt, const Delta<FEAT> &d) {
+__device__ __forceinline__ F3 hbase(const LayerP<FEAT> &P, F3 mb, F3 mt, const Delta<FEAT> &d) {
   using F = Feat<FEAT>;
   F3 H = F::waves ? d.dH : P.h0;
-  const float da = dot(P.a, m);
-  float ka = F::swaves ? P.kc + d.dK : P.kc;
-  if (F::k2) ka = fmaf(F::swaves ? P.k2c + d.dK2 : P.k2c, da * da, ka);
-  H = fma3(P.a, ka * da, H);
   if (HB) {
-    const float jb = F::swaves ? P.jb + d.dJb : P.jb;
-    const float cb = F::iec2 ? fmaf(F::swaves ? P.j2b + d.dJ2b : P.j2b, dot(mb, m), jb) : jb;
-    H = fma3(mb, cb, H);
+    if (!F::iec2) H = fma3(mb, F::swaves ? P.jb + d.dJb : P.jb, H);
     if (F::idmi) H = H + cross(mb, P.dmib);
     if (F::dipole) H = H - matvec(P.Db, mb);
   }
   if (HT) {
-    const float jt = F::swaves ? P.jt + d.dJt : P.jt;
-    const float ct = F::iec2 ? fmaf(F::swaves ? P.j2t + d.dJ2t : P.j2t, dot(mt, m), jt) : jt;
-    H = fma3(mt, ct, H);
+    if (!F::iec2) H = fma3(mt, F::swaves ? P.jt + d.dJt : P.jt, H);
     if (F::idmi) H = H + cross(mt, P.dmit);
     if (F::dipole) H = H - matvec(P.Dt, mt);
   }
+  return H;
+}
+
+// Effective field + LL torque of one layer (junction.hpp:580-815) given its
+// hbase() sum H, returned already multiplied by dt (Euler-Heun, Heun: f dt)
+// or by dt/6 (RK4: k/6).
+template <int FEAT, bool HB, bool HT>
+__device__ __forceinline__ F3 rhs(const LayerP<FEAT> &P, F3 m, F3 mb, F3 mt, const Delta<FEAT> &d, F3 H) {
+  using F = Feat<FEAT>;
+  if (F::diag) {
+    H = f3(fmaf(P.M.x, m.x, H.x), fmaf(P.M.y, m.y, H.y), fmaf(P.M.z, m.z, H.z));
+  } else {
+    const float da = dot(P.a, m);
+    float ka = F::swaves ? P.kc + d.dK : P.kc;
+    if (F::k2) ka = fmaf(F::swaves ? P.k2c + d.dK2 : P.k2c, da * da, ka);
+    H = fma3(P.a, ka * da, H);
+  }
+  if (F::iec2) {
+    if (HB) {
+      const float jb = F::swaves ? P.jb + d.dJb : P.jb;
+      H = fma3(mb, fmaf(F::swaves ? P.j2b + d.dJ2b : P.j2b, dot(mb, m), jb), H);
+    }
+    if (HT) {
+      const float jt = F::swaves ? P.jt + d.dJt : P.jt;
+      H = fma3(mt, fmaf(F::swaves ? P.j2t + d.dJ2t : P.j2t, dot(mt, m), jt), H);
+    }
+  }
   if (F::full_demag) {
     H = H - matvec(P.N, m);
-  } else {
+  } else if (!F::diag) {
     H = f3(fmaf(-P.N[0], m.x, H.x), fmaf(-P.N[4], m.y, H.y), fmaf(-P.N[8], m.z, H.z));
   }
   const F3 mxH = cross(m, H);
@@ -324,7 +368,7 @@ __device__ __forceinline__ F3 rhs(const LayerP<FEAT> &P, F3 m, F3 mb, F3 mt, con
       const F3 fl = cross(m, p);
       const F3 dl = cross(m, fl);
       // gdt carries -gamma dt/(1+alpha^2), sttc dt/(1+alpha^2) (each /6 for RK4).
-      return fma3(fl, s * P.sttb, fma3(dl, -s * P.sttk, acc * P.gdt));
+      return fma3(fl, s * P.sttb, fma3(dl, -s * P.sttk, F::prescale ? acc : acc * P.gdt));
     }
     if (F::sot && (P.flags & CMTJ_F32_SOT)) {
       float hfl, hdl, hfl2 = 0.f, hdl2 = 0.f;
@@ -346,7 +390,7 @@ __device__ __forceinline__ F3 rhs(const LayerP<FEAT> &P, F3 m, F3 mb, F3 mt, con
       acc = fma3(cross(m, cs), fmaf(P.alpha, hfl2, hdl2), acc);
     }
   }
-  return acc * P.gdt;
+  return F::prescale ? acc : acc * P.gdt;
 }
 
 // stochasticTorque (junction.hpp:824-831).
@@ -354,6 +398,98 @@ template <int FEAT>
 __device__ __forceinline__ F3 stoch(const LayerP<FEAT> &P, F3 m, F3 dW) {
   const F3 th = cross(m, dW);
   return fma3(cross(m, th), P.alpha, th) * P.gam;
+}
+
+// Layer l of an L-layer stack: which neighbours it has (edge layers see a
+// zero vector, junction.hpp:1686-1695).
+template <int L, int FEAT>
+__device__ __forceinline__ F3 hbase_at(int l, const LayerP<FEAT> &P, F3 mb, F3 mt, const Delta<FEAT> &d) {
+  if (L == 1) return hbase<FEAT, false, false>(P, mb, mt, d);
+  if (l == 0) return hbase<FEAT, false, true>(P, mb, mt, d);
+  if (l == L - 1) return hbase<FEAT, true, false>(P, mb, mt, d);
+  return hbase<FEAT, true, true>(P, mb, mt, d);
+}
+template <int L, int FEAT>
+__device__ __forceinline__ F3 rhs_at(int l, const LayerP<FEAT> &P, F3 m, F3 mb, F3 mt, const Delta<FEAT> &d, F3 H) {
+  if (L == 1) return rhs<FEAT, false, false>(P, m, mb, mt, d, H);
+  if (l == 0) return rhs<FEAT, false, true>(P, m, mb, mt, d, H);
+  if (l == L - 1) return rhs<FEAT, true, false>(P, m, mb, mt, d, H);
+  return rhs<FEAT, true, true>(P, m, mb, mt, d, H);
+}
+
+// ---- Packed two-layer form.  A 2-layer junction runs both layers through
+// the same arithmetic, so each float2 holds (layer 0, layer 1) and every
+// vector operation is one packed FFMA2 / FMUL2 / FADD2 instead of two
+// scalar ones: half the issue slots for the same FMA-pipe work.  Each lane
+// repeats the scalar path's operations in the same order, so both forms give
+// the same bits.
+struct V2 {
+  float2 x, y, z;
+};
+__device__ __forceinline__ float2 bc2(float s) { return make_float2(s, s); }
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ V2 v2(float2 x, float2 y, float2 z) {
+  V2 r;
+  r.x = x;
+  r.y = y;
+  r.z = z;
+  return r;
+}
+__device__ __forceinline__ V2 pack2(F3 a, F3 b) {
+  return v2(make_float2(a.x, b.x), make_float2(a.y, b.y), make_float2(a.z, b.z));
+}
+__device__ __forceinline__ F3 lane0(V2 v) { return f3(v.x.x, v.y.x, v.z.x); }
+__device__ __forceinline__ F3 lane1(V2 v) { return f3(v.x.y, v.y.y, v.z.y); }
+__device__ __forceinline__ V2 swap2(V2 v) {
+  return v2(make_float2(v.x.y, v.x.x), make_float2(v.y.y, v.y.x), make_float2(v.z.y, v.z.x));
+}
+__device__ __forceinline__ V2 v2add(V2 a, V2 b) {
+  return v2(__fadd2_rn(a.x, b.x), __fadd2_rn(a.y, b.y), __fadd2_rn(a.z, b.z));
+}
+__device__ __forceinline__ V2 v2mul(V2 a, float2 s) {
+  return v2(__fmul2_rn(a.x, s), __fmul2_rn(a.y, s), __fmul2_rn(a.z, s));
+}
+// a * s + b, s per layer
+__device__ __forceinline__ V2 v2fma(V2 a, float2 s, V2 b) {
+  return v2(__ffma2_rn(a.x, s, b.x), __ffma2_rn(a.y, s, b.y), __ffma2_rn(a.z, s, b.z));
+}
+// a * s + b componentwise
+__device__ __forceinline__ V2 v2fmav(V2 a, V2 s, V2 b) {
+  return v2(__ffma2_rn(a.x, s.x, b.x), __ffma2_rn(a.y, s.y, b.y), __ffma2_rn(a.z, s.z, b.z));
+}
+__device__ __forceinline__ float2 v2dot(V2 a, V2 b) {
+  return __ffma2_rn(a.x, b.x, __ffma2_rn(a.y, b.y, __fmul2_rn(a.z, b.z)));
+}
+__device__ __forceinline__ V2 v2cross(V2 a, V2 b) {
+  return v2(__ffma2_rn(a.y, b.z, neg2(__fmul2_rn(a.z, b.y))), __ffma2_rn(a.z, b.x, neg2(__fmul2_rn(a.x, b.z))),
+            __ffma2_rn(a.x, b.y, neg2(__fmul2_rn(a.y, b.x))));
+}
+__device__ __forceinline__ V2 v2renorm(V2 m) {
+  const float2 q = v2dot(m, m);
+  return v2mul(m, make_float2(rsqrtf(q.x), rsqrtf(q.y)));
+}
+
+// Both layers' constants of a 2-layer junction whose variant has only the
+// constant field, field waves, uniaxial anisotropy along a coordinate axis,
+// diagonal demag and bilinear IEC: every field term pre-scaled by the
+// layer's gamma dt prefactor (LayerP with Feat::prescale).
+struct PairP {
+  V2 M, h0;      // folded anisotropy + demag tensor, constant field
+  float2 alpha;  // per layer
+  float2 jn;     // IEC of the one neighbour: (jt of layer 0, jb of layer 1)
+  template <int FEAT> __device__ __forceinline__ void load(const LayerP<FEAT> &p0, const LayerP<FEAT> &p1) {
+    M = pack2(p0.M, p1.M);
+    h0 = pack2(p0.h0, p1.h0);
+    alpha = make_float2(p0.alpha, p1.alpha);
+    jn = make_float2(p0.jt, p1.jb);
+  }
+};
+
+// rhs() of both layers at once, given hbase() of both layers.
+__device__ __forceinline__ V2 rhs2(const PairP &Q, V2 m, V2 H) {
+  H = v2fmav(Q.M, m, H);
+  const V2 mxH = v2cross(m, H);
+  return v2fma(v2cross(m, mxH), Q.alpha, mxH);
 }
 
 struct Args {
@@ -425,9 +561,16 @@ __global__ void __launch_bounds__(128, (FEAT == CMTJ_FEAT_ALL) ? 1 : CMTJ_BATCH_
   const uint32_t T = p.log_tile;
   float *tile = smem + (size_t)threadIdx.x * T * (C > 0 ? C : 1);
 
+  // Packed two-layer RK4 for the variants with only constant / wave fields,
+  // uniaxial anisotropy, diagonal demag and bilinear IEC.
+  constexpr bool kPacked = L == 2 && SOLVER == CMTJ_RK4 && (FEAT & ~CMTJ_FEAT_WAVES) == 0;
+  static_assert(!kPacked || Feat<FEAT>::prescale, "the packed path reads pre-scaled fields");
+
   // junction-lifetime registers
   LayerP<FEAT> P[L];
   WaveR<L> W[NW > 0 ? NW : 1];
+  PairP Q;                      // kPacked: both layers' constants
+  V2 HD[NW > 0 ? NW : 1];       // kPacked: each wave's field direction x amplitude, both layers
   int nw = 0;
   F3 m[L];
   int32_t jid = -1;
@@ -466,10 +609,19 @@ __global__ void __launch_bounds__(128, (FEAT == CMTJ_FEAT_ALL) ? 1 : CMTJ_BATCH_
 #pragma unroll
             for (int l = 0; l < L; ++l) P[l].load(A.Ly[J.layer_offset + l], SOLVER == CMTJ_RK4);
             if (F::waves) {
+              float hs[L];
+#pragma unroll
+              for (int l = 0; l < L; ++l) hs[l] = F::prescale ? P[l].gdt : 1.f;
               nw = J.n_waves < NW ? J.n_waves : NW;
 #pragma unroll
               for (int w = 0; w < NW; ++w)
-                if (w < nw) W[w].load(J.waves[w]);
+                if (w < nw) W[w].load(J.waves[w], hs);
+            }
+            if constexpr (kPacked) {
+              Q.load(P[0], P[1]);
+#pragma unroll
+              for (int w = 0; w < NW; ++w)
+                if (w < nw) HD[w] = pack2(W[w].hdir[0], W[w].hdir[1]);
             }
             step = S.step;
             if (step == 0) {
@@ -512,10 +664,39 @@ __global__ void __launch_bounds__(128, (FEAT == CMTJ_FEAT_ALL) ? 1 : CMTJ_BATCH_
     while (step < burst_end) {
       const uint32_t next_ev = next_log < next_red ? next_log : next_red;
       const uint32_t stop = (next_ev < burst_end) ? next_ev + 1 : burst_end;
+      if constexpr (kPacked) {
+        // RK4 on both layers at once (the scalar RK4 below, lane by lane)
+        V2 mp = pack2(m[0], m[1]);
+        for (; step < stop; ++step) {
+          const V2 nb = swap2(mp);  // frozen neighbours: layer 0 sees layer 1, layer 1 sees layer 0
+          V2 hb, acc, kp;
+#pragma unroll
+          for (int st = 0; st < 4; ++st) {
+            const int s = st == 0 ? 0 : (st == 3 ? 2 : 1);
+            if ((F::waves && st != 2) || (!F::waves && st == 0)) {
+              hb = Q.h0;
+              if (F::waves) {
+#pragma unroll
+                for (int w = 0; w < NW; ++w)
+                  if (w < nw) hb = v2fma(HD[w], bc2(W[w].unit(step, s, dtf)), hb);
+              }
+              hb = v2fma(nb, Q.jn, hb);
+            }
+            const V2 ms = st == 0 ? mp : v2fma(kp, bc2(st == 3 ? 6.f : 3.f), mp);
+            kp = rhs2(Q, ms, hb);
+            if (st == 0) acc = kp;
+            else if (st == 3) acc = v2add(acc, kp);
+            else acc = v2fma(kp, bc2(2.f), acc);
+          }
+          mp = v2renorm(v2add(mp, acc));
+        }
+        m[0] = lane0(mp);
+        m[1] = lane1(mp);
+      } else {
       for (; step < stop; ++step) {
       if (SOLVER == CMTJ_RK4) {
         // neighbours frozen at their start-of-step values (junction.hpp:1682-1707)
-        F3 acc[L], kp[L];
+        F3 acc[L], kp[L], hb[L];
         Delta<FEAT> d[L];
 #pragma unroll
         for (int st = 0; st < 4; ++st) {
@@ -528,6 +709,10 @@ __global__ void __launch_bounds__(128, (FEAT == CMTJ_FEAT_ALL) ? 1 : CMTJ_BATCH_
               for (int w = 0; w < NW; ++w)
                 if (w < nw) add_wave<L, FEAT>(W[w], step, s, dtf, d);
             }
+#pragma unroll
+            for (int l = 0; l < L; ++l)
+              hb[l] = hbase_at<L, FEAT>(l, P[l], l > 0 ? m[l - 1] : f3(0.f, 0.f, 0.f),
+                                        l < L - 1 ? m[l + 1] : f3(0.f, 0.f, 0.f), d[l]);
           }
           // k' = k/6 through the host's dt/6 prefactors, so the stage
           // offsets (3k', 3k', 6k') and weights (1, 2, 2, 1) are exact; the
@@ -539,11 +724,7 @@ __global__ void __launch_bounds__(128, (FEAT == CMTJ_FEAT_ALL) ? 1 : CMTJ_BATCH_
             const F3 ms = st == 0 ? m[l] : fma3(kp[l], c, m[l]);
             const F3 mb = l > 0 ? m[l - 1] : f3(0.f, 0.f, 0.f);
             const F3 mt = l < L - 1 ? m[l + 1] : f3(0.f, 0.f, 0.f);
-            F3 k;
-            if (l == 0 && L == 1) k = rhs<FEAT, false, false>(P[l], ms, mb, mt, d[l]);
-            else if (l == 0) k = rhs<FEAT, false, true>(P[l], ms, mb, mt, d[l]);
-            else if (l == L - 1) k = rhs<FEAT, true, false>(P[l], ms, mb, mt, d[l]);
-            else k = rhs<FEAT, true, true>(P[l], ms, mb, mt, d[l]);
+            const F3 k = rhs_at<L, FEAT>(l, P[l], ms, mb, mt, d[l], hb[l]);
             kp[l] = k;
             if (st == 0) acc[l] = k;
             else if (st == 3) acc[l] = acc[l] + k;
@@ -576,10 +757,7 @@ __global__ void __launch_bounds__(128, (FEAT == CMTJ_FEAT_ALL) ? 1 : CMTJ_BATCH_
           }
           const F3 mb = l > 0 ? m[l - 1] : f3(0.f, 0.f, 0.f);
           const F3 mt = l < L - 1 ? m[l + 1] : f3(0.f, 0.f, 0.f);
-          if (l == 0 && L == 1) f[l] = rhs<FEAT, false, false>(P[l], m[l], mb, mt, d[l]);
-          else if (l == 0) f[l] = rhs<FEAT, false, true>(P[l], m[l], mb, mt, d[l]);
-          else if (l == L - 1) f[l] = rhs<FEAT, true, false>(P[l], m[l], mb, mt, d[l]);
-          else f[l] = rhs<FEAT, true, true>(P[l], m[l], mb, mt, d[l]);
+          f[l] = rhs_at<L, FEAT>(l, P[l], m[l], mb, mt, d[l], hbase_at<L, FEAT>(l, P[l], mb, mt, d[l]));
           g[l] = stoch<FEAT>(P[l], m[l], dW[l]);
         }
         if (SOLVER == CMTJ_EULER_HEUN) {
@@ -603,19 +781,17 @@ __global__ void __launch_bounds__(128, (FEAT == CMTJ_FEAT_ALL) ? 1 : CMTJ_BATCH_
           }
 #pragma unroll
           for (int l = 0; l < L; ++l) {
+            // the corrector sees the predicted neighbours (junction.hpp:1790-1800)
             const F3 mb = l > 0 ? mn[l - 1] : f3(0.f, 0.f, 0.f);
             const F3 mt = l < L - 1 ? mn[l + 1] : f3(0.f, 0.f, 0.f);
-            F3 f2;
-            if (l == 0 && L == 1) f2 = rhs<FEAT, false, false>(P[l], mn[l], mb, mt, d[l]);
-            else if (l == 0) f2 = rhs<FEAT, false, true>(P[l], mn[l], mb, mt, d[l]);
-            else if (l == L - 1) f2 = rhs<FEAT, true, false>(P[l], mn[l], mb, mt, d[l]);
-            else f2 = rhs<FEAT, true, true>(P[l], mn[l], mb, mt, d[l]);
+            const F3 f2 = rhs_at<L, FEAT>(l, P[l], mn[l], mb, mt, d[l], hbase_at<L, FEAT>(l, P[l], mb, mt, d[l]));
             const F3 g2 = stoch<FEAT>(P[l], mn[l], dW[l]);
             m[l] = renorm(m[l] + fma3(g[l] + g2, 0.5f * sqdt, (f[l] + f2) * 0.5f));
           }
         }
       }
       }  // steps up to (and including) the next sampling step
+      }
       const uint32_t last = step - 1;
 
       // ---- reductions: R and I(t) R(t) from win_start on

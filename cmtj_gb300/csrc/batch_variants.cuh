@@ -8,9 +8,11 @@
 #define CMTJ_BATCH_VARIANTS(X, L)                                        \
   X(L, CMTJ_RK4, 0, 1)                                                   \
   X(L, CMTJ_RK4, CMTJ_FEAT_WAVES, 1)                                     \
+  X(L, CMTJ_RK4, CMTJ_FEAT_WAVES | CMTJ_FEAT_OFFAXIS, 1)                 \
   X(L, CMTJ_RK4, CMTJ_FEAT_ALL, 4)                                       \
   X(L, CMTJ_EULER_HEUN, CMTJ_FEAT_WAVES, 1)                              \
   X(L, CMTJ_EULER_HEUN, CMTJ_FEAT_WAVES | CMTJ_FEAT_STT, 1)              \
+  X(L, CMTJ_EULER_HEUN, CMTJ_FEAT_WAVES | CMTJ_FEAT_STT | CMTJ_FEAT_OFFAXIS, 1) \
   X(L, CMTJ_EULER_HEUN, CMTJ_FEAT_ALL, 4)                                \
   X(L, CMTJ_HEUN, CMTJ_FEAT_ALL, 4)
 

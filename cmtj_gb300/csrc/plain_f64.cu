@@ -1,7 +1,7 @@
 // FP64 plain form of the macrospin time loop.
 //
 // One device thread runs one Junction::runSimulation (core/junction.hpp:
-// 1948-1981) from start to end.  Every floating-point expression keeps the
+// 1948-2045, fixed-step or Dormand-Prince) from start to end.  Every floating-point expression keeps the
 // reference's operand order, and this translation unit is compiled with
 // --fmad=false, so a*b+c is never contracted into an FMA: additions,
 // multiplications, divisions and square roots round exactly as the
@@ -45,15 +45,72 @@ __global__ void __launch_bounds__(64) k_run_simulation_f64(const cmtj_junction_t
   const bool energies = p.calculate_energies != 0;
   uint32_t row = 0, code = CMTJ_STATUS_OK;
   double *out = log + (size_t)j * p.n_log * p.log_width;
-  for (uint32_t i = 0; i < p.total_iterations; ++i) {
-    const double t = (double)i * dt;
-    if (!junction_step(n, Ls, mag, work, side, i, t, p, tables, nullptr, false)) {
-      code = CMTJ_STATUS_NAN;
-      break;
+  if (p.solver == CMTJ_DORMAND_PRINCE) {
+    // runSimulation's adaptive loop (junction.hpp:1982-2045).  Each layer's
+    // step sees the step size the previous layer's step chose (one shared
+    // timeStep reference in runMultiLayerSolver, 1680-1707), and t advances
+    // by the size chosen for the next step, both as in the reference.  A
+    // rejection with several layers stops with CMTJ_STATUS_DP_STALL where
+    // the reference continues from hopt = -1 without end.
+    double t = 0.0, next_write = 0.0, cur = dt;
+    uint64_t attempts = 0;
+    while (t < p.total_time) {
+      if (++attempts > p.max_attempts) {
+        code = CMTJ_STATUS_LIMIT;
+        break;
+      }
+      if (t + cur > p.total_time) cur = p.total_time - t;
+      int consecutive = 0;
+      if (isnan(cur) || isinf(cur) || cur <= 0) {
+        cur = dt;
+        consecutive++;
+      }
+      bool accepted = true, nan = false;
+      if (n > 1) {
+        work[0] = zero3();
+        work[n + 1] = zero3();
+        for (int l = 0; l < n; ++l) work[l + 1] = mag[l];
+        for (int l = 0; l < n; ++l)
+          if (!dp_layer(Ls[l], Ls[l].adaptive, p.c, t, cur, mag[l], work[l], work[l + 2], tables,
+                        energies ? &side[l] : nullptr, nan))
+            accepted = false;
+        if (!accepted) {
+          code = CMTJ_STATUS_DP_STALL;
+          break;
+        }
+      } else {
+        accepted = dp_layer(Ls[0], Ls[0].adaptive, p.c, t, cur, mag[0], zero3(), zero3(), tables,
+                            energies ? &side[0] : nullptr, nan);
+      }
+      if (nan) {
+        code = CMTJ_STATUS_NAN;
+        break;
+      }
+      if (!accepted && (cur < 1e-15 || consecutive >= 10)) accepted = true;
+      if (accepted) {
+        t += cur;
+        if (t >= next_write) {
+          if (row >= p.n_log) {
+            code = CMTJ_STATUS_LIMIT;
+            break;
+          }
+          log_row(out + (size_t)row * p.log_width, J, n, Ls, mag, side, t, energies);
+          ++row;
+          next_write = ((double)(uint32_t)(t / p.write_frequency) + 1) * p.write_frequency;
+        }
+      }
     }
-    if (!(i % p.write_every)) {
-      log_row(out + (size_t)row * p.log_width, J, n, Ls, mag, side, t, energies);
-      ++row;
+  } else {
+    for (uint32_t i = 0; i < p.total_iterations; ++i) {
+      const double t = (double)i * dt;
+      if (!junction_step(n, Ls, mag, work, side, i, t, p, tables, nullptr, false)) {
+        code = CMTJ_STATUS_NAN;
+        break;
+      }
+      if (!(i % p.write_every)) {
+        log_row(out + (size_t)row * p.log_width, J, n, Ls, mag, side, t, energies);
+        ++row;
+      }
     }
   }
   for (int l = 0; l < n; ++l) {
@@ -84,8 +141,15 @@ extern "C" int cmtj_run_simulation_f64(const cmtj_junction_t *d_junctions, int32
     cmtj_set_error("cmtj_run_simulation_f64: write_every must be >= 1");
     return CMTJ_ERR_ARG;
   }
-  if (p->solver != CMTJ_RK4 && p->solver != CMTJ_EULER_HEUN && p->solver != CMTJ_HEUN) {
-    cmtj_set_error("cmtj_run_simulation_f64: solver %d is not supported by the FP64 plain form", p->solver);
+  if (p->solver != CMTJ_RK4 && p->solver != CMTJ_EULER_HEUN && p->solver != CMTJ_HEUN &&
+      p->solver != CMTJ_DORMAND_PRINCE) {
+    cmtj_set_error("cmtj_run_simulation_f64: unknown solver %d", p->solver);
+    return CMTJ_ERR_ARG;
+  }
+  if (p->solver == CMTJ_DORMAND_PRINCE &&
+      !(p->write_frequency > 0 && p->time_step > 0 && p->total_time >= 0 && p->max_attempts > 0)) {
+    cmtj_set_error("cmtj_run_simulation_f64: Dormand-Prince needs time_step > 0, write_frequency > 0, "
+                   "total_time >= 0 and max_attempts > 0");
     return CMTJ_ERR_ARG;
   }
   const int threads = 64;

@@ -308,6 +308,66 @@ static __device__ bool junction_step(int n, const cmtj_layer_t *Ls, D3 *mag, D3 
   return true;
 }
 
+// Layer::dormand_prince_step (junction.hpp:866-1002) of one layer: tries a
+// step of size ts from time t, sets ts to the next step size (whether the
+// step is accepted or not) and updates the layer's PID state in place.
+// Returns accepted; nan is set when an accepted m is NaN.  Custom drivers
+// are rejected by the host (their tables hold fixed-step times only).
+static __device__ bool dp_layer(const cmtj_layer_t &L, cmtj_adaptive_t &ap, const cmtj_constants_t &c, double t,
+                                double &ts, D3 &mag, const D3 &bottom, const D3 &top, const double *tables,
+                                Side *side, bool &nan) {
+  const DriverCtx dc = {tables, 0u, 0};
+  const D3 m_t = mag;
+  const double c2 = 1.0 / 5.0, c3 = 3.0 / 10.0, c4 = 4.0 / 5.0, c5 = 8.0 / 9.0, c6 = 1.0, c7 = 1.0;
+  const D3 k1 = rhs(L, c, t, m_t, bottom, top, dc, nullptr) * ts;
+  const D3 k2 = rhs(L, c, t + c2 * ts, m_t + k1 * (c2), bottom, top, dc, nullptr) * ts;
+  const D3 k3 = rhs(L, c, t + c3 * ts, m_t + k1 * (3.0 / 40.0) + k2 * (9.0 / 40.0), bottom, top, dc, nullptr) * ts;
+  const D3 k4 = rhs(L, c, t + c4 * ts, m_t + k1 * (44.0 / 45.0) + k2 * (-56.0 / 15.0) + k3 * (32.0 / 9.0), bottom,
+                    top, dc, nullptr) * ts;
+  const D3 k5 = rhs(L, c, t + c5 * ts,
+                    m_t + k1 * (19372.0 / 6561.0) + k2 * (-25360.0 / 2187.0) + k3 * (64448.0 / 6561.0) +
+                        k4 * (-212.0 / 729.0),
+                    bottom, top, dc, nullptr) * ts;
+  const D3 k6 = rhs(L, c, t + c6 * ts,
+                    m_t + k1 * (9017.0 / 3168.0) + k2 * (-355.0 / 33.0) + k3 * (46732.0 / 5247.0) +
+                        k4 * (49.0 / 176.0) + k5 * (-5103.0 / 18656.0),
+                    bottom, top, dc, nullptr) * ts;
+  const D3 k7 = rhs(L, c, t + c7 * ts,
+                    m_t + k1 * (35.0 / 384.0) + k3 * (500.0 / 1113.0) + k4 * (125.0 / 192.0) +
+                        k5 * (-2187.0 / 6784.0) + k6 * (11.0 / 84.0),
+                    bottom, top, dc, side) * ts;
+  const D3 m5 = m_t + k1 * (35.0 / 384.0) + k3 * (500.0 / 1113.0) + k4 * (125.0 / 192.0) +
+                k5 * (-2187.0 / 6784.0) + k6 * (11.0 / 84.0);
+  const D3 m4 = m_t + k1 * (5179.0 / 57600.0) + k3 * (7571.0 / 16695.0) + k4 * (393.0 / 640.0) +
+                k5 * (-92097.0 / 339200.0) + k6 * (187.0 / 2100.0) + k7 * (1.0 / 40.0);
+  const D3 err = m5 - m4;
+  const double err_norm = sqrt(err.x * err.x + err.y * err.y + err.z * err.z);
+  const double tol = ap.abs_tol + ap.rel_tol * sqrt(m_t.x * m_t.x + m_t.y * m_t.y + m_t.z * m_t.z);
+  double ratio = err_norm / tol;
+  if (tol < 1e-15 || isnan(ratio) || isinf(ratio)) ratio = 10.0;
+  double factor;
+  if (ap.use_pid_control) {
+    const double e_n = log(ratio);
+    ap.integral_error += e_n;
+    factor = exp(ap.kp * e_n + ap.ki * ap.integral_error + ap.kd * (e_n - ap.prev_error_ratio));
+    ap.prev_error_ratio = e_n;
+  } else {
+    factor = ap.safety_factor * pow(1.0 / ratio, 0.2);
+  }
+  if (isnan(factor) || isinf(factor)) factor = ap.min_factor;
+  factor = fmin(factor, ap.max_factor);
+  factor = fmax(factor, ap.min_factor);
+  double next = ts * factor;
+  if (isnan(next) || isinf(next) || next <= 0) next = ts * ap.min_factor;
+  ts = next;
+  if (ratio <= 1.0) {
+    mag = normalized(m5);
+    if (isnan(mag.x)) nan = true;
+    return true;
+  }
+  return false;
+}
+
 // logLayerParams (junction.hpp:1580-1636) into one row of p.log_width doubles.
 static __device__ void log_row(double *r, const cmtj_junction_t &J, int n, const cmtj_layer_t *Ls, const D3 *mag,
                         const Side *side, double t, bool energies) {

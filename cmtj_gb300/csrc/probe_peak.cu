@@ -1,6 +1,7 @@
 // Measurement probe (libcmtj_probe.so, used by bench.py only): FP32 FMA
 // throughput of this GPU, the denominator of the FP32 roofline.  Each
 // thread runs 8 independent FMA chains so the pipe, not latency, bounds it.
+// Two forms: scalar FFMA, and the packed two-lane __ffma2_rn (sm_100+).
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -19,8 +20,25 @@ __global__ void k_fma_peak(int iters, float seed, float *out) {
   if (s == 1234.5f) out[0] = s;  // keeps the chains live
 }
 
-// Runs the probe `reps` times; returns the best FP32 FLOP/s (2 per FMA).
-extern "C" double cmtj_probe_fp32_peak(int reps) {
+__global__ void k_fma2_peak(int iters, float seed, float *out) {
+  float2 a[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) a[k] = make_float2(seed + threadIdx.x * 1e-7f + k, seed - k);
+  const float2 b = make_float2(0.999999f, 0.999998f), c = make_float2(1e-7f, 2e-7f);
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) a[k] = __ffma2_rn(a[k], b, c);
+  }
+  float s = 0.f;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) s += a[k].x + a[k].y;
+  if (s == 1234.5f) out[0] = s;
+}
+
+namespace {
+// Runs one probe kernel `reps` times; returns the best FLOP/s (2 per lane FMA).
+template <typename K>
+double time_probe(K kernel, int reps, double lanes) {
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -30,16 +48,16 @@ extern "C" double cmtj_probe_fp32_peak(int reps) {
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  k_fma_peak<<<blocks, threads>>>(iters, 1.0f, out);
+  kernel<<<blocks, threads>>>(iters, 1.0f, out);
   double best = 0.0;
   for (int r = 0; r < reps; ++r) {
     cudaEventRecord(e0);
-    k_fma_peak<<<blocks, threads>>>(iters, 1.0f, out);
+    kernel<<<blocks, threads>>>(iters, 1.0f, out);
     cudaEventRecord(e1);
     cudaEventSynchronize(e1);
     float ms = 0.f;
     cudaEventElapsedTime(&ms, e0, e1);
-    const double flops = 2.0 * 8.0 * (double)iters * threads * blocks;
+    const double flops = 2.0 * lanes * 8.0 * (double)iters * threads * blocks;
     if (ms > 0 && flops / (ms * 1e-3) > best) best = flops / (ms * 1e-3);
   }
   cudaEventDestroy(e0);
@@ -47,3 +65,9 @@ extern "C" double cmtj_probe_fp32_peak(int reps) {
   cudaFree(out);
   return best;
 }
+}  // namespace
+
+// Best FP32 FLOP/s of scalar FFMA over `reps` runs.
+extern "C" double cmtj_probe_fp32_peak(int reps) { return time_probe(k_fma_peak, reps, 1.0); }
+// Best FP32 FLOP/s of packed FFMA2 (two FMAs per lane per instruction).
+extern "C" double cmtj_probe_fp32x2_peak(int reps) { return time_probe(k_fma2_peak, reps, 2.0); }

@@ -72,6 +72,7 @@ def run_lowered_f64(lowered, stream=None):
 def run_junctions(junctions, plan, solver, calculate_energies=False):
     """Junction::runSimulation for a list of junctions sharing one plan
     (each junction keeps its own layers, drivers and log)."""
+    plan = plan.for_solver(solver)
     lowered = lower(junctions, plan, solver, calculate_energies)
     require_gpu()
     log, status, layers = run_lowered_f64(lowered)

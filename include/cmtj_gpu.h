@@ -38,6 +38,12 @@ extern "C" {
 #define CMTJ_STATUS_NAN 1u       /* "NAN magnetisation" (junction.hpp:1037) */
 #define CMTJ_STATUS_NOT_RUN 2u   /* junction never reached (work queue bug)  */
 #define CMTJ_STATUS_BAD_INPUT 3u /* layer count outside the supported range  */
+/* Dormand-Prince, multi-layer: a layer rejected the step.  The reference
+ * then takes the step size from Layer::hopt, which is never assigned (-1,
+ * junction.hpp:259, 1700-1705); the forced acceptance that follows moves t
+ * back by 1 s and the run does not terminate.  The GPU solver stops here. */
+#define CMTJ_STATUS_DP_STALL 4u
+#define CMTJ_STATUS_LIMIT 5u     /* Dormand-Prince: more than max_attempts steps */
 
 /* ScalarDriver update types: drivers.hpp:18-29 (UpdateType). */
 enum cmtj_update_type {
@@ -100,6 +106,16 @@ enum cmtj_mr_mode { CMTJ_MR_NONE = 0, CMTJ_MR_CLASSIC = 1, CMTJ_MR_STRIP = 2,
                     * series formula of cmtj/utils/resistance.py:121-150 */
                    CMTJ_MR_SERIES = 3 };
 
+/* AdaptiveIntegrationParams<double> (junction.hpp:125-139) of one layer.
+ * prev_error_ratio and integral_error are the PID controller's state, which
+ * the solver updates in place like mag. */
+typedef struct cmtj_adaptive {
+  double abs_tol, rel_tol, max_factor, min_factor, safety_factor;
+  double ki, kp, kd;
+  double prev_error_ratio, integral_error;
+  int32_t use_pid_control, reserved;
+} cmtj_adaptive_t;         /* 88 bytes */
+
 /* One Layer<double> (junction.hpp:145-258), as the solver needs it. */
 typedef struct cmtj_layer {
   double mag[3];             /* current magnetisation (the solver state)   */
@@ -117,6 +133,7 @@ typedef struct cmtj_layer {
   uint32_t seed_lo, seed_hi; /* Philox4x32-10 key of this layer's noise    */
   uint64_t noise_step;       /* Philox step counter at iteration 0         */
   cmtj_driver_t drv[CMTJ_NUM_SLOTS];
+  cmtj_adaptive_t adaptive;  /* Dormand-Prince step control               */
 } cmtj_layer_t;
 
 /* One Junction<double> (junction.hpp:1139-1243). */
@@ -142,16 +159,22 @@ typedef struct cmtj_constants {
  * host has resolved them exactly as the reference does:
  *   total_iterations = (unsigned)(totalTime / timeStep)
  *   write_every      = (unsigned)(writeFrequency / timeStep)
- *   solver           = getSolver(...) result (junction.hpp:1891-1931). */
+ *   solver           = getSolver(...) result (junction.hpp:1891-1931).
+ * Dormand-Prince (junction.hpp:1982-2045) reads total_time, write_frequency
+ * and time_step (the first step) instead of the two counts; its log holds at
+ * most floor(total_time / write_frequency) + 2 rows. */
 typedef struct cmtj_sim_params {
   double time_step;
   uint32_t total_iterations;
   uint32_t write_every;
-  uint32_t n_log;            /* rows written: ceil(total_iterations/write_every) */
-  int32_t solver;            /* enum cmtj_solver (RK4, EULER_HEUN, HEUN)   */
+  uint32_t n_log;            /* fixed step: ceil(total_iterations/write_every);
+                                Dormand-Prince: log capacity in rows         */
+  int32_t solver;            /* enum cmtj_solver                             */
   int32_t calculate_energies;
   int32_t log_width;         /* doubles per log row, cmtj_log_width()       */
   cmtj_constants_t c;
+  double total_time, write_frequency;
+  uint64_t max_attempts;     /* Dormand-Prince: step attempts before CMTJ_STATUS_LIMIT */
 } cmtj_sim_params_t;
 
 /* Log row layout (per junction, per row): for each layer l, either 3
@@ -388,7 +411,11 @@ typedef struct cmtj_f32_params {
                                       STT or SOT, on I / FL / DL / FL2 / DL2      */
 #define CMTJ_FEAT_SCALAR_WAVES 128 /* waves on K, K2, J*, T                      */
 #define CMTJ_FEAT_IEC2 256         /* quadratic (biquadratic) IEC, J2 != 0        */
-#define CMTJ_FEAT_ALL 511
+#define CMTJ_FEAT_OFFAXIS 512      /* an anisotropy axis with more than one
+                                    * non-zero component.  Without it, K2, full
+                                    * demag and scalar waves, anisotropy and
+                                    * demag fold into one diagonal tensor.     */
+#define CMTJ_FEAT_ALL 1023
 
 /* Runs every junction of one partition (all with n_layers layers and the
  * same solver) for up to p->chunk_steps iterations, resuming from d_state

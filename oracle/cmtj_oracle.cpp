@@ -12,12 +12,14 @@
 //   core/junction.hpp:54-72            calculate_tensor_interaction
 //   core/junction.hpp:580-701          calculateHeff and its field terms
 //   core/junction.hpp:716-831          solveLLG (LLG + STT + SOT), stochasticTorque
+//   core/junction.hpp:866-1002         Layer::dormand_prince_step
 //   core/junction.hpp:1017-1041        Layer::rk4_step
 //   core/junction.hpp:1111-1128        thermal field standard deviation
 //   core/junction.hpp:1580-1636        logLayerParams
 //   core/junction.hpp:1668-1815        runners (single/multi layer, Euler-Heun, Heun)
 //   core/junction.hpp:1835-1867        strip / classic magnetoresistance
 //   core/junction.hpp:1948-1981        runSimulation fixed-step loop
+//   core/junction.hpp:1982-2045        runSimulation Dormand-Prince loop
 // keeping the reference's expression order so that deterministic runs are
 // bit-identical to the reference build (checked by tests/test_oracle_pin.py).
 //
@@ -33,6 +35,7 @@
 #include <cstring>
 #include <thread>
 #include <vector>
+#include <algorithm>
 #include <atomic>
 
 #include "../include/cmtj_gpu.h"
@@ -450,6 +453,120 @@ template <typename T> struct JunctionRun {
     row[col++] = (double)t;
   }
 
+  // dormand_prince_step (junction.hpp:866-1002) of layer l: tries a step
+  // of size ts from time t; updates ts to the next step size (accepted or
+  // not) and the layer's PID state.  Returns accepted; nan set when an
+  // accepted m is NaN (the reference throws "NAN magnetisation").
+  bool dp(int l, const T &t, T &ts, const V3<T> &bottom, const V3<T> &top, bool &nan) {
+    cmtj_adaptive_t &ap = layers[l].adaptive;
+    const V3<T> m_t = mag[l];
+    const T c2 = 1.0 / 5.0, c3 = 3.0 / 10.0, c4 = 4.0 / 5.0, c5 = 8.0 / 9.0, c6 = 1.0, c7 = 1.0;
+    Ctx<T> c0 = ctx(l, 0, 0, false), cl = ctx(l, 0, 0, true);
+    const V3<T> k1 = rhs<T>(c0, t, m_t, bottom, top) * ts;
+    const V3<T> k2 = rhs<T>(c0, t + c2 * ts, m_t + k1 * (c2), bottom, top) * ts;
+    const V3<T> k3 = rhs<T>(c0, t + c3 * ts, m_t + k1 * (3.0 / 40.0) + k2 * (9.0 / 40.0), bottom, top) * ts;
+    const V3<T> k4 = rhs<T>(c0, t + c4 * ts, m_t + k1 * (44.0 / 45.0) + k2 * (-56.0 / 15.0) + k3 * (32.0 / 9.0),
+                            bottom, top) * ts;
+    const V3<T> k5 = rhs<T>(c0, t + c5 * ts,
+                            m_t + k1 * (19372.0 / 6561.0) + k2 * (-25360.0 / 2187.0) + k3 * (64448.0 / 6561.0) +
+                                k4 * (-212.0 / 729.0),
+                            bottom, top) * ts;
+    const V3<T> k6 = rhs<T>(c0, t + c6 * ts,
+                            m_t + k1 * (9017.0 / 3168.0) + k2 * (-355.0 / 33.0) + k3 * (46732.0 / 5247.0) +
+                                k4 * (49.0 / 176.0) + k5 * (-5103.0 / 18656.0),
+                            bottom, top) * ts;
+    const V3<T> k7 = rhs<T>(cl, t + c7 * ts,
+                            m_t + k1 * (35.0 / 384.0) + k3 * (500.0 / 1113.0) + k4 * (125.0 / 192.0) +
+                                k5 * (-2187.0 / 6784.0) + k6 * (11.0 / 84.0),
+                            bottom, top) * ts;
+    V3<T> m5 = m_t + k1 * (35.0 / 384.0) + k3 * (500.0 / 1113.0) + k4 * (125.0 / 192.0) + k5 * (-2187.0 / 6784.0) +
+               k6 * (11.0 / 84.0);
+    const V3<T> m4 = m_t + k1 * (5179.0 / 57600.0) + k3 * (7571.0 / 16695.0) + k4 * (393.0 / 640.0) +
+                     k5 * (-92097.0 / 339200.0) + k6 * (187.0 / 2100.0) + k7 * (1.0 / 40.0);
+    const V3<T> err = m5 - m4;
+    const T err_norm = sqrt(sq(err.x) + sq(err.y) + sq(err.z));
+    const T tol = ap.abs_tol + ap.rel_tol * sqrt(sq(m_t.x) + sq(m_t.y) + sq(m_t.z));
+    T ratio = err_norm / tol;
+    if (tol < 1e-15 || std::isnan(ratio) || std::isinf(ratio)) ratio = 10.0;
+    T factor;
+    if (ap.use_pid_control) {
+      const T e_n = log(ratio);
+      ap.integral_error += e_n;
+      factor = exp(ap.kp * e_n + ap.ki * ap.integral_error + ap.kd * (e_n - ap.prev_error_ratio));
+      ap.prev_error_ratio = e_n;
+    } else {
+      factor = ap.safety_factor * pow(1.0 / ratio, 0.2);
+    }
+    if (std::isnan(factor) || std::isinf(factor)) factor = ap.min_factor;
+    factor = std::min(factor, T(ap.max_factor));
+    factor = std::max(factor, T(ap.min_factor));
+    T next = ts * factor;
+    if (std::isnan(next) || std::isinf(next) || next <= 0) next = ts * ap.min_factor;
+    if (ratio <= 1.0) {
+      mag[l] = normalized(m5);
+      if (std::isnan(mag[l].x)) nan = true;
+      ts = next;
+      return true;
+    }
+    ts = next;
+    return false;
+  }
+
+  // runSimulation's Dormand-Prince loop (1982-2045) with runSingleLayerSolver
+  // / runMultiLayerSolver (1668-1707).  Every layer's step sees the step size
+  // the previous layer's step chose (one shared timeStep reference), and t
+  // advances by the step size chosen for the NEXT step, both as in the
+  // reference.  A multi-layer rejection stops with CMTJ_STATUS_DP_STALL
+  // where the reference would continue from hopt = -1 without end.
+  uint32_t run_dp(double *log) {
+    const int n = J.n_layers;
+    const T total = p.total_time, wf = p.write_frequency;
+    T t = 0.0, next_write = 0.0, cur = p.time_step;
+    uint32_t row = 0, status = CMTJ_STATUS_OK;
+    uint64_t attempts = 0;
+    std::vector<V3<T>> copies(n + 2);
+    while (t < total) {
+      if (++attempts > p.max_attempts) { status = CMTJ_STATUS_LIMIT; break; }
+      if (t + cur > total) cur = total - t;
+      int consecutive = 0;
+      if (std::isnan(cur) || std::isinf(cur) || cur <= 0) {
+        cur = p.time_step;
+        consecutive++;
+      }
+      bool accepted, nan = false;
+      if (n > 1) {
+        accepted = true;
+        for (int l = 0; l < n; ++l) copies[l + 1] = mag[l];
+        for (int l = 0; l < n; ++l)
+          if (!dp(l, t, cur, copies[l], copies[l + 2], nan)) accepted = false;
+        if (!accepted) { status = CMTJ_STATUS_DP_STALL; break; }
+      } else {
+        accepted = dp(0, t, cur, V3<T>(), V3<T>(), nan);
+      }
+      if (nan) { status = CMTJ_STATUS_NAN; break; }
+      if (!accepted && (cur < 1e-15 || consecutive >= 10)) {
+        accepted = true;
+        consecutive = 0;
+      }
+      if (accepted) {
+        t += cur;
+        if (t >= next_write) {
+          if (row >= p.n_log) { status = CMTJ_STATUS_LIMIT; break; }
+          log_row(log + (size_t)row * p.log_width, t);
+          ++row;
+          next_write = ((double)(uint32_t)(t / wf) + 1) * wf;
+        }
+      }
+    }
+    rows = row;
+    for (int l = 0; l < n; ++l) {
+      layers[l].mag[0] = (double)mag[l].x;
+      layers[l].mag[1] = (double)mag[l].y;
+      layers[l].mag[2] = (double)mag[l].z;
+    }
+    return status;
+  }
+
   // runSimulation fixed-step loop (1966-1981).
   uint32_t rows = 0;
   uint32_t run(double *log) {
@@ -548,7 +665,8 @@ int oracle_run_simulation(const cmtj_junction_t *junctions, int32_t n_junctions,
       if (j >= n_junctions) break;
       const cmtj_junction_t &J = junctions[j];
       oracle::JunctionRun<double> run(J, layers + J.layer_offset, *p, tables);
-      status[2 * j] = run.run(log + (size_t)j * p->n_log * p->log_width);
+      double *out = log + (size_t)j * p->n_log * p->log_width;
+      status[2 * j] = p->solver == CMTJ_DORMAND_PRINCE ? run.run_dp(out) : run.run(out);
       status[2 * j + 1] = run.rows;
     }
   };

@@ -22,7 +22,7 @@ def _demag(cm, rows):
     return [cm.CVector(*r) for r in rows]
 
 
-def config0_point(cm, hx=-300e3, total=1e-9):
+def mtj_rh_point(cm, hx=-300e3, total=1e-9):
     """One field point of the 2-layer R(H) sweep (free Ms 1.2 T, Ku 3e5 z,
     t 1.5 nm; reference Ms 1.5 T, Ku 1e6 z, t 2 nm; alpha 0.01; demag
     diag(0.0024, 0.0024, 0.9952); surface 1e-16; IEC -5e-5)."""
@@ -237,8 +237,37 @@ def euler_heun_det(cm):
     return tri_layer(cm, solver="EulerHeun")
 
 
+def _dormand_prince(fn, total=None):
+    """Case `fn` run with SolverMode.DormandPrince (junction.hpp:866-1002,
+    1982-2045), optionally over a shorter horizon."""
+    def case(cm):
+        j, runs = fn(cm)
+        out = []
+        for r in runs:
+            r = dict(r)
+            r["solverMode"] = cm.SolverMode.DormandPrince
+            if total is not None:
+                r["totalTime"] = total
+            out.append(r)
+        return j, out
+    case.__doc__ = "%s with the Dormand-Prince solver" % fn.__name__
+    return case
+
+
+# Multi-layer Dormand-Prince runs only while no layer rejects a step (the
+# reference's rejection path for several layers does not terminate), so the
+# multi-layer cases are short.
+DORMAND_PRINCE = {
+    "dp_sto": _dormand_prince(sto),
+    "dp_vsd_sine": _dormand_prince(vsd_sine),
+    "dp_harmonic_hall": _dormand_prince(harmonic_hall),
+    "dp_energies_k2": _dormand_prince(energies_k2),
+    "dp_mtj_rh_point": _dormand_prince(mtj_rh_point, total=2e-11),
+    "dp_tri_layer": _dormand_prince(tri_layer, total=2e-12),
+}
+
 DETERMINISTIC = {
-    "config0_point": config0_point,
+    "mtj_rh_point": mtj_rh_point,
     "sto": sto,
     "sot_strip": sot_strip,
     "tri_layer": tri_layer,
@@ -251,6 +280,7 @@ DETERMINISTIC = {
     "fmr_unnormalised": fmr_unnormalised,
     "heun_det": heun_det,
     "euler_heun_det": euler_heun_det,
+    **DORMAND_PRINCE,
 }
 
 
@@ -360,3 +390,33 @@ def run_stack_case(cm, name):
                 break
             q += 1
     return slog, jlogs
+
+
+def junctions_from_spec(spec, rows, oersted=None):
+    """Junction objects for rows of a sweeps.* spec (constant parts only;
+    `oersted(k)` returns the AxialDriver of row k's time-dependent field)."""
+    import cmtj_gb300 as cm
+    out = []
+    for k in rows:
+        L = int(spec.n_layers[k])
+        layers = []
+        for l in range(L):
+            d = [cm.CVector(*spec.demag[k, l, 3 * r:3 * r + 3]) for r in range(3)]
+            ly = cm.Layer("L%d" % l, cm.CVector(*spec.m0[k, l]), cm.CVector(*spec.anis[k, l]), float(spec.Ms[k, l]),
+                          float(spec.thickness[k, l]), float(spec.surface[k, l]), d, float(spec.alpha[k, l]))
+            ly.setAnisotropyDriver(cm.constantDriver(float(spec.K[k, l])))
+            ly.setExternalFieldDriver(cm.AxialDriver(*[float(x) for x in spec.Hc[k, l]]))
+            if oersted is not None:
+                ly.setOerstedFieldDriver(oersted(k))
+            ly.mag = cm.CVector(*spec.m0[k, l])  # exact start, no renormalisation
+            layers.append(ly)
+        if spec.mr_mode[k] == 1:
+            if L == 1:
+                layers[0].setReferenceLayer(cm.CVector(*spec.ref[k, 0]))
+            j = cm.Junction(layers, float(spec.Rp[k]), float(spec.Rap[k]))
+        else:
+            j = cm.Junction(layers)
+        for l in range(L - 1):
+            j.setIECDriver("L%d" % l, "L%d" % (l + 1), cm.constantDriver(float(spec.Jt[k, l])))
+        out.append(j)
+    return out

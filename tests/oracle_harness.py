@@ -58,8 +58,8 @@ def run_lowered(lowered, threads=1):
 
 def run_oracle(junctions, totalTime, timeStep=1e-13, writeFrequency=1e-11, verbose=False,
                calculateEnergies=False, solverMode=cmtj_gb300.SolverMode.RK4, threads=1):
-    plan = plan_run(totalTime, timeStep, writeFrequency)
     solver = junctions[0].getSolver(solverMode)
+    plan = plan_run(totalTime, timeStep, writeFrequency, solver=solver)
     lowered = lower(junctions, plan, solver, calculateEnergies)
     log, status = run_lowered(lowered, threads)
     apply_results(junctions, lowered, log, status, plan)

@@ -18,7 +18,7 @@ TOL_M_F32 = 1e-4
 # moves it by 2.9e-4 (the other cases: at most 1.5e-5). Reordering its FP64
 # arithmetic moves it by 5e-6, and FP32 (in any formulation) by 5e-4, so no
 # 1e-4 comparison is meaningful for it.
-F32_CASES = ["config0_point", "sto", "sot_strip", "tri_layer", "vsd_sine", "energies_k2", "alt_stt_bottom",
+F32_CASES = ["mtj_rh_point", "sto", "sot_strip", "tri_layer", "vsd_sine", "energies_k2", "alt_stt_bottom",
              "heun_det"]
 
 
@@ -65,7 +65,7 @@ def test_fp32_batch_mixed_layers_alone_equals_in_mix(gpu_lib):
     trajectory is bit-identical alone and inside the mix."""
     js = []
     for k in range(24):
-        name = ["config0_point", "sto", "tri_layer", "vsd_sine"][k % 4]
+        name = ["mtj_rh_point", "sto", "tri_layer", "vsd_sine"][k % 4]
         js.append(cases.DETERMINISTIC[name](cmtj_gb300)[0])
     run, logs = batch.simulate_junctions_f32(js, 3e-10, 1e-13, 1e-12)
     for k in (0, 1, 2, 3, 13):

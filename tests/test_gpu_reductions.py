@@ -12,38 +12,10 @@ import pytest
 
 import cmtj_gb300 as cm
 import oracle_harness
+from cases import junctions_from_spec
 from cmtj_gb300 import _abi, batch, engine, sweeps
 
 DT = 1e-13
-
-
-def junctions_from_spec(spec, rows, oersted=None):
-    """Junction objects for rows of a sweeps.* spec (constant parts only;
-    `oersted(k)` returns the AxialDriver of row k's time-dependent field)."""
-    out = []
-    for k in rows:
-        L = int(spec.n_layers[k])
-        layers = []
-        for l in range(L):
-            d = [cm.CVector(*spec.demag[k, l, 3 * r:3 * r + 3]) for r in range(3)]
-            ly = cm.Layer("L%d" % l, cm.CVector(*spec.m0[k, l]), cm.CVector(*spec.anis[k, l]), float(spec.Ms[k, l]),
-                          float(spec.thickness[k, l]), float(spec.surface[k, l]), d, float(spec.alpha[k, l]))
-            ly.setAnisotropyDriver(cm.constantDriver(float(spec.K[k, l])))
-            ly.setExternalFieldDriver(cm.AxialDriver(*[float(x) for x in spec.Hc[k, l]]))
-            if oersted is not None:
-                ly.setOerstedFieldDriver(oersted(k))
-            ly.mag = cm.CVector(*spec.m0[k, l])  # exact start, no renormalisation
-            layers.append(ly)
-        if spec.mr_mode[k] == 1:
-            if L == 1:
-                layers[0].setReferenceLayer(cm.CVector(*spec.ref[k, 0]))
-            j = cm.Junction(layers, float(spec.Rp[k]), float(spec.Rap[k]))
-        else:
-            j = cm.Junction(layers)
-        for l in range(L - 1):
-            j.setIECDriver("L%d" % l, "L%d" % (l + 1), cm.constantDriver(float(spec.Jt[k, l])))
-        out.append(j)
-    return out
 
 
 @pytest.mark.gpu

@@ -34,7 +34,7 @@ def test_oracle_matches_reference_bitwise(name):
 def test_log_length_law():
     """len(time) = ceil(T/dt / writeEvery) (tests/test_layer.cpp:42-47 in
     the reference asserts T/dt rows at writeEvery 1)."""
-    j, _ = cases.config0_point(oracle_harness.oracle_module())
+    j, _ = cases.mtj_rh_point(oracle_harness.oracle_module())
     j.runSimulation(1e-10, 1e-13, 1e-13)
     assert len(j.getLog()["time"]) == int(1e-10 / 1e-13)
     assert j.getLog()["time"][:3] == [0.0, 1e-13, 2e-13]

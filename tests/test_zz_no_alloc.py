@@ -24,7 +24,7 @@ TOL_M_F32 = 1e-4
 def _mixed_batch():
     js = []
     for k in range(40):
-        name = ["config0_point", "sto", "tri_layer", "vsd_sine", "sot_strip"][k % 5]
+        name = ["mtj_rh_point", "sto", "tri_layer", "vsd_sine", "sot_strip"][k % 5]
         js.append(cases.DETERMINISTIC[name](cmtj_gb300)[0])
     spec = batch.BatchSpec.from_junctions(js)
     low = batch.lower(spec, 1e-13, 2000)
