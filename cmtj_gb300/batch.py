@@ -58,15 +58,17 @@ F32_JUNCTION_DTYPE = np.dtype(
      ("win_start", "<u4"), ("log_offset", "<u4"), ("Rp", "<f4"), ("Rap", "<f4"),
      ("Rx0", "<f4", 4), ("Ry0", "<f4", 4), ("AMR_X", "<f4", 4), ("AMR_Y", "<f4", 4), ("SMR_X", "<f4", 4),
      ("SMR_Y", "<f4", 4), ("AHE", "<f4", 4), ("mix_w", "<f4", 4), ("vsd_ph0", "<u8"), ("vsd_dph", "<u8"),
-     ("n_waves", "<i4"), ("reserved", "<i4"), ("waves", WAVE_DTYPE, MAX_WAVES)], align=True)
+     ("n_waves", "<i4"), ("red_total", "<u4"), ("waves", WAVE_DTYPE, MAX_WAVES)], align=True)
 
 F32_STATE_DTYPE = np.dtype(
     [("m", "<f4", (4, 3)), ("step", "<u4"), ("status", "<u4"), ("n_logged", "<u4"), ("n_red", "<u4"),
-     ("r_sum", "<f4"), ("r_c", "<f4"), ("v_sum", "<f4"), ("v_c", "<f4")], align=True)
+     ("r_sum", "<f4"), ("r_c", "<f4"), ("v_sum", "<f4"), ("v_c", "<f4"), ("vw_sum", "<f4"), ("vw_c", "<f4")],
+    align=True)
 
 F32_PARAMS_DTYPE = np.dtype(
     [("dt", "<f8"), ("chunk_steps", "<u4"), ("solver", "<i4"), ("log_mode", "<i4"), ("log_axis", "<i4"),
-     ("log_every", "<u4"), ("log_tile", "<u4"), ("red_every", "<u4"), ("reserved", "<i4")], align=True)
+     ("log_every", "<u4"), ("log_tile", "<u4"), ("red_every", "<u4"), ("reserved", "<i4"),
+     ("red_weights", "<u8")], align=True)
 
 STRUCT_SIZES_F32 = {
     "cmtj_wave_t": WAVE_DTYPE.itemsize, "cmtj_f32_layer_t": F32_LAYER_DTYPE.itemsize,
@@ -548,7 +550,7 @@ class BatchRun:
     `fetch()` to read results back."""
 
     def __init__(self, lowered, time_step, solver=SolverMode.RK4, log_mode=LOG_NONE, log_every=0, log_axis=0,
-                 red_every=0, device="cuda"):
+                 red_every=0, red_weights=None, device="cuda"):
         from . import engine
         t = engine.torch()
         engine.require_gpu()
@@ -611,6 +613,20 @@ class BatchRun:
         self.params["log_axis"] = log_axis
         self.params["log_every"] = self.log_every
         self.params["red_every"] = red_every
+        self.d_w = None
+        if red_weights is not None:
+            # weighted I*R sum: sample k of N gets red_weights[N-1-k]
+            if not red_every:
+                raise ValueError("red_weights need red_every >= 1")
+            total = reduction_samples(lowered.n_steps, lowered.junctions["win_start"].astype(np.int64),
+                                      int(red_every))
+            w = np.ascontiguousarray(red_weights, dtype=np.float32).ravel()
+            if total.max(initial=0) > w.size:
+                raise ValueError("red_weights holds %d values; a junction takes %d samples" % (w.size, total.max()))
+            lowered.junctions["red_total"] = total.astype(np.uint32)
+            self.d_j = engine.to_device(lowered.junctions)
+            self.d_w = t.from_numpy(w.copy()).to(device)
+            self.params["red_weights"] = self.d_w.data_ptr()
 
     def variants(self):
         """[(n_layers, variant code, junction count)] of the partitions."""
@@ -643,6 +659,25 @@ class BatchRun:
         s, c = int(self.samples[k]), int(self.log_chans[k])
         a = log[self.log_starts[k]: self.log_starts[k] + self.log_pad[k] * c].reshape(-1, c)
         return a[:s]
+
+
+def reduction_samples(n_steps, win_start, red_every):
+    """Samples each junction's on-device reductions take: steps s in
+    [win_start, n_steps) with (s - win_start) % red_every == 0."""
+    n_steps = np.asarray(n_steps, dtype=np.int64)
+    win = np.broadcast_to(np.asarray(win_start, dtype=np.int64), n_steps.shape)
+    return np.where(n_steps > win, (n_steps - 1 - win) // red_every + 1, 0)
+
+
+def lowpass_step_response(n, fs, cutoff=10e6, order=3):
+    """Step response s[0..n-1] of the digital Butterworth low-pass that
+    cmtj/utils/filters.py:33-43 applies (scipy.signal.butter(order,
+    cutoff / (fs/2)) run through lfilter from rest).  For x_0..x_{N-1},
+    mean(lfilter(b, a, x)) = sum_k s[N-1-k] x_k / N, so these are the
+    red_weights of the filtered spin-diode mean."""
+    from scipy.signal import butter, lfilter
+    b, a = butter(order, cutoff / (0.5 * fs), btype="low", analog=False)
+    return lfilter(b, a, np.ones(int(n)))
 
 
 def simulate_junctions_f32(junctions, totalTime, timeStep=1e-13, writeFrequency=1e-11,

@@ -76,7 +76,9 @@ extern "C" int cmtj_batch_run_f32(const cmtj_f32_junction_t *d_junctions, const 
     return CMTJ_ERR_ARG;
   }
   const int threads = 128;
-  const size_t smem = (size_t)threads * (channels > 0 ? p->log_tile * channels : 1) * sizeof(float);
+  // per thread: its log tile, then (weighted reduction) a compensated sum pair
+  const size_t smem =
+      (size_t)threads * ((channels > 0 ? p->log_tile * channels : 1) + (p->red_weights ? 2 : 0)) * sizeof(float);
   int blocks = grid_blocks;
   if (blocks <= 0) {
     int dev = 0, sms = 0, per_sm = 0;

@@ -544,13 +544,26 @@ template <int L> __device__ __forceinline__ int log_channels(int mode) {
 }
 
 // Resident CTAs of 128 threads per SM the specialised variants are built
-// for (register cap); the catch-all CMTJ_FEAT_ALL variants take what they need.
+// for (register cap); the catch-all CMTJ_FEAT_ALL variants take what they
+// need.  The packed two-layer RK4 variants have their own bound.
 #ifndef CMTJ_BATCH_MINB
 #define CMTJ_BATCH_MINB 5
 #endif
+#ifndef CMTJ_BATCH_MINB_PACKED
+#define CMTJ_BATCH_MINB_PACKED CMTJ_BATCH_MINB
+#endif
+
+template <int L, int SOLVER, int FEAT>
+__host__ __device__ constexpr bool packed_variant() {
+  return L == 2 && SOLVER == CMTJ_RK4 && (FEAT & ~CMTJ_FEAT_WAVES) == 0;
+}
+template <int L, int SOLVER, int FEAT>
+__host__ __device__ constexpr int min_blocks() {
+  return FEAT == CMTJ_FEAT_ALL ? 1 : (packed_variant<L, SOLVER, FEAT>() ? CMTJ_BATCH_MINB_PACKED : CMTJ_BATCH_MINB);
+}
 
 template <int L, int SOLVER, int FEAT, int NW>
-__global__ void __launch_bounds__(128, (FEAT == CMTJ_FEAT_ALL) ? 1 : CMTJ_BATCH_MINB) k_batch(Args A) {
+__global__ void __launch_bounds__(128, (min_blocks<L, SOLVER, FEAT>())) k_batch(Args A) {
   using F = Feat<FEAT>;
   extern __shared__ __align__(16) float smem[];
   const int lane = threadIdx.x & 31;
@@ -559,11 +572,15 @@ __global__ void __launch_bounds__(128, (FEAT == CMTJ_FEAT_ALL) ? 1 : CMTJ_BATCH_
   const float sqdt = (float)sqrt(p.dt);
   const int C = log_channels<L>(p.log_mode);
   const uint32_t T = p.log_tile;
-  float *tile = smem + (size_t)threadIdx.x * T * (C > 0 ? C : 1);
+  // shared memory per thread: its log tile; after all tiles, when
+  // p.red_weights is set, the (sum, compensation) pair of the weighted sum
+  const uint32_t tile_floats = C > 0 ? T * (uint32_t)C : 1u;
+  float *tile = smem + (size_t)threadIdx.x * tile_floats;
+  float *wsum = smem + (size_t)blockDim.x * tile_floats + 2u * threadIdx.x;
 
   // Packed two-layer RK4 for the variants with only constant / wave fields,
   // uniaxial anisotropy, diagonal demag and bilinear IEC.
-  constexpr bool kPacked = L == 2 && SOLVER == CMTJ_RK4 && (FEAT & ~CMTJ_FEAT_WAVES) == 0;
+  constexpr bool kPacked = packed_variant<L, SOLVER, FEAT>();
   static_assert(!kPacked || Feat<FEAT>::prescale, "the packed path reads pre-scaled fields");
 
   // junction-lifetime registers
@@ -639,6 +656,10 @@ __global__ void __launch_bounds__(128, (FEAT == CMTJ_FEAT_ALL) ? 1 : CMTJ_BATCH_
             rc = S.r_c;
             vs = S.v_sum;
             vc = S.v_c;
+            if (p.red_weights) {
+              wsum[0] = S.vw_sum;
+              wsum[1] = S.vw_c;
+            }
             win = J.win_start;
             Jp = &J;
             ref0 = A.Ly[J.layer_offset].ref;
@@ -804,6 +825,14 @@ __global__ void __launch_bounds__(128, (FEAT == CMTJ_FEAT_ALL) ? 1 : CMTJ_BATCH_
           const uint64_t ph = Jp->vsd_ph0 + (uint64_t)last * vdph;
           const float I = sinpif(2.0f * ((float)(uint32_t)(ph >> 40) * 5.9604644775390625e-08f));
           kadd(vs, vc, I * R);
+          if (p.red_weights) {
+            const uint32_t tot = Jp->red_total;
+            const float w = __ldg(p.red_weights + (tot > n_red ? tot - 1u - n_red : 0u));
+            float ws = wsum[0], wc = wsum[1];
+            kadd(ws, wc, w * (I * R));
+            wsum[0] = ws;
+            wsum[1] = wc;
+          }
         }
         ++n_red;
       }
@@ -862,6 +891,10 @@ __global__ void __launch_bounds__(128, (FEAT == CMTJ_FEAT_ALL) ? 1 : CMTJ_BATCH_
       S.r_c = rc;
       S.v_sum = vs;
       S.v_c = vc;
+      if (p.red_weights) {
+        S.vw_sum = wsum[0];
+        S.vw_c = wsum[1];
+      }
       jid = -1;
     }
   }

@@ -363,7 +363,8 @@ typedef struct cmtj_f32_junction {
   float mix_w[CMTJ_MAX_LAYERS_F32]; /* weights of the mixed log channel        */
   uint64_t vsd_ph0, vsd_dph;        /* I(t) = sin(2 pi (vsd_ph0 + i vsd_dph))  */
   int32_t n_waves;
-  int32_t reserved;
+  uint32_t red_total;     /* reduction samples the whole run takes: sample k
+                             of the weighted sum gets red_weights[red_total-1-k] */
   cmtj_wave_t waves[CMTJ_MAX_WAVES];
 } cmtj_f32_junction_t;
 
@@ -376,6 +377,7 @@ typedef struct cmtj_f32_state {
   uint32_t n_red;         /* samples in the reductions                         */
   float r_sum, r_c;       /* compensated (Neumaier) sum of R                   */
   float v_sum, v_c;       /* compensated sum of I(t) * R(t)                    */
+  float vw_sum, vw_c;     /* compensated sum of w_k I R (params.red_weights)   */
 } cmtj_f32_state_t;
 
 /* What the kernel logs every log_every steps (from step 0, like the
@@ -396,6 +398,11 @@ typedef struct cmtj_f32_params {
   uint32_t log_tile;      /* samples staged per thread before a bulk store     */
   uint32_t red_every;     /* reduction cadence in steps (0: none)              */
   int32_t reserved;
+  /* Optional (null: off) weights of a second I(t) R(t) sum.  With w the step
+   * response of a causal linear filter started at rest, sum_k w[N-1-k] x_k
+   * / N is the mean of the filtered x: the Butterworth low-pass mean of
+   * cmtj/utils/resistance.py:12-22 (compute_sd) without a per-step filter. */
+  const float *red_weights;
 } cmtj_f32_params_t;
 
 /* Kernel variant of a batch partition: n_layers (1-4), solver, and the

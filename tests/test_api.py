@@ -4,6 +4,8 @@ test_imports.py in the reference suite): construction, driver arithmetic,
 error types and messages.  No simulation runs here."""
 import math
 
+import numpy as np
+
 import pytest
 
 import cmtj_gb300 as cmtj
@@ -216,3 +218,28 @@ def test_stack_validation():
         s.setCouplingStrength([0.1, 0.2])
     with pytest.raises(RuntimeError, match="only supported for 2 layer stacks"):
         s.setDelayed(False)
+
+
+def test_lowpass_weights_reproduce_filtered_mean():
+    """mean(lfilter(b, a, x)) = sum_k s[N-1-k] x_k / N for the step response
+    s of the Butterworth low-pass used by compute_sd (resistance.py:12-22)."""
+    from scipy.signal import butter, lfilter
+    from cmtj_gb300 import batch
+    rng = np.random.default_rng(3)
+    n, dt = 4000, 1e-13
+    x = rng.standard_normal(n) + 0.3 * np.sin(np.arange(n) * 0.01)
+    s = batch.lowpass_step_response(n, 1.0 / dt)
+    b, a = butter(3, 10e6 / (0.5 / dt), btype="low", analog=False)
+    want = np.mean(lfilter(b, a, x))
+    got = np.dot(s[::-1], x) / n
+    assert abs(got - want) <= 1e-12 * max(1.0, abs(want)) + 1e-18
+
+
+def test_reduction_sample_counts():
+    from cmtj_gb300 import batch
+    n_steps = np.array([0, 1, 10, 11, 100])
+    win = np.array([0, 0, 3, 11, 5])
+    for every in (1, 3, 7):
+        got = batch.reduction_samples(n_steps, win, every)
+        want = [len(range(w, n, every)) if n > w else 0 for n, w in zip(n_steps, win)]
+        assert got.tolist() == want

@@ -4,6 +4,8 @@
   without the low-pass) accumulated in the FP32 batch kernel with
   compensated sums, on uneven 1-4 layer junctions of the spin-diode sweep,
   against the mean over the oracle's FP64 trajectory;
+* the low-passed form of resistance.py:12-22 (compute_sd) as a weighted
+  on-device sum, against compute_sd on the oracle's FP64 trajectory;
 * the PIMM spectrum (procedures.py:28-39): cmtj_spectrum_f32 on the FP32 log
   against numpy's FFT of the same log (the FFT itself) and of the FP64
   trajectory (end to end)."""
@@ -48,6 +50,52 @@ def test_vsd_mixing_voltage_matches_fp64(gpu_lib):
         I = np.sin(2 * np.pi * spec.vsd_freq[k] * t)
         v64 = float(np.mean(I * R))
         assert abs(v32[k] - v64) <= 1e-4 * scale, (k, L, v32[k], v64)
+
+
+def compute_sd_f64(R, I, dt):
+    """The reference's filtered spin-diode voltage on an FP64 trajectory
+    (cmtj/utils/resistance.py:12-22 with filters.py:33-43): mean of the
+    3rd-order 10 MHz Butterworth low-pass of -I R."""
+    from scipy.signal import butter, lfilter
+    b, a = butter(3, 10e6 / (0.5 / dt), btype="low", analog=False)
+    return float(np.mean(lfilter(b, a, -I * R)))
+
+
+@pytest.mark.gpu
+def test_vsd_filtered_voltage_matches_compute_sd(gpu_lib):
+    """The weighted on-device sum (weights = the filter's step response)
+    against compute_sd run on the oracle's FP64 trajectory."""
+    spec, _ = sweeps.vsd_config(n_f=4, n_h=6, seed=13, dt=DT, amp=5e3)
+    batch.relax(spec, DT, 20000, alpha=1.0)
+    n_steps = 30000
+    low = batch.lower(spec, DT, n_steps)
+    w = batch.lowpass_step_response(n_steps, 1.0 / DT)
+    run = batch.BatchRun(low, DT, cm.SolverMode.RK4, batch.LOG_NONE, 0, red_every=1, red_weights=w)
+    run.launch()
+    st = run.state()
+    assert np.all(st["status"] == 0) and np.all(st["n_red"] == n_steps)
+    v32 = -(st["vw_sum"].astype(np.float64) + st["vw_c"]) / n_steps
+    plain32 = (st["v_sum"].astype(np.float64) + st["v_c"]) / n_steps
+    rows = list(range(spec.n))
+    js = junctions_from_spec(spec, rows, lambda k: cm.AxialDriver(cm.NullDriver(),
+                                                                     cm.sineDriver(0, 5e3, float(spec.vsd_freq[k]), 0),
+                                                                     cm.NullDriver()))
+    oracle_harness.run_oracle(js, n_steps * DT, DT, DT, threads=8)
+    for q, k in enumerate(rows):
+        lg = js[q].getLogArrays()
+        L = int(spec.n_layers[k])
+        if spec.mr_mode[k] == 1:
+            R = lg["R"] if L == 1 else lg["R_L0_L1"]
+            scale = spec.Rap[k] - spec.Rp[k]
+        else:
+            R = sum(spec.strip[k, 0, l] + spec.strip[k, 2, l] * lg["L%d_mx" % l] ** 2 +
+                    spec.strip[k, 4, l] * lg["L%d_my" % l] ** 2 for l in range(L))
+            scale = sum(abs(spec.strip[k, 2, l]) + abs(spec.strip[k, 4, l]) for l in range(L))
+        I = np.sin(2 * np.pi * spec.vsd_freq[k] * lg["time"])
+        v64 = compute_sd_f64(R, I, DT)
+        assert abs(v32[k] - v64) <= 1e-4 * scale, (k, L, v32[k], v64)
+        # the filter removes part of the plain mean: the two differ
+        assert np.isfinite(plain32[k])
 
 
 @pytest.mark.gpu
