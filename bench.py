@@ -446,7 +446,78 @@ def measure_rest(run, low, spec, n_steps, kern_ms, fft_ms, lib):
     out["accuracy"] = {"max_abs_dm_final_vs_fp64": dm_final, "max_abs_dmix_logged_vs_fp64": dmix,
                        "tolerance": 1e-4, "sample_junctions": 256, "pass": max(dm_final, dmix) <= 1e-4}
     out["serving"] = serving_leg(fp64_batch)
+    out["other_workloads"] = other_workloads()
     out["cpu_baseline"] = cpu_baseline()
+    return out
+
+
+def _timed_run(run):
+    """One full launch of a BatchRun timed with CUDA events on its stream."""
+    import torch
+    torch.cuda.synchronize()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record()
+    run.launch()
+    b.record()
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / 1e3
+
+
+def other_workloads():
+    """The remaining sweep families at full size, each one timed launch:
+    the stochastic p-bit sweep (64 currents x 16,384 single-layer STT
+    junctions, Euler-Heun at 300 K, 5-20 ns each), the uneven spin-diode
+    sweep (128 frequencies x 1024 fields, 1-4 layers, 5-50 ns, plain and
+    Butterworth-filtered <I R> on the device), and a 16-junction series
+    stack in the FP64 form (2000 steps)."""
+    import torch
+    import cmtj_gb300 as cm
+    import cases
+    from cmtj_gb300 import batch, stack, sweeps
+    out = {}
+    # p-bit
+    spec, n_steps, jd = sweeps.pbit_config(dt=DT)
+    low = batch.lower(spec, DT, n_steps)
+    run = batch.BatchRun(low, DT, batch.SolverMode.EulerHeun, batch.LOG_NONE, 0)
+    el = _timed_run(run)
+    st = run.state()
+    mz = st["m"][:, 0, 2]
+    cur = np.unique(jd)
+    p_sw = [float(np.mean(mz[jd == c] < 0)) for c in cur]
+    norm = np.linalg.norm(st["m"][:, 0, :].astype(np.float64), axis=1)
+    out["pbit_1M"] = {"layer_steps_per_s": float(n_steps.sum()) / el, "seconds": el, "junctions": spec.n,
+                      "layer_steps": float(n_steps.sum()), "all_ok": bool(np.all(st["status"] == 0)),
+                      "p_switch_first_last": [p_sw[0], p_sw[-1]], "max_norm_drift": float(np.max(np.abs(norm - 1)))}
+    del run, low, spec
+    torch.cuda.empty_cache()
+    # uneven spin-diode sweep with both voltage forms
+    spec, n_steps = sweeps.vsd_config(dt=DT)
+    low = batch.lower(spec, DT, n_steps)
+    w = batch.lowpass_step_response(int(n_steps.max()), 1.0 / DT)
+    run = batch.BatchRun(low, DT, batch.SolverMode.RK4, batch.LOG_NONE, 0, red_every=1, red_weights=w)
+    el = _timed_run(run)
+    st = run.state()
+    ls = float((n_steps * spec.n_layers).sum())
+    out["vsd_uneven_131k"] = {"layer_steps_per_s": ls / el, "seconds": el, "junctions": spec.n, "layer_steps": ls,
+                              "all_ok": bool(np.all(st["status"] == 0)),
+                              "variants": [[int(a), int(b), int(c)] for a, b, c in run.variants()],
+                              "reductions": "plain and Butterworth-weighted <I R>, every step"}
+    del run, low, spec
+    torch.cuda.empty_cache()
+    # 16-junction series stack, FP64 plain form
+    js = [cases._stt_junction(cm, 1.0 + 0.02 * k, 1e3 + 50 * k, (0.1, 0.2, 1), (1, 0, 0)) for k in range(16)]
+    s = cm.stack.SeriesStack(js)
+    s.setCouplingStrength(0.3)
+    s.setCoupledCurrentDriver(cm.constantDriver(5e10))
+    steps = 2000
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    s.runSimulation(steps * DT, DT, DT * 10)
+    torch.cuda.synchronize()
+    el = time.perf_counter() - t0
+    out["series_stack_16_fp64"] = {"layer_steps_per_s": 16 * steps / el, "seconds": el,
+                                   "sample": "16 STT junctions x %d steps, KCL, one CTA" % steps}
     return out
 
 

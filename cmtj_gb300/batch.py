@@ -586,7 +586,9 @@ class BatchRun:
         st = np.zeros(self.n, dtype=F32_STATE_DTYPE)
         self.d_s = engine.to_device(st)
         self.d_log = t.zeros(max(total_floats, 4), dtype=t.float32, device=device)
-        self.d_ticket = t.zeros(4, dtype=t.int32, device=device)
+        # one work ticket per partition, 64 B apart: partitions run concurrently
+        self.d_ticket = t.zeros(16 * 5 * 16, dtype=t.int32, device=device)
+        self._streams = None
         # Partitions: one per (layer count, kernel variant).  The variant is
         # chosen from each junction's own features, never from its batch
         # partners, so a junction runs the same code (and gives the same
@@ -635,20 +637,47 @@ class BatchRun:
     def launch(self, chunk_steps=None, stream=None, grid_blocks=0):
         """Advance every junction by up to chunk_steps iterations (all of
         them when None).  A chunk must hold whole log tiles so that resumed
-        logs stay 16-byte aligned."""
+        logs stay 16-byte aligned.  Partitions (layer count x kernel
+        variant) run concurrently, each on its own stream with its own work
+        ticket, so a small partition's long junctions overlap the others
+        instead of adding their tail; `stream` waits for all of them."""
         from . import engine
+        t = engine.torch()
         p = self.params
         p["chunk_steps"] = 2 ** 32 - 1 if chunk_steps is None else int(chunk_steps)
-        for nl, d_order, cnt, code in self.parts:
-            p["log_tile"] = default_tile(log_channels(self.log_mode, nl))
-            if chunk_steps is not None and self.log_mode != LOG_NONE:
-                if int(chunk_steps) % (self.log_every * int(p["log_tile"][0])):
-                    raise ValueError("chunk_steps must be a multiple of log_every * %d" % int(p["log_tile"][0]))
+        if chunk_steps is not None and self.log_mode != LOG_NONE:
+            for nl, _, _, _ in self.parts:
+                tile = default_tile(log_channels(self.log_mode, nl))
+                if int(chunk_steps) % (self.log_every * tile):
+                    raise ValueError("chunk_steps must be a multiple of log_every * %d" % tile)
+        if len(self.parts) > 80:
+            raise ValueError("more than 80 partitions in one batch")
+        main = stream if stream is not None else t.cuda.current_stream()
+        multi = len(self.parts) > 1
+        if multi and self._streams is None:
+            self._streams = [t.cuda.Stream() for _ in range(min(len(self.parts), 8))]
+        start = t.cuda.Event()
+        if multi:
+            start.record(main)
+        ends = []
+        for q, (nl, d_order, cnt, code) in enumerate(self.parts):
+            s = self._streams[q % len(self._streams)] if multi else main
+            if multi:
+                s.wait_event(start)
+            pq = p.copy()  # the library copies params at launch; one record per partition
+            pq["log_tile"] = default_tile(log_channels(self.log_mode, nl))
+            ticket = self.d_ticket[16 * q:]
             rc = self.lib.cmtj_batch_run_f32(engine.ptr(self.d_j), engine.ptr(self.d_l), engine.ptr(self.d_s),
-                                             engine.ptr(d_order), cnt, nl, code, p.ctypes.data,
-                                             engine.ptr(self.d_log), engine.ptr(self.d_ticket), grid_blocks,
-                                             engine.stream_ptr(stream))
+                                             engine.ptr(d_order), cnt, nl, code, pq.ctypes.data,
+                                             engine.ptr(self.d_log), engine.ptr(ticket), grid_blocks,
+                                             engine.stream_ptr(s))
             _abi.check(rc, self.lib)
+            if multi:
+                e = t.cuda.Event()
+                e.record(s)
+                ends.append(e)
+        for e in ends:
+            main.wait_event(e)
 
     def state(self):
         return self.d_s.cpu().numpy().view(F32_STATE_DTYPE)

@@ -238,6 +238,14 @@ template <int L> struct WaveR {
     off2 = w.off[2];
   }
 
+  // True when the waveform is 0 at every stage of steps [i0_, i1_): a step
+  // driver whose stage windows [on_s, off_s] all miss that range.
+  __device__ __forceinline__ bool off_during(uint32_t i0_, uint32_t i1_) const {
+    if (kind != CMTJ_WAVE_STEP || i1_ <= i0_) return false;
+    const uint32_t lo = min(on0, min(on1, on2)), hi = max(off0, max(off1, off2));
+    return i1_ - 1u < lo || i0_ > hi;
+  }
+
   // Unit waveform at step i, stage s (0: t, 1: t + dt/2, 2: t + dt).
   __device__ __forceinline__ float unit(uint32_t i, int s, float dtf) const {
     switch (kind) {
@@ -492,6 +500,33 @@ __device__ __forceinline__ V2 rhs2(const PairP &Q, V2 m, V2 H) {
   return v2fma(v2cross(m, mxH), Q.alpha, mxH);
 }
 
+// One packed RK4 step of a 2-layer junction (the scalar RK4 of k_batch,
+// lane by lane).  WAVES: evaluate the waves at the three stage times;
+// otherwise the field base is time-independent and formed once.
+template <bool WAVES, int NW>
+__device__ __forceinline__ void packed_rk4_step(V2 &mp, const PairP &Q, const WaveR<2> *W, const V2 *HD, int nw,
+                                                uint32_t step, float dtf) {
+  const V2 nb = swap2(mp);  // frozen neighbours: layer 0 sees layer 1, layer 1 sees layer 0
+  V2 hb = v2fma(nb, Q.jn, Q.h0), acc, kp;
+#pragma unroll
+  for (int st = 0; st < 4; ++st) {
+    const int s = st == 0 ? 0 : (st == 3 ? 2 : 1);
+    if (WAVES && st != 2) {
+      hb = Q.h0;
+#pragma unroll
+      for (int w = 0; w < NW; ++w)
+        if (w < nw) hb = v2fma(HD[w], bc2(W[w].unit(step, s, dtf)), hb);
+      hb = v2fma(nb, Q.jn, hb);
+    }
+    const V2 ms = st == 0 ? mp : v2fma(kp, bc2(st == 3 ? 6.f : 3.f), mp);
+    kp = rhs2(Q, ms, hb);
+    if (st == 0) acc = kp;
+    else if (st == 3) acc = v2add(acc, kp);
+    else acc = v2fma(kp, bc2(2.f), acc);
+  }
+  mp = v2renorm(v2add(mp, acc));
+}
+
 struct Args {
   const cmtj_f32_junction_t *J;
   const cmtj_f32_layer_t *Ly;
@@ -685,31 +720,21 @@ __global__ void __launch_bounds__(128, (min_blocks<L, SOLVER, FEAT>())) k_batch(
     while (step < burst_end) {
       const uint32_t next_ev = next_log < next_red ? next_log : next_red;
       const uint32_t stop = (next_ev < burst_end) ? next_ev + 1 : burst_end;
+      // When every wave is a step driver whose on-windows miss this whole
+      // burst, u = 0 at every stage and the waves are skipped: adding
+      // amp * 0 would leave every term's bits unchanged.
+      bool quiet = true;
+#pragma unroll
+      for (int w = 0; w < NW; ++w)
+        if (w < nw) quiet = quiet && W[w].off_during(step, stop);
       if constexpr (kPacked) {
-        // RK4 on both layers at once (the scalar RK4 below, lane by lane)
+        // RK4 on both layers at once (the scalar RK4 below, lane by lane);
+        // a quiet burst forms the field base once per step.
         V2 mp = pack2(m[0], m[1]);
-        for (; step < stop; ++step) {
-          const V2 nb = swap2(mp);  // frozen neighbours: layer 0 sees layer 1, layer 1 sees layer 0
-          V2 hb, acc, kp;
-#pragma unroll
-          for (int st = 0; st < 4; ++st) {
-            const int s = st == 0 ? 0 : (st == 3 ? 2 : 1);
-            if ((F::waves && st != 2) || (!F::waves && st == 0)) {
-              hb = Q.h0;
-              if (F::waves) {
-#pragma unroll
-                for (int w = 0; w < NW; ++w)
-                  if (w < nw) hb = v2fma(HD[w], bc2(W[w].unit(step, s, dtf)), hb);
-              }
-              hb = v2fma(nb, Q.jn, hb);
-            }
-            const V2 ms = st == 0 ? mp : v2fma(kp, bc2(st == 3 ? 6.f : 3.f), mp);
-            kp = rhs2(Q, ms, hb);
-            if (st == 0) acc = kp;
-            else if (st == 3) acc = v2add(acc, kp);
-            else acc = v2fma(kp, bc2(2.f), acc);
-          }
-          mp = v2renorm(v2add(mp, acc));
+        if (quiet) {
+          for (; step < stop; ++step) packed_rk4_step<false, NW>(mp, Q, W, HD, nw, step, dtf);
+        } else {
+          for (; step < stop; ++step) packed_rk4_step<F::waves, NW>(mp, Q, W, HD, nw, step, dtf);
         }
         m[0] = lane0(mp);
         m[1] = lane1(mp);
@@ -725,7 +750,7 @@ __global__ void __launch_bounds__(128, (min_blocks<L, SOLVER, FEAT>())) k_batch(
           if ((F::waves && st != 2) || (!F::waves && st == 0)) {
 #pragma unroll
             for (int l = 0; l < L; ++l) d[l].clear(P[l].h0);
-            if (F::waves) {
+            if (F::waves && !quiet) {
 #pragma unroll
               for (int w = 0; w < NW; ++w)
                 if (w < nw) add_wave<L, FEAT>(W[w], step, s, dtf, d);
@@ -759,7 +784,7 @@ __global__ void __launch_bounds__(128, (min_blocks<L, SOLVER, FEAT>())) k_batch(
         Delta<FEAT> d[L];
 #pragma unroll
         for (int l = 0; l < L; ++l) d[l].clear(P[l].h0);
-        if (F::waves) {
+        if (F::waves && !quiet) {
 #pragma unroll
           for (int w = 0; w < NW; ++w)
             if (w < nw) add_wave<L, FEAT>(W[w], step, 0, dtf, d);
@@ -793,7 +818,7 @@ __global__ void __launch_bounds__(128, (min_blocks<L, SOLVER, FEAT>())) k_batch(
         } else {
 #pragma unroll
           for (int l = 0; l < L; ++l) mn[l] = m[l] + fma3(g[l], sqdt, f[l]);
-          if (F::waves) {
+          if (F::waves && !quiet) {
 #pragma unroll
             for (int l = 0; l < L; ++l) d[l].clear(P[l].h0);
 #pragma unroll
