@@ -45,21 +45,34 @@ WORKLOAD = ("batched FP32 PIMM: 262144 2-layer MTJs (512 H x 512 seeded Ku/J dra
             "4096-pt device FFT")
 
 
-def fp32_flops_per_layer_step(n_layers=2, waves_per_junction=1):
+def fp32_flops_per_layer_step(n_layers=2, waves_per_junction=1, quiet_fraction=0.0):
     """FP32 operations per layer-step of the batched RK4 integrator for the
     PIMM junction (FMA = 2, rsqrt = 1), counted from its formulation.  The
     field terms are stored pre-multiplied by gamma dt/6, and the anisotropy
     (axis along z) and the diagonal demag fold into one diagonal tensor M.
-    Per stage time (3 per step: t, t + dt/2, t + dt) and layer: base field
-    h0 + wave 6 per wave, + IEC neighbour 6 per neighbour.  Per RHS (4 per
-    step) and layer: M m 6, m x H 9, m x (m x H) 9, alpha FMA 6.  Per
-    layer-step: stage states 18, RK4 accumulation 15, m + increment 3,
-    renormalisation 9."""
+    Per RHS (4 per step) and layer: M m 6, m x H 9, m x (m x H) 9, alpha
+    FMA 6.  Per layer-step: stage states 18, RK4 accumulation 15,
+    m + increment 3, renormalisation 9.  Field base per layer: while a
+    step driver is on, h0 + wave 6 per wave and IEC neighbour 6 per
+    neighbour at 3 stage times; in quiet bursts (driver off for the whole
+    burst) only the IEC term, once per step.  `quiet_fraction` is the share
+    of steps run in quiet bursts."""
     nb = 2.0 * (n_layers - 1) / n_layers
-    waves_per_layer = float(waves_per_junction)
-    stage_fields = 3 * (6 * waves_per_layer + 6 * nb)
-    rhs = 6 + 9 + 9 + 6
-    return stage_fields + 4 * rhs + 18 + 15 + 3 + 9
+    rk4 = 4 * (6 + 9 + 9 + 6) + 18 + 15 + 3 + 9
+    loud = rk4 + 3 * (6 * float(waves_per_junction) + 6 * nb)
+    quiet = rk4 + 6 * nb
+    return quiet_fraction * quiet + (1.0 - quiet_fraction) * loud
+
+
+def pimm_quiet_fraction(n_steps):
+    """Share of the PIMM run's steps in quiet bursts: bursts end at every
+    log step (LOG_EVERY), and the bursts that overlap the pulse's stage
+    windows ([0, pulse_len] inclusive) evaluate the waves."""
+    from cmtj_gb300.sweeps import step_window
+    on, off = step_window(0.0, 1e-12, DT, None)
+    last = int(np.max(off))
+    loud = (last // LOG_EVERY + 1) * LOG_EVERY
+    return max(0.0, 1.0 - loud / float(n_steps))
 
 
 def dist_info():
@@ -376,7 +389,8 @@ def measure_rest(run, low, spec, n_steps, kern_ms, fft_ms, lib):
     out = {}
     # roofline of the dominant kernel (the FP32 batch integrator)
     ref_fpls, fcount = flops_per_layer_step()
-    fpls = fp32_flops_per_layer_step(2, 1)
+    quiet = pimm_quiet_fraction(n_steps)
+    fpls = fp32_flops_per_layer_step(2, 1, quiet)
     n = spec.n
     kavg = float(np.mean(kern_ms)) / 1e3
     achieved = fpls * n * n_steps * 2 / kavg / 1e12
@@ -394,6 +408,8 @@ def measure_rest(run, low, spec, n_steps, kern_ms, fft_ms, lib):
     out["roofline"] = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                        "frac": achieved / peak, "traffic": None,
                        "flop_per_layer_step": fpls,
+                       "flop_model": "171 per layer-step in quiet bursts, 201 while the pulse is on; "
+                                     "quiet share %.5f" % quiet,
                        "reference_flop_per_layer_step": ref_fpls,
                        "reference_flop_breakdown_add_mul_div_sqrt_trans": fcount,
                        "peak_source": "measured FP32 FMA probe on this GPU, best of scalar FFMA and packed FFMA2 "

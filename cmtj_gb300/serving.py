@@ -122,12 +122,19 @@ class ServingEngine:
         self.stream = self.t.cuda.Stream()
         self.streams = [self.t.cuda.Stream() for _ in range(max(1, n_streams))]
         self.stream64 = self.t.cuda.Stream()
-        self.tickets = self.t.zeros(len(self.streams) * 64, dtype=self.t.int32, device="cuda")
+        # one 64-byte work ticket per launch group of a tick
+        self.tickets = self.t.zeros(256 * 16, dtype=self.t.int32, device="cuda")
         self.active = []     # FP32 requests on the device: (req, slot, meta)
         self.active64 = []   # (req, lowered, log, status, event)
         self._next_id = 0
         self.params = np.zeros(1, dtype=batch.F32_PARAMS_DTYPE)
         self.stats = {"ticks": 0, "host_s": 0.0, "device_wait_s": 0.0, "admit_s": 0.0}
+        # launch groups (device order arrays) are rebuilt only when the set
+        # of running requests changes; the host runs at most `ahead` ticks
+        # in front of the device and synchronises only to retire requests
+        self._groups = None
+        self._tick_events = []
+        self.ahead = 2
 
     # ------------------------------------------------------------ admission
     def _admit(self, req, now):
@@ -207,56 +214,88 @@ class ServingEngine:
         return True
 
     # ------------------------------------------------------------ ticks
-    def _tick(self):
-        """Advance every admitted FP32 junction by up to chunk_steps."""
-        # one launch per (layer count, solver, kernel variant, reduction
-        # cadence): a junction always runs the same code whatever its
-        # neighbours in the pool
-        t_host = time.perf_counter()
+    def _build_groups(self):
+        """(layer count, solver, variant, reduction cadence) -> junction ids
+        of the running requests, one launch each per tick: a junction always
+        runs the same code whatever its neighbours in the pool."""
         groups = {}
         for req, meta in self.active:
             if meta["done"] >= meta["steps_max"]:
                 continue
             for key, ids in meta["parts"].items():
                 groups.setdefault(key, []).append(ids)
-        # partitions of one tick run concurrently, one stream (and one ticket)
-        # each, so their launch tails overlap; junction sets are disjoint
+        built = []
+        with self.t.cuda.stream(self.stream):
+            for key, parts in sorted(groups.items()):
+                order = np.concatenate(parts).astype(np.int32)
+                built.append((key, engine.to_device(order), int(order.size)))
         ev = self.t.cuda.Event()
-        ev.record(self.stream)  # admission copies happened on self.stream
-        keep = []
-        for q, ((nl, solver, v, red), parts) in enumerate(sorted(groups.items())):
+        ev.record(self.stream)  # admission copies and the order uploads
+        self._groups = (built, ev)
+
+    def _tick(self):
+        """Advance every running FP32 junction by up to chunk_steps, without
+        waiting for the device (at most `ahead` ticks in flight)."""
+        while len(self._tick_events) >= self.ahead:
+            t_dev = time.perf_counter()
+            self._tick_events.pop(0).synchronize()
+            self.stats["device_wait_s"] += time.perf_counter() - t_dev
+        t_host = time.perf_counter()
+        if self._groups is None:
+            self._build_groups()
+        built, ready = self._groups
+        # partitions of one tick run concurrently, one stream (and one ticket)
+        # each, so their launch tails overlap; junction sets are disjoint.
+        # A stream's next tick follows its previous one in stream order, and
+        # every stream waits for the previous tick's end on all streams.
+        prev = self._tick_events[-1] if self._tick_events else None
+        if len(built) > 256:
+            raise RuntimeError("more than 256 launch groups in one tick")
+        ends = []
+        for q, ((nl, solver, v, red), d_order, cnt) in enumerate(built):
             s = self.streams[q % len(self.streams)]
-            s.wait_event(ev)
+            s.wait_event(ready)
+            if prev is not None:
+                s.wait_event(prev)
             p = np.zeros(1, dtype=batch.F32_PARAMS_DTYPE)
             p["dt"] = self.dt
             p["chunk_steps"] = self.chunk
             p["log_mode"] = batch.LOG_NONE
             p["solver"] = solver
             p["red_every"] = red
-            order = np.concatenate(parts).astype(np.int32)
-            with self.t.cuda.stream(s):
-                d_order = engine.to_device(order)
-            ticket = self.tickets[q * 4:q * 4 + 1] if q < len(self.tickets) // 4 else None
+            ticket = self.tickets[q * 16:]
+            d_order.record_stream(s)  # kept alive for s when the groups are rebuilt
             rc = self.lib.cmtj_batch_run_f32(engine.ptr(self.pool.d_j), engine.ptr(self.pool.d_l),
-                                             engine.ptr(self.pool.d_s), engine.ptr(d_order), int(order.size), nl,
-                                             v, p.ctypes.data, engine.ptr(self.pool.d_log), engine.ptr(ticket),
-                                             0, engine.stream_ptr(s))
+                                             engine.ptr(self.pool.d_s), engine.ptr(d_order), cnt, nl, v,
+                                             p.ctypes.data, engine.ptr(self.pool.d_log), engine.ptr(ticket), 0,
+                                             engine.stream_ptr(s))
             _abi.check(rc, self.lib)
-            keep.append((d_order, p))
+            e = self.t.cuda.Event()
+            e.record(s)
+            ends.append(e)
+        done = self.t.cuda.Event()
+        for e in ends:
+            self.stream.wait_event(e)
+        done.record(self.stream)
+        self._tick_events.append(done)
         self.stats["host_s"] += time.perf_counter() - t_host
-        t_dev = time.perf_counter()
-        for s in self.streams:
-            s.synchronize()
-        self.stats["device_wait_s"] += time.perf_counter() - t_dev
         self.stats["ticks"] += 1
+        finished = False
         for req, meta in self.active:
-            meta["done"] += self.chunk
+            if meta["done"] < meta["steps_max"]:
+                meta["done"] += self.chunk
+                if meta["done"] >= meta["steps_max"]:
+                    meta["end_event"] = done
+                    finished = True
+        if finished:
+            self._groups = None
 
     def _retire(self, now):
         keep = []
         SB = batch.F32_STATE_DTYPE.itemsize
         for req, meta in self.active:
-            if meta["done"] >= meta["steps_max"]:
+            ev = meta.get("end_event")
+            if ev is not None and ev.query():
                 a = meta["slot"]
                 st = self.pool.d_s[a * SB:(a + req.n) * SB].cpu().numpy().view(batch.F32_STATE_DTYPE).copy()
                 req.state = st
@@ -292,10 +331,19 @@ class ServingEngine:
             while qi < len(pending) and pending[qi].arrival <= tnow:
                 if not self._admit(pending[qi], tnow):
                     break  # head of line waits for slots to free up
+                if pending[qi].precision != "f64":
+                    self._groups = None
                 qi += 1
             self.stats["admit_s"] += time.perf_counter() - ta
-            if self.active:
+            if any(meta["done"] < meta["steps_max"] for _, meta in self.active):
                 self._tick()
+                self._retire(now)
+            elif self.active:
+                # everything launched: wait for the oldest tick, then retire
+                t_dev = time.perf_counter()
+                if self._tick_events:
+                    self._tick_events.pop(0).synchronize()
+                self.stats["device_wait_s"] += time.perf_counter() - t_dev
                 self._retire(now)
             elif self.active64:
                 time.sleep(0.0005)

@@ -52,3 +52,17 @@ CASES = {
     "vsd_bilayer": vsd_bilayer,
     "vsd_bilayer_rx": vsd_bilayer_rx,
 }
+
+
+def pimm_bilayer_saturated(cm, RP):
+    """The same junction swept from saturation downwards along +x (no
+    switching on the way): a well-conditioned chain."""
+    j, kw = pimm_bilayer(cm, RP)
+    Hspan = np.linspace(600e3, 350e3, 5)
+    kw["Hvecs"] = np.stack([Hspan, 0 * Hspan, 0 * Hspan], 1)
+    j.setLayerMagnetisation("free", cm.CVector(1, 0, 0.1))
+    j.setLayerMagnetisation("ref", cm.CVector(1, 0, 0.2))
+    return j, kw
+
+
+CASES["pimm_bilayer_saturated"] = pimm_bilayer_saturated
