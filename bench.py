@@ -210,7 +210,7 @@ def spec_to_junctions(spec):
     return out
 
 
-def cpu_baseline(budget_s=12.0):
+def cpu_baseline(budget_s=15.0):
     """The oracle (the reference's arithmetic, bit-identical on the pinned
     cases) on all host cores: a pilot of whole 5 ns PIMM solves on 2
     junctions per core, then as many junctions as fill about budget_s."""
@@ -417,6 +417,27 @@ def measure_rest(run, low, spec, n_steps, kern_ms, fft_ms, lib):
                        "peak_scalar_ffma": peaks["cmtj_probe_fp32_peak"],
                        "peak_packed_ffma2": peaks["cmtj_probe_fp32x2_peak"],
                        "kernel_ms_avg": kavg * 1e3, "fft_ms_avg": float(np.mean(fft_ms))}
+    # HBM view of both kernels against MEASURED_PEAKS.json's copy bandwidth:
+    # k_batch moves its records once plus the decimated log; the FFT reads
+    # each row's last n_fft samples and writes the kept bins
+    hbm_peak = None
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            hbm_peak = float(json.load(f)["hbm_gbs"])
+    except (OSError, KeyError, ValueError):
+        pass
+    rec_bytes = low.junctions.nbytes + low.layers.nbytes + n * batch.F32_STATE_DTYPE.itemsize
+    log_bytes = 4.0 * float(np.sum(run.samples))
+    b_lo, b_hi = fft_bins()
+    fft_bytes = 4.0 * n * (N_FFT + (b_hi - b_lo))
+    k_gbs = (rec_bytes + log_bytes) / kavg / 1e9
+    f_gbs = fft_bytes / (float(np.mean(fft_ms)) / 1e3) / 1e9
+    out["roofline"]["hbm_secondary"] = {
+        "peak_gbs": hbm_peak, "peak_source": "MEASURED_PEAKS.json hbm_gbs" if hbm_peak else None,
+        "k_batch": {"algorithmic_bytes": rec_bytes + log_bytes, "achieved_gbs": k_gbs,
+                    "frac": k_gbs / hbm_peak if hbm_peak else None},
+        "k_spectrum": {"algorithmic_bytes": fft_bytes, "achieved_gbs": f_gbs,
+                       "frac": f_gbs / hbm_peak if hbm_peak else None}}
 
     # FP64 plain form and accuracy on a sample of the same junctions
     rows = np.arange(0, n, max(1, n // 256))[:256]
@@ -545,12 +566,18 @@ def serving_leg(fp64_rate, n_requests=200, rate_hz=200.0):
     continuous batching (cmtj_gb300.serving).  Latency = completion minus
     arrival, wall clock."""
     from cmtj_gb300 import serving
+    fifo = serving.ServingEngine(hbm_budget_bytes=8 << 30, chunk_steps=4000, policy="fifo")
+    t0 = time.perf_counter()
+    done_fifo = fifo.run(serving.make_trace(n_requests, rate_hz=rate_hz, seed=3))
+    fifo_summary = serving.summary(done_fifo, time.perf_counter() - t0)
     reqs = serving.make_trace(n_requests, rate_hz=rate_hz, seed=3)
-    eng = serving.ServingEngine(hbm_budget_bytes=8 << 30, chunk_steps=4000)
+    eng = serving.ServingEngine(hbm_budget_bytes=8 << 30, chunk_steps=4000, policy="sjf")
     t0 = time.perf_counter()
     done = eng.run(reqs)
     wall = time.perf_counter() - t0
     out = serving.summary(done, wall)
+    out["policy"] = "sjf: smallest layer-steps first among arrived requests"
+    out["fifo"] = {k: fifo_summary[k] for k in ("p50_ms", "p99_ms", "layer_steps_per_s", "wall_s")}
     offered = sum(r.layer_steps for r in done)
     out.update({"trace": "%d requests, Poisson %.0f req/s, 64-16384 solves, 2-40 ns, pimm/pbit/vsd mix"
                          % (n_requests, rate_hz),

@@ -54,7 +54,11 @@ LAYER_DTYPE = np.dtype(
      ("referenceType", "<i4"), ("includeSTT", "<i4"), ("includeSOT", "<i4"), ("dynamicSOT", "<i4"),
      ("alternativeSTT", "<i4"), ("temperatureSet", "<i4"),
      ("seed_lo", "<u4"), ("seed_hi", "<u4"), ("noise_step", "<u8"),
-     ("drv", DRIVER_DTYPE, NUM_SLOTS), ("adaptive", ADAPTIVE_DTYPE)], align=True)
+     ("drv", DRIVER_DTYPE, NUM_SLOTS), ("adaptive", ADAPTIVE_DTYPE),
+     ("conv_term", "<f8"), ("stoch_conv", "<f8"), ("ms_over_mu0", "<f8"), ("zero_terms", "<u4"),
+     ("reserved2", "<u4")], align=True)
+
+ZERO_DIPOLE, ZERO_IDMI, ZERO_K2, ZERO_J2 = 1, 2, 4, 8
 
 JUNCTION_DTYPE = np.dtype(
     [("n_layers", "<i4"), ("mr_mode", "<i4"), ("layer_offset", "<i4"), ("reserved", "<i4"),

@@ -163,6 +163,33 @@ def lower_layer(layer, rec, tables=None):
     for name, base in _AXIAL_SLOTS.items():
         for k in range(3):
             _fill_driver(drv[base + k], layer.axial[name].drivers[k], tables)
+    derive_layer(rec)
+
+
+def _const_zero(d):
+    return int(d["update"]) == _abi.DRV_CONSTANT and float(d["constantValue"]) == 0.0
+
+
+def derive_layer(rec):
+    """The derived fields of a cmtj_layer_t record: the reference's constant
+    sub-expressions, evaluated once in FP64 exactly as it writes them, and
+    the CMTJ_ZERO_* mask of field terms that are identically zero."""
+    c = _constants.snapshot()
+    d = float(rec["damping"])
+    rec["conv_term"] = 1 / (1 + d * d)
+    rec["stoch_conv"] = -c["gyro"] / (1. + d * d)
+    rec["ms_over_mu0"] = float(rec["Ms"]) / c["mu0"]
+    z = 0
+    if not np.any(rec["dipole_top"]) and not np.any(rec["dipole_bottom"]):
+        z |= _abi.ZERO_DIPOLE
+    drv = rec["drv"]
+    if all(_const_zero(drv[_abi.SLOT_IDMI_TOP + k]) and _const_zero(drv[_abi.SLOT_IDMI_BOTTOM + k]) for k in range(3)):
+        z |= _abi.ZERO_IDMI
+    if _const_zero(drv[_abi.SLOT_ANIS2]):
+        z |= _abi.ZERO_K2
+    if _const_zero(drv[_abi.SLOT_IECQ_TOP]) and _const_zero(drv[_abi.SLOT_IECQ_BOTTOM]):
+        z |= _abi.ZERO_J2
+    rec["zero_terms"] = z
 
 
 def lower_junction(junction, rec, layer_offset):

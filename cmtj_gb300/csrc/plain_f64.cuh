@@ -40,10 +40,17 @@ static __device__ __forceinline__ D3 normalized(const D3 &v) {
 }
 
 // calculate_tensor_interaction (junction.hpp:54-72).
-static __device__ __forceinline__ D3 tensor_mul(const D3 &m, const double *t, double Ms, double mu0) {
+// ms_mu0 = Ms / mu0, evaluated once by the host (cmtj_layer_t.ms_over_mu0).
+static __device__ __forceinline__ D3 tensor_mul(const D3 &m, const double *t, double ms_mu0) {
   const D3 r = d3(t[0] * m.x + t[1] * m.y + t[2] * m.z, t[3] * m.x + t[4] * m.y + t[5] * m.z,
                   t[6] * m.x + t[7] * m.y + t[8] * m.z);
-  return r * (Ms / mu0);
+  return r * ms_mu0;
+}
+
+// True when every component is +0 or -0 (integer test: no FP64 instruction).
+static __device__ __forceinline__ bool is_zero3(const D3 &v) {
+  const unsigned long long mask = 0x7fffffffffffffffull;
+  return ((__double_as_longlong(v.x) | __double_as_longlong(v.y) | __double_as_longlong(v.z)) & mask) == 0ull;
 }
 
 // x^3 rounded once: x*x is split exactly into hi + lo (FMA error-free
@@ -115,31 +122,54 @@ struct Side {
 // calculateHeff + solveLLG (junction.hpp:580-815, 855-864).
 static __device__ D3 rhs(const cmtj_layer_t &L, const cmtj_constants_t &c, double time, const D3 &m, const D3 &bottom,
                   const D3 &top, const DriverCtx &dc, Side *side, const cmtj_driver_t *cur = nullptr) {
-  const double mu0 = c.mu0;
   const double Ms = L.Ms;
-  // --- calculateHeff (580-622)
-  const D3 Hdipole = tensor_mul(bottom, L.dipole_bottom, Ms, mu0) + tensor_mul(top, L.dipole_top, Ms, mu0);
+  const uint32_t zt = L.zero_terms;
+  // --- calculateHeff (580-622).  Terms the host marked identically zero
+  // (CMTJ_ZERO_*), and IEC / IDMI against a zero neighbour vector, are left
+  // out of the sum: adding an exact zero changes no value.
+  const bool zb = is_zero3(bottom), ztop = is_zero3(top);
+  D3 Hdipole = zero3();
+  if (!(zt & CMTJ_ZERO_DIPOLE))
+    Hdipole = tensor_mul(bottom, L.dipole_bottom, L.ms_over_mu0) + tensor_mul(top, L.dipole_top, L.ms_over_mu0);
   const D3 Hext = axial(L, CMTJ_SLOT_HEXT, time, dc);
   const D3 Hoe = axial(L, CMTJ_SLOT_HOE, time, dc);
-  const D3 Hdemag = tensor_mul(m, L.demag, Ms, mu0);
+  const D3 Hdemag = tensor_mul(m, L.demag, L.ms_over_mu0);
   const double Jb = drv(L.drv[CMTJ_SLOT_IEC_BOTTOM], time, dc);
   const double Jt = drv(L.drv[CMTJ_SLOT_IEC_TOP], time, dc);
-  const double J2b = drv(L.drv[CMTJ_SLOT_IECQ_BOTTOM], time, dc);
-  const double J2t = drv(L.drv[CMTJ_SLOT_IECQ_TOP], time, dc);
   const double Mst = Ms * L.thickness;
-  const D3 Hiec = (bottom * (Jb + 2 * J2b * dot(bottom, m))) / Mst + (top * (Jt + 2 * J2t * dot(top, m))) / Mst;
-  const D3 Db = axial(L, CMTJ_SLOT_IDMI_BOTTOM, time, dc);
-  const D3 Dt = axial(L, CMTJ_SLOT_IDMI_TOP, time, dc);
-  const D3 Hidmi = smul(-1.0, cross(Db, bottom)) / Mst + smul(-1.0, cross(Dt, top)) / Mst;
+  D3 Hiec = zero3();
+  if (zt & CMTJ_ZERO_J2) {
+    // Jx + 2*0*dot = Jx exactly
+    if (!zb && !ztop) Hiec = (bottom * Jb) / Mst + (top * Jt) / Mst;
+    else if (!zb) Hiec = (bottom * Jb) / Mst;
+    else if (!ztop) Hiec = (top * Jt) / Mst;
+  } else {
+    const double J2b = drv(L.drv[CMTJ_SLOT_IECQ_BOTTOM], time, dc);
+    const double J2t = drv(L.drv[CMTJ_SLOT_IECQ_TOP], time, dc);
+    Hiec = (bottom * (Jb + 2 * J2b * dot(bottom, m))) / Mst + (top * (Jt + 2 * J2t * dot(top, m))) / Mst;
+  }
+  D3 Hidmi = zero3();
+  if (!(zt & CMTJ_ZERO_IDMI)) {
+    const D3 Db = axial(L, CMTJ_SLOT_IDMI_BOTTOM, time, dc);
+    const D3 Dt = axial(L, CMTJ_SLOT_IDMI_TOP, time, dc);
+    Hidmi = smul(-1.0, cross(Db, bottom)) / Mst + smul(-1.0, cross(Dt, top)) / Mst;
+  }
   const D3 anis = load3(L.anis);
   const double K = drv(L.drv[CMTJ_SLOT_ANIS], time, dc);
   const D3 Hanis = anis * ((2 * K) * dot(anis, m) / Ms);
   const D3 Hdmi = axial(L, CMTJ_SLOT_HDMI, time, dc);
   const D3 Hres = axial(L, CMTJ_SLOT_HRES, time, dc);
-  const double K2 = drv(L.drv[CMTJ_SLOT_ANIS2], time, dc);
-  const D3 Hanis2 = anis * ((4 * K2) * cube_rn(dot(anis, m)) / Ms);
-  const D3 Hfluct = zero3();
-  const D3 H = Hext + Hanis + Hanis2 + Hiec + Hidmi + Hoe + Hdmi + Hfluct - Hdemag - Hdipole + Hres;
+  double K2 = 0.0;
+  D3 H = Hext + Hanis;
+  if (!(zt & CMTJ_ZERO_K2)) {
+    K2 = drv(L.drv[CMTJ_SLOT_ANIS2], time, dc);
+    H = H + anis * ((4 * K2) * cube_rn(dot(anis, m)) / Ms);
+  }
+  H = H + Hiec;
+  if (!(zt & CMTJ_ZERO_IDMI)) H = H + Hidmi;
+  H = H + Hoe + Hdmi - Hdemag;  // + Hfluct (zero without a thermal field here)
+  if (!(zt & CMTJ_ZERO_DIPOLE)) H = H - Hdipole;
+  H = H + Hres;
   if (side) {
     side->K = K;
     side->K2 = K2;
@@ -155,7 +185,7 @@ static __device__ D3 rhs(const cmtj_layer_t &L, const cmtj_constants_t &c, doubl
   const double damping = L.damping;
   const D3 prod = cross(m, H);
   const D3 prod2 = cross(m, prod);
-  const double convTerm = 1 / (1 + damping * damping);
+  const double convTerm = L.conv_term;  // 1 / (1 + damping^2)
   const D3 dmdt = prod + prod2 * damping;
   D3 reference = zero3();
   if (L.referenceType == CMTJ_REF_FIXED) reference = load3(L.ref);
@@ -210,7 +240,7 @@ static __device__ D3 rhs(const cmtj_layer_t &L, const cmtj_constants_t &c, doubl
 // stochasticTorque (junction.hpp:824-831).
 static __device__ __forceinline__ D3 stoch_torque(const cmtj_layer_t &L, const cmtj_constants_t &c, const D3 &m,
                                            const D3 &dW) {
-  const double convTerm = -c.gyro / (1. + L.damping * L.damping);
+  const double convTerm = L.stoch_conv;  // -gyro / (1 + damping^2)
   const D3 th = cross(m, dW);
   const D3 th2 = cross(m, th);
   return (th + th2 * L.damping) * convTerm;

@@ -2,14 +2,17 @@
 //
 // cmtj_spectrum_f32 replaces the per-junction numpy/scipy post-processing of
 // PIMM_procedure (cmtj/utils/procedures.py:28-39, compute_spectrum_strip:
-// |scipy.fft.fft(m)| truncated to a frequency range).  One CTA of n/8
-// threads transforms one log row: a Stockham FFT (self-sorting, no bit
-// reversal) in radix-8 stages with a final radix-4 or radix-2 stage when
-// log2(n) is not a multiple of 3.  Every thread keeps its 8 points in
-// registers through a stage; stages exchange through one shared-memory
-// buffer (n complex floats), so an n = 4096 transform takes 4 stages and 8
-// CTA barriers.  The first stage reads the row straight from HBM
-// (coalesced), the last writes |X[k]| for k in [bin_lo, bin_hi).
+// |scipy.fft.fft(m)| truncated to a frequency range).  One CTA of n/16
+// threads transforms one log row.  The row is real, so its n-point spectrum
+// comes from an n/2-point complex FFT of (even, odd) sample pairs and one
+// unpacking pass over the kept bins.  The complex FFT is a Stockham FFT
+// (self-sorting, no bit reversal) in radix-8 stages, with a final radix-4
+// or radix-2 stage when log2(n/2) is not a multiple of 3.  Every thread
+// keeps its 8 points in registers through a stage; stages exchange through
+// one shared-memory buffer (n/2 complex floats), so an n = 4096 spectrum
+// takes 4 stages and 8 CTA barriers.  The first stage reads the row
+// straight from HBM (coalesced); the last pass writes |X[k]| for k in
+// [bin_lo, bin_hi).
 #include "common.cuh"
 
 namespace {
@@ -81,7 +84,9 @@ __device__ __forceinline__ void stage(const float *__restrict__ src_re, const fl
 #pragma unroll
     for (int r = 0; r < R; ++r) {
       const int idx = g + r * stride;
-      v[q][r] = from_global ? c2(grow[idx], 0.f) : c2(src_re[idx], src_im[idx]);
+      // from global: point idx of the half-length complex sequence
+      // z[m] = x[2m] + i x[2m+1] of the real row x
+      v[q][r] = from_global ? c2(grow[2 * idx], grow[2 * idx + 1]) : c2(src_re[idx], src_im[idx]);
     }
     const int k = g % Ns;
     if (!first && k) {
@@ -114,25 +119,32 @@ __device__ __forceinline__ void stage(const float *__restrict__ src_re, const fl
   __syncthreads();
 }
 
-__global__ void __launch_bounds__(1024) k_spectrum(const float *__restrict__ series, int64_t row_stride, int32_t series_len, int32_t n,
-                           int32_t bin_lo, int32_t bin_hi, float *__restrict__ out) {
+// |X[k]| of a real row x of n points, from the n/2-point complex FFT Z of
+// z[m] = x[2m] + i x[2m+1]:  with E = FFT(x even), O = FFT(x odd),
+// E[k] = (Z[k] + conj Z[h-k]) / 2, O[k] = (Z[k] - conj Z[h-k]) / 2i and
+// X[k] = E[k] + W_n^k O[k] (h = n/2, indices mod h); bins above n/2 use
+// |X[k]| = |X[n-k]|.
+__global__ void __launch_bounds__(512) k_spectrum(const float *__restrict__ series, int64_t row_stride,
+                                                  int32_t series_len, int32_t n, int32_t bin_lo, int32_t bin_hi,
+                                                  float *__restrict__ out) {
   extern __shared__ __align__(16) float sm[];
+  const int h = n / 2;
   float *re = sm;
-  float *im = sm + n;
+  float *im = sm + h;
   const int64_t row = blockIdx.x;
   const float *src = series + row * row_stride + (series_len - n);
   int Ns = 1;
   bool first = true;
-  while (Ns < n) {
-    const int left = n / Ns;
+  while (Ns < h) {
+    const int left = h / Ns;
     if (left >= 8) {
-      stage<8>(re, im, re, im, n, Ns, first, src, first);
+      stage<8>(re, im, re, im, h, Ns, first, src, first);
       Ns *= 8;
     } else if (left == 4) {
-      stage<4>(re, im, re, im, n, Ns, first, src, first);
+      stage<4>(re, im, re, im, h, Ns, first, src, first);
       Ns *= 4;
     } else {
-      stage<2>(re, im, re, im, n, Ns, first, src, first);
+      stage<2>(re, im, re, im, h, Ns, first, src, first);
       Ns *= 2;
     }
     first = false;
@@ -140,8 +152,18 @@ __global__ void __launch_bounds__(1024) k_spectrum(const float *__restrict__ ser
   const int nb = bin_hi - bin_lo;
   float *dst = out + row * (int64_t)nb;
   for (int k = threadIdx.x; k < nb; k += blockDim.x) {
-    const int q = bin_lo + k;
-    dst[k] = sqrtf(fmaf(re[q], re[q], im[q] * im[q]));
+    int q = bin_lo + k;
+    if (q > h) q = n - q;
+    const int a = q == h ? 0 : q;
+    const int b = q == 0 ? 0 : h - q;
+    const C2 zk = c2(re[a], im[a]);
+    const C2 zc = c2(re[b], -im[b]);
+    const C2 e = c2(0.5f * (zk.r + zc.r), 0.5f * (zk.i + zc.i));
+    const C2 o = c2(0.5f * (zk.i - zc.i), -0.5f * (zk.r - zc.r));
+    float sn, cs;
+    sincospif(-2.0f * (float)q / (float)n, &sn, &cs);
+    const C2 x = cadd(e, cmul(c2(cs, sn), o));
+    dst[k] = sqrtf(fmaf(x.r, x.r, x.i * x.i));
   }
 }
 
@@ -165,12 +187,12 @@ extern "C" int cmtj_spectrum_f32(const float *d_series, int64_t row_stride, int3
     cmtj_set_error("cmtj_spectrum_f32: null buffer");
     return CMTJ_ERR_ARG;
   }
-  const size_t smem = (size_t)(2 * n_fft) * sizeof(float);
+  const size_t smem = (size_t)n_fft * sizeof(float);  // n/2 complex points
   if (smem > 48 * 1024) {
     CMTJ_CUDA_TRY(cudaFuncSetAttribute(k_spectrum, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   }
-  k_spectrum<<<n_rows, n_fft / 8, smem, cmtj_stream(stream)>>>(d_series, row_stride, series_len, n_fft, bin_lo,
-                                                               bin_hi, d_out);
+  k_spectrum<<<n_rows, n_fft / 16, smem, cmtj_stream(stream)>>>(d_series, row_stride, series_len, n_fft, bin_lo,
+                                                                bin_hi, d_out);
   CMTJ_LAUNCH_CHECK("k_spectrum");
   return CMTJ_OK;
 }

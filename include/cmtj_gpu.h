@@ -134,7 +134,21 @@ typedef struct cmtj_layer {
   uint64_t noise_step;       /* Philox step counter at iteration 0         */
   cmtj_driver_t drv[CMTJ_NUM_SLOTS];
   cmtj_adaptive_t adaptive;  /* Dormand-Prince step control               */
+  /* Derived by the host from the fields above, with the reference's own
+   * expressions evaluated once (the solver would recompute the same bits at
+   * every call): 1/(1+damping^2) (solveLLG, junction.hpp:719),
+   * -gyro/(1+damping^2) (stochasticTorque, 826), Ms/mu0 (the demag and
+   * dipole scale, 54-72), and which field terms are identically zero
+   * (CMTJ_ZERO_*): adding an exact zero changes no value, so the solver
+   * skips them. */
+  double conv_term, stoch_conv, ms_over_mu0;
+  uint32_t zero_terms, reserved2;
 } cmtj_layer_t;
+
+#define CMTJ_ZERO_DIPOLE 1u  /* both dipole tensors are zero                 */
+#define CMTJ_ZERO_IDMI 2u    /* the six IDMI driver slots are constant 0     */
+#define CMTJ_ZERO_K2 4u      /* second-order anisotropy is constant 0        */
+#define CMTJ_ZERO_J2 8u      /* both quadratic IEC drivers are constant 0    */
 
 /* One Junction<double> (junction.hpp:1139-1243). */
 typedef struct cmtj_junction {

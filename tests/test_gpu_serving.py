@@ -44,3 +44,16 @@ def test_serving_admission_waits_for_hbm_budget(gpu_lib):
     done = eng.run(reqs)
     assert all(r.done_at is not None for r in done)
     assert eng.pool.free == [(0, eng.pool.capacity)]
+
+
+@pytest.mark.gpu
+def test_serving_policy_changes_order_not_results(gpu_lib):
+    """Shortest-job-first and FIFO admission give the same bits per request."""
+    states = []
+    for policy in ("fifo", "sjf"):
+        eng = serving.ServingEngine(hbm_budget_bytes=64 << 20, chunk_steps=500, policy=policy)
+        done = eng.run(_trace())
+        states.append({r.tag + str(r.arrival): r.state for r in done})
+    assert states[0].keys() == states[1].keys()
+    for k in states[0]:
+        assert np.array_equal(states[0][k]["m"], states[1][k]["m"]), k
