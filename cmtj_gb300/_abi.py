@@ -114,6 +114,7 @@ PROTOTYPES = {
     "cmtj_batch_run_f32_noalloc": (ctypes.c_int, [_P, _P, _P, _P, _I32, _I32, _I32, _P, _P, _I32, _I32, _P]),
     "cmtj_spectrum_f32": (ctypes.c_int, [_P, ctypes.c_int64, _I32, _I32, _I32, _I32, _I32, _P, _P]),
     "cmtj_run_stack_f64": (ctypes.c_int, [_P, _I32, _P, _P, _P, _P, _P, _P, _P, _P, _I32, _I32, _P, _P]),
+    "cmtj_run_group_f64": (ctypes.c_int, [_P, _I32, _P, _P, _P, _P, _P, _P, _P, _I32, _P, _P]),
 }
 
 _lib = None
@@ -146,10 +147,13 @@ def load(path=None):
 
 def check_layout(lib):
     from .batch import STRUCT_SIZES_F32
+    from .reservoir import GROUP_DTYPE, PAIR_DTYPE
     from .stack import STACK_DTYPE
     sizes = dict(STRUCT_SIZES)
     sizes.update(STRUCT_SIZES_F32)
     sizes["cmtj_stack_t"] = STACK_DTYPE.itemsize
+    sizes["cmtj_group_t"] = GROUP_DTYPE.itemsize
+    sizes["cmtj_pair_t"] = PAIR_DTYPE.itemsize
     n = len(sizes)
     buf = (ctypes.c_int32 * n)()
     lib.cmtj_struct_sizes(ctypes.cast(buf, _P), n)

@@ -212,7 +212,8 @@ int cmtj_device_info(int device, int32_t *sm_count, int32_t *cc_major, int32_t *
 /* sizeof of the structs of this header, in this order: cmtj_driver_t,
  * cmtj_layer_t, cmtj_junction_t, cmtj_constants_t, cmtj_sim_params_t,
  * cmtj_wave_t, cmtj_f32_layer_t, cmtj_f32_junction_t, cmtj_f32_state_t,
- * cmtj_f32_params_t, cmtj_stack_t (the first n <= 11); lets a binding check
+ * cmtj_f32_params_t, cmtj_stack_t, cmtj_group_t, cmtj_pair_t (the first
+ * n <= 13); lets a binding check
  * its mirror of the layout. */
 int cmtj_struct_sizes(int32_t *sizes, int32_t n);
 
@@ -263,6 +264,50 @@ int cmtj_run_stack_f64(const cmtj_stack_t *d_stacks, int32_t n_stacks, const dou
                        const cmtj_junction_t *d_junctions, const int32_t *d_top_bottom, cmtj_layer_t *d_layers,
                        const double *d_tables, const cmtj_sim_params_t *p, double *d_log, double *d_stack_log,
                        int32_t stack_width, int32_t max_junctions, uint32_t *d_status, void *stream);
+
+/* ---------------------------------------------------------------------- */
+/* Dipole-coupled groups: GroupInteraction (reservoir.hpp:122-245).        */
+/* ---------------------------------------------------------------------- */
+/* The interaction function of a group (reservoir.hpp:61-122). */
+enum cmtj_interaction {
+  CMTJ_INTERACTION_NULL = 0,    /* nullDipoleInteraction                    */
+  CMTJ_INTERACTION_DIPOLE = 1,  /* computeDipoleInteraction (the default)   */
+  CMTJ_INTERACTION_NOUMRA = 2   /* computeDipoleInteractionNoumra           */
+};
+
+typedef struct cmtj_group {
+  int32_t first_junction;       /* its junctions: [first, first + n_junctions) */
+  int32_t n_junctions;          /* 1 .. 256                                     */
+  int32_t interaction;          /* enum cmtj_interaction                        */
+  int32_t single_layer_runner;  /* RK4 with runSingleLayerSolver for every
+                                   junction (the last one has one layer)      */
+  int64_t pair_offset;          /* its n*n cmtj_pair_t records, row i = target */
+} cmtj_group_t;                 /* 24 bytes */
+
+/* The fixed geometry of the ordered pair (i, j) of a group (the field on i
+ * from j), formed once on the host with the reference's own expressions:
+ *   DIPOLE: g = (rij.x, rij.y, rij.z, |rij|^3, |rij|^5) with rij = r_i - r_j
+ *           (computeDipoleInteraction, reservoir.hpp:77-97); scale =
+ *           (Ms_j / mu0) * thickness_j * cellSurface_j
+ *   NOUMRA: g = the 3x3 tensor of getDipoleTensorFromRelPositions (37-57),
+ *           row-major; scale = Ms_j * V_j / mu0 (calculate_tensor_interaction)
+ * so the device evaluates only the part that depends on m_j. */
+typedef struct cmtj_pair {
+  double g[9];
+  double scale;
+} cmtj_pair_t;                  /* 80 bytes */
+
+/* GroupInteraction::runSimulation for n_groups groups, one CTA each, one
+ * thread per junction.  Every step: each junction's field from all others'
+ * top-layer magnetisations (frozen at step start) is summed in index order
+ * and set as its top layer's reserved interaction field (the HRES driver
+ * slots, setLayerReservedInteractionField), then every junction steps.
+ * d_top[j]: index (within junction j) of the topId layer.  Logs and status
+ * as cmtj_run_simulation_f64 (calculateEnergies off). */
+int cmtj_run_group_f64(const cmtj_group_t *d_groups, int32_t n_groups, const cmtj_pair_t *d_pairs,
+                       const cmtj_junction_t *d_junctions, const int32_t *d_top, cmtj_layer_t *d_layers,
+                       const double *d_tables, const cmtj_sim_params_t *p, double *d_log, int32_t max_junctions,
+                       uint32_t *d_status, void *stream);
 
 /* ---------------------------------------------------------------------- */
 /* FP32 batched form.                                                      */

@@ -20,6 +20,7 @@
 //   core/junction.hpp:1835-1867        strip / classic magnetoresistance
 //   core/junction.hpp:1948-1981        runSimulation fixed-step loop
 //   core/junction.hpp:1982-2045        runSimulation Dormand-Prince loop
+//   core/reservoir.hpp:61-151, 185-230 GroupInteraction (dipole-coupled groups)
 // keeping the reference's expression order so that deterministic runs are
 // bit-identical to the reference build (checked by tests/test_oracle_pin.py).
 //
@@ -676,6 +677,94 @@ int oracle_run_simulation(const cmtj_junction_t *junctions, int32_t n_junctions,
     std::vector<std::thread> pool;
     for (int k = 0; k < n_threads; ++k) pool.emplace_back(worker);
     for (auto &t : pool) t.join();
+  }
+  return CMTJ_OK;
+}
+
+// GroupInteraction::runSimulation (reservoir.hpp:185-230) with
+// stepFunctionalSolver (130-151), for n_groups groups.  The fixed pair
+// geometry comes from the host (cmtj_pair_t, formed with the reference's own
+// expressions); each step freezes every top layer's m, sums each junction's
+// interaction field from all others in index order (computeDipoleInteraction
+// 77-97 or the tensor form 99-122), sets it as the top layer's reserved
+// interaction field, then steps every junction with the last junction's
+// runner.  Same inputs, log layout and status words as cmtj_run_group_f64.
+int oracle_run_group(const cmtj_junction_t *junctions, cmtj_layer_t *layers, const double *tables,
+                     const cmtj_group_t *groups, int32_t n_groups, const cmtj_pair_t *pairs, const int32_t *top,
+                     const cmtj_sim_params_t *p, double *log, uint32_t *status) {
+  using oracle::V3;
+  if (n_groups < 0 || !p || p->write_every == 0) return CMTJ_ERR_ARG;
+  for (int32_t g = 0; g < n_groups; ++g) {
+    const cmtj_group_t &G = groups[g];
+    const int N = G.n_junctions;
+    std::vector<oracle::JunctionRun<double>> runs;
+    runs.reserve(N);
+    for (int k = 0; k < N; ++k) {
+      const cmtj_junction_t &J = junctions[G.first_junction + k];
+      runs.emplace_back(J, layers + J.layer_offset, *p, tables);
+      cmtj_layer_t &T = layers[J.layer_offset + top[G.first_junction + k]];
+      for (int c = 0; c < 3; ++c) T.drv[CMTJ_SLOT_HRES + c].update = CMTJ_DRV_CONSTANT;
+    }
+    uint32_t row = 0, code = CMTJ_STATUS_OK;
+    std::vector<V3<double>> frozen(N);
+    for (uint32_t i = 0; i < p->total_iterations && code == CMTJ_STATUS_OK; ++i) {
+      const double t = (double)i * p->time_step;
+      for (int k = 0; k < N; ++k) frozen[k] = runs[k].mag[top[G.first_junction + k]];
+      for (int k = 0; k < N; ++k) {
+        V3<double> H;
+        if (G.interaction != CMTJ_INTERACTION_NULL) {
+          for (int q = 0; q < N; ++q) {
+            if (q == k) continue;
+            const cmtj_pair_t &pr = pairs[G.pair_offset + (int64_t)k * N + q];
+            const V3<double> &m = frozen[q];
+            V3<double> term;
+            if (G.interaction == CMTJ_INTERACTION_DIPOLE) {
+              const V3<double> rij(pr.g[0], pr.g[1], pr.g[2]);
+              const double s = 3 * (m.x * rij.x + m.y * rij.y + m.z * rij.z);
+              term = oracle::smul<double>(pr.scale, oracle::smul<double>(s, rij) / pr.g[4] - m / pr.g[3]);
+            } else {
+              const double *tt = pr.g;
+              term = V3<double>(tt[0] * m.x + tt[1] * m.y + tt[2] * m.z, tt[3] * m.x + tt[4] * m.y + tt[5] * m.z,
+                                tt[6] * m.x + tt[7] * m.y + tt[8] * m.z) * pr.scale;
+            }
+            H = H + term;
+          }
+        }
+        const cmtj_junction_t &J = junctions[G.first_junction + k];
+        cmtj_layer_t &T = layers[J.layer_offset + top[G.first_junction + k]];
+        T.drv[CMTJ_SLOT_HRES + 0].constantValue = H.x;
+        T.drv[CMTJ_SLOT_HRES + 1].constantValue = H.y;
+        T.drv[CMTJ_SLOT_HRES + 2].constantValue = H.z;
+      }
+      for (int k = 0; k < N && code == CMTJ_STATUS_OK; ++k) {
+        if (p->solver == CMTJ_RK4) {
+          const bool ok = G.single_layer_runner ? runs[k].rk4(0, t, i, V3<double>(), V3<double>())
+                                                : runs[k].step_rk4(t, i);
+          if (!ok) code = CMTJ_STATUS_NAN;
+        } else if (p->solver == CMTJ_EULER_HEUN) {
+          runs[k].step_euler_heun(t, i);
+        } else {
+          runs[k].step_heun(t, i);
+        }
+      }
+      if (code != CMTJ_STATUS_OK) break;
+      if (!(i % p->write_every)) {
+        for (int k = 0; k < N; ++k)
+          runs[k].log_row(log + ((size_t)(G.first_junction + k) * p->n_log + row) * p->log_width, t);
+        ++row;
+      }
+    }
+    for (int k = 0; k < N; ++k) {
+      const int gj = G.first_junction + k;
+      cmtj_layer_t *Ls = layers + junctions[gj].layer_offset;
+      for (int l = 0; l < junctions[gj].n_layers; ++l) {
+        Ls[l].mag[0] = runs[k].mag[l].x;
+        Ls[l].mag[1] = runs[k].mag[l].y;
+        Ls[l].mag[2] = runs[k].mag[l].z;
+      }
+      status[2 * gj] = code;
+      status[2 * gj + 1] = row;
+    }
   }
   return CMTJ_OK;
 }

@@ -34,6 +34,8 @@ def oracle_lib():
         lib.oracle_gaussian3.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64, P]
         lib.oracle_log_width.restype = ctypes.c_int
         lib.oracle_log_width.argtypes = [ctypes.c_int, ctypes.c_int]
+        lib.oracle_run_group.restype = ctypes.c_int
+        lib.oracle_run_group.argtypes = [P, P, P, P, ctypes.c_int32, P, P, P, P, P]
         _lib = lib
     return _lib
 
@@ -78,6 +80,10 @@ def oracle_module():
     """A stand-in for the `cmtj` module whose Junction runs on the oracle."""
     m = types.SimpleNamespace(**{k: getattr(cmtj_gb300, k) for k in dir(cmtj_gb300) if not k.startswith("__")})
     m.Junction = OracleJunction
+    from cmtj_gb300 import reservoir
+    m.reservoir = types.SimpleNamespace(**{k: getattr(reservoir, k) for k in dir(reservoir)
+                                           if not k.startswith("__")})
+    m.reservoir.GroupInteraction = OracleGroupInteraction
     return m
 
 
@@ -99,3 +105,25 @@ def gaussian3(seed_lo, seed_hi, step):
     g = np.zeros(3, dtype=np.float64)
     oracle_lib().oracle_gaussian3(seed_lo, seed_hi, step, _p(g))
     return g
+
+
+def run_groups_oracle(groups, totalTime, timeStep=1e-13, writeFrequency=1e-11):
+    """cmtj_gb300.reservoir.run_groups with the oracle in place of the GPU
+    (same host preparation, same records)."""
+    from cmtj_gb300 import reservoir
+    plan, junctions, low, grec, tops, pairs = reservoir.prepare_groups(groups, totalTime, timeStep, writeFrequency)
+    n = len(junctions)
+    log = np.zeros((n, max(plan.n_log, 1), low.log_width), dtype=np.float64)
+    status = np.zeros(2 * n, dtype=np.uint32)
+    rc = oracle_lib().oracle_run_group(_p(low.junctions), _p(low.layers), _p(low.tables), _p(grec), len(groups),
+                                       _p(pairs), _p(tops), _p(low.params), _p(log), _p(status))
+    assert rc == 0, rc
+    apply_results(junctions, low, log, status, plan)
+    reservoir.finish_groups(groups, junctions, low, tops)
+
+
+class OracleGroupInteraction(cmtj_gb300.reservoir.GroupInteraction):
+    """A GroupInteraction whose runSimulation runs on the oracle."""
+
+    def runSimulation(self, totalTime, timeStep=1e-13, writeFrequency=1e-11):
+        run_groups_oracle([self], totalTime, timeStep, writeFrequency)

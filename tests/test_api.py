@@ -243,3 +243,31 @@ def test_reduction_sample_counts():
         got = batch.reduction_samples(n_steps, win, every)
         want = [len(range(w, n, every)) if n > w else 0 for n, w in zip(n_steps, win)]
         assert got.tolist() == want
+
+
+def test_layer_records_mark_identically_zero_terms():
+    """The FP64 solver skips field terms the host marks identically zero
+    (CMTJ_ZERO_*); the mask must be set exactly when the term is zero, and
+    the derived constants are the reference's expressions evaluated once."""
+    import cases
+    from cmtj_gb300 import _abi, constants
+    from cmtj_gb300._lower import lower, plan_run
+    plain, _ = cases.mtj_rh_point(cmtj, total=1e-12)
+    zoo, _ = cases.drivers_zoo(cmtj)
+    k2, _ = cases.energies_k2(cmtj)
+    plan = plan_run(1e-12, 1e-13, 1e-13)
+    every = _abi.ZERO_DIPOLE | _abi.ZERO_IDMI | _abi.ZERO_K2 | _abi.ZERO_J2
+    low = lower([plain], plan, cmtj.SolverMode.RK4, False)
+    assert all(int(r["zero_terms"]) == every for r in low.layers)
+    low = lower([zoo], plan, cmtj.SolverMode.RK4, False)
+    masks = [int(r["zero_terms"]) for r in low.layers]
+    assert all(not (m & _abi.ZERO_DIPOLE) for m in masks)  # both layers carry a dipole tensor
+    assert all(not (m & _abi.ZERO_IDMI) and not (m & _abi.ZERO_J2) for m in masks)
+    low = lower([k2], plan, cmtj.SolverMode.RK4, False)
+    assert any(not (int(r["zero_terms"]) & _abi.ZERO_K2) for r in low.layers)
+    c = constants.snapshot()
+    for r in low.layers:
+        d = float(r["damping"])
+        assert r["conv_term"] == 1 / (1 + d * d)
+        assert r["stoch_conv"] == -c["gyro"] / (1. + d * d)
+        assert r["ms_over_mu0"] == float(r["Ms"]) / c["mu0"]

@@ -1,0 +1,105 @@
+"""Dipole-coupled groups (cmtj_gb300.reservoir.GroupInteraction) against the
+reference's own logs (tests/golden/groups.npz, tests/golden/make_groups.py):
+the oracle bit for bit on CPU, the FP64 plain GPU form within 1e-9.  Plus
+the reference's API checks (tests/test_group_interaction.py in its suite)."""
+import os
+
+import numpy as np
+import pytest
+
+import cmtj_gb300 as cm
+import group_cases
+import oracle_harness
+
+GOLDEN = np.load(os.path.join(os.path.dirname(__file__), "golden", "groups.npz"))
+
+
+def _golden(name):
+    out = {}
+    for key in GOLDEN.files:
+        case, k, col = key.split("__", 2)
+        if case == name:
+            out.setdefault(int(k), {})[col] = GOLDEN[key]
+    return out
+
+
+@pytest.mark.parametrize("name", sorted(group_cases.CASES))
+def test_group_oracle_matches_reference_bitwise(name):
+    got = group_cases.run_case(oracle_harness.oracle_module(), name)
+    want = _golden(name)
+    assert sorted(got) == sorted(want)
+    for k in want:
+        assert set(got[k]) == set(want[k]), (k, set(got[k]) ^ set(want[k]))
+        for col, v in want[k].items():
+            assert got[k][col].shape == v.shape, (name, k, col)
+            assert np.array_equal(got[k][col], v), (name, k, col, np.max(np.abs(got[k][col] - v)))
+
+
+def test_group_api_checks():
+    z = cm.CVector(0, 0, 0)
+
+    def junction():
+        l = cm.Layer("free", mag=cm.CVector(0, 0, 1), anis=cm.CVector(0, 0, 1), Ms=1.0, thickness=2e-9,
+                     cellSurface=1e-16, demagTensor=[z, z, z])
+        return cm.Junction([l])
+
+    p1, p2 = cm.CVector(0, 0, 0), cm.CVector(100e-9, 0, 0)
+    cm.reservoir.GroupInteraction([p1, p2], [junction(), junction()])
+    with pytest.raises(RuntimeError):
+        cm.reservoir.GroupInteraction([p1], [junction(), junction()])
+    with pytest.raises(RuntimeError):
+        cm.reservoir.GroupInteraction([], [])
+    with pytest.raises(RuntimeError):
+        cm.reservoir.GroupInteraction([p1, p1], [junction(), junction()])
+    g = cm.reservoir.GroupInteraction([p1, p2], [junction(), junction()])
+    with pytest.raises(RuntimeError, match="non-existing"):
+        g.getLog(5)
+    j1, j2 = junction(), junction()
+    h = cm.reservoir.nullDipoleInteraction(p1, p2, j1.getLayer("free"), j2.getLayer("free"))
+    assert (h.x, h.y, h.z) == (0, 0, 0)
+    assert isinstance(cm.reservoir.computeDipoleInteraction(p1, p2, j1.getLayer("free"), j2.getLayer("free")),
+                      cm.CVector)
+    assert isinstance(cm.reservoir.computeDipoleInteractionNoumra(p1, p2, j1.getLayer("free"),
+                                                                  j2.getLayer("free")), cm.CVector)
+    with pytest.raises(RuntimeError, match="too close"):
+        cm.reservoir.computeDipoleInteraction(p1, cm.CVector(1e-12, 0, 0), j1.getLayer("free"), j2.getLayer("free"))
+
+
+def test_group_interaction_functions_match_reference_formula():
+    """The host forms of the two dipole fields against their formulas
+    written with numpy (reservoir.hpp:77-97 and 37-57, 99-122)."""
+    z = cm.CVector(0, 0, 0)
+    l1 = cm.Layer("free", mag=cm.CVector(0, 0, 1), anis=cm.CVector(0, 0, 1), Ms=1.1, thickness=2e-9,
+                  cellSurface=1e-16, demagTensor=[z, z, z])
+    l2 = cm.Layer("free", mag=cm.CVector(0.6, 0.0, 0.8), anis=cm.CVector(0, 0, 1), Ms=1.3, thickness=3e-9,
+                  cellSurface=2e-16, demagTensor=[z, z, z])
+    r1, r2 = np.array([10e-9, 5e-9, 0.0]), np.array([-40e-9, 20e-9, 3e-9])
+    mu0 = cm.constants.snapshot()["mu0"] if hasattr(cm.constants, "snapshot") else 12.566e-7
+    rij = r1 - r2
+    n = np.linalg.norm(rij)
+    m = np.array([0.6, 0.0, 0.8])
+    V = 3e-9 * 2e-16
+    want = (1.3 / mu0) * V * (3 * np.dot(m, rij) * rij / n ** 5 - m / n ** 3)
+    got = cm.reservoir.computeDipoleInteraction(cm.CVector(*r1), cm.CVector(*r2), l1, l2)
+    assert np.allclose([got.x, got.y, got.z], want, rtol=1e-12, atol=0)
+    T = 3 / (4 * np.pi * n ** 5) * (np.outer(rij, rij) - np.eye(3) * n * n / 3)
+    want = T @ m * (1.3 * V / mu0)
+    got = cm.reservoir.computeDipoleInteractionNoumra(cm.CVector(*r1), cm.CVector(*r2), l1, l2)
+    assert np.allclose([got.x, got.y, got.z], want, rtol=1e-12, atol=0)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", sorted(group_cases.CASES))
+def test_group_fp64_gpu_matches_reference(gpu_lib, name):
+    got = group_cases.run_case(cm, name)
+    want = _golden(name)
+    for k in want:
+        for col, v in want[k].items():
+            a = got[k][col]
+            assert a.shape == v.shape
+            if col == "time":
+                assert np.array_equal(a, v)
+            elif col.endswith(("_mx", "_my", "_mz")):
+                assert np.max(np.abs(a - v)) <= 1e-9, (name, k, col)
+            else:
+                assert np.max(np.abs(a - v)) <= 1e-9 * max(np.max(np.abs(v)), 1e-300), (name, k, col)
