@@ -71,8 +71,10 @@ template <int FEAT> struct Feat {
   // into one diagonal tensor: H += M m with M_i = 2K a_i^2/(mu0 Ms) - N_ii
   static constexpr bool diag = !full_demag && !k2 && !swaves && !offaxis;
   // every field term is stored pre-multiplied by the layer's gamma dt
-  // prefactor, so the torque needs no final scaling
-  static constexpr bool prescale = diag && !sot && !dipole && !idmi;
+  // prefactor, so the torque needs no final scaling (not with SOT, whose
+  // torques add to the LL term before the scaling, nor with scalar waves,
+  // whose deltas add to the unscaled coefficients)
+  static constexpr bool prescale = !sot && !swaves;
 };
 
 // Per-layer constants held in registers for the life of a junction.
@@ -146,12 +148,36 @@ template <int FEAT> struct LayerP {
       M = f3(fmaf(kc * a.x, a.x, -N[0]), fmaf(kc * a.y, a.y, -N[4]), fmaf(kc * a.z, a.z, -N[8]));
     }
     if (F::prescale) {
-      M = M * gdt;
       h0 = h0 * gdt;
       jb *= gdt;
       jt *= gdt;
       j2b *= gdt;
       j2t *= gdt;
+      if (F::diag) {
+        M = M * gdt;
+      } else {
+        kc *= gdt;
+        k2c *= gdt;
+        if (F::full_demag) {
+#pragma unroll
+          for (int q = 0; q < 9; ++q) N[q] *= gdt;
+        } else {
+          N[0] *= gdt;
+          N[4] *= gdt;
+          N[8] *= gdt;
+        }
+      }
+      if (F::dipole) {
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+          Db[q] *= gdt;
+          Dt[q] *= gdt;
+        }
+      }
+      if (F::idmi) {
+        dmib = dmib * gdt;
+        dmit = dmit * gdt;
+      }
     }
     sigc = r.sig_c;
     t0 = r.t0;
