@@ -503,37 +503,65 @@ __device__ __forceinline__ V2 v2renorm(V2 m) {
   return v2mul(m, make_float2(rsqrtf(q.x), rsqrtf(q.y)));
 }
 
-// Both layers' constants of a 2-layer junction whose variant has only the
-// constant field, field waves, uniaxial anisotropy along a coordinate axis,
-// diagonal demag and bilinear IEC: every field term pre-scaled by the
-// layer's gamma dt prefactor (LayerP with Feat::prescale).
-struct PairP {
-  V2 M, h0;      // folded anisotropy + demag tensor, constant field
-  float2 alpha;  // per layer
-  float2 jn;     // IEC of the one neighbour: (jt of layer 0, jb of layer 1)
-  template <int FEAT> __device__ __forceinline__ void load(const LayerP<FEAT> &p0, const LayerP<FEAT> &p1) {
-    M = pack2(p0.M, p1.M);
-    h0 = pack2(p0.h0, p1.h0);
-    alpha = make_float2(p0.alpha, p1.alpha);
-    jn = make_float2(p0.jt, p1.jb);
+// Constants of a layer pair (layers 2p, 2p+1) of a junction whose variant
+// has only the constant field, field waves, uniaxial anisotropy, diagonal
+// demag and bilinear IEC, with every field term pre-scaled by the layer's
+// gamma dt prefactor (LayerP with Feat::prescale).  DIAG: the anisotropy
+// axis lies on a coordinate axis and folds with the demag into M.  A pair
+// whose second layer does not exist (an odd layer count) carries a pad lane
+// with every coefficient zero: its m = (0, 0, 1) never moves.
+template <bool DIAG> struct PairC {
+  V2 A;          // DIAG: folded tensor M; else the anisotropy axis a
+  V2 nN;         // !DIAG: -diag(N)
+  V2 h0;         // constant field
+  float2 kc;     // !DIAG: anisotropy coefficient
+  float2 alpha;
+  float2 jb, jt; // IEC coefficient of each lane's bottom / top neighbour (0 at an edge)
+  template <int FEAT, int L>
+  __device__ __forceinline__ void load(const LayerP<FEAT> *P, int p) {
+    const int l0 = 2 * p, l1 = 2 * p + 1;
+    const bool has1 = l1 < L;
+    const F3 z = f3(0.f, 0.f, 0.f);
+    if (DIAG) {
+      A = pack2(P[l0].M, has1 ? P[l1].M : z);
+    } else {
+      A = pack2(P[l0].a, has1 ? P[l1].a : z);
+      nN = pack2(f3(-P[l0].N[0], -P[l0].N[4], -P[l0].N[8]),
+                 has1 ? f3(-P[l1].N[0], -P[l1].N[4], -P[l1].N[8]) : z);
+      kc = make_float2(P[l0].kc, has1 ? P[l1].kc : 0.f);
+    }
+    h0 = pack2(P[l0].h0, has1 ? P[l1].h0 : z);
+    alpha = make_float2(P[l0].alpha, has1 ? P[l1].alpha : 0.f);
+    jb = make_float2(l0 > 0 ? P[l0].jb : 0.f, has1 ? P[l1].jb : 0.f);
+    jt = make_float2(has1 ? P[l0].jt : 0.f, (has1 && l1 + 1 < L) ? P[l1].jt : 0.f);
   }
 };
 
-// rhs() of both layers at once, given hbase() of both layers.
-__device__ __forceinline__ V2 rhs2(const PairP &Q, V2 m, V2 H) {
-  H = v2fmav(Q.M, m, H);
+// rhs() of both lanes of a pair, given their hbase() sums.
+template <bool DIAG>
+__device__ __forceinline__ V2 rhs2(const PairC<DIAG> &Q, V2 m, V2 H) {
+  if (DIAG) {
+    H = v2fmav(Q.A, m, H);
+  } else {
+    const float2 da = v2dot(Q.A, m);
+    H = v2fma(Q.A, __fmul2_rn(Q.kc, da), H);
+    H = v2fmav(Q.nN, m, H);
+  }
   const V2 mxH = v2cross(m, H);
   return v2fma(v2cross(m, mxH), Q.alpha, mxH);
 }
 
 // One packed RK4 step of a 2-layer junction (the scalar RK4 of k_batch,
-// lane by lane).  WAVES: evaluate the waves at the three stage times;
-// otherwise the field base is time-independent and formed once.
-template <bool WAVES, int NW>
-__device__ __forceinline__ void packed_rk4_step(V2 &mp, const PairP &Q, const WaveR<2> *W, const V2 *HD, int nw,
-                                                uint32_t step, float dtf) {
+// lane by lane): the two layers are each other's only neighbour, so the
+// neighbour vector is the swapped pair.  WAVES: evaluate the waves at the
+// three stage times; otherwise the field base is time-independent and
+// formed once.
+template <bool DIAG, bool WAVES, int NW>
+__device__ __forceinline__ void packed_rk4_step(V2 &mp, const PairC<DIAG> &Q, const WaveR<2> *W, const V2 *HD,
+                                                int nw, uint32_t step, float dtf) {
   const V2 nb = swap2(mp);  // frozen neighbours: layer 0 sees layer 1, layer 1 sees layer 0
-  V2 hb = v2fma(nb, Q.jn, Q.h0), acc, kp;
+  const float2 jn = make_float2(Q.jt.x, Q.jb.y);
+  V2 hb = v2fma(nb, jn, Q.h0), acc, kp;
 #pragma unroll
   for (int st = 0; st < 4; ++st) {
     const int s = st == 0 ? 0 : (st == 3 ? 2 : 1);
@@ -542,15 +570,64 @@ __device__ __forceinline__ void packed_rk4_step(V2 &mp, const PairP &Q, const Wa
 #pragma unroll
       for (int w = 0; w < NW; ++w)
         if (w < nw) hb = v2fma(HD[w], bc2(W[w].unit(step, s, dtf)), hb);
-      hb = v2fma(nb, Q.jn, hb);
+      hb = v2fma(nb, jn, hb);
     }
     const V2 ms = st == 0 ? mp : v2fma(kp, bc2(st == 3 ? 6.f : 3.f), mp);
-    kp = rhs2(Q, ms, hb);
+    kp = rhs2<DIAG>(Q, ms, hb);
     if (st == 0) acc = kp;
     else if (st == 3) acc = v2add(acc, kp);
     else acc = v2fma(kp, bc2(2.f), acc);
   }
   mp = v2renorm(v2add(mp, acc));
+}
+
+// One packed RK4 step of a 3- or 4-layer junction as NP layer pairs.  Lane 0
+// of pair p is layer 2p (bottom neighbour: lane 1 of pair p-1, top: lane 1
+// of pair p); lane 1 is layer 2p+1 (bottom: lane 0 of pair p, top: lane 0
+// of pair p+1).  Neighbour terms add bottom then top, as hbase() does.
+template <int L, bool DIAG, bool WAVES, int NW>
+__device__ __forceinline__ void packed_rk4_step_pairs(V2 *mp, const PairC<DIAG> *Q, const WaveR<L> *W,
+                                                      const V2 (*HD)[(L + 1) / 2], int nw, uint32_t step,
+                                                      float dtf) {
+  constexpr int NP = (L + 1) / 2;
+  V2 nbB[NP], nbT[NP], hb[NP], acc[NP], kp[NP];
+#pragma unroll
+  for (int q = 0; q < NP; ++q) {
+    const V2 below = q > 0 ? mp[q - 1] : v2(bc2(0.f), bc2(0.f), bc2(0.f));
+    const V2 above = q + 1 < NP ? mp[q + 1] : v2(bc2(0.f), bc2(0.f), bc2(0.f));
+    nbB[q] = v2(make_float2(below.x.y, mp[q].x.x), make_float2(below.y.y, mp[q].y.x),
+                make_float2(below.z.y, mp[q].z.x));
+    nbT[q] = v2(make_float2(mp[q].x.y, above.x.x), make_float2(mp[q].y.y, above.y.x),
+                make_float2(mp[q].z.y, above.z.x));
+    hb[q] = v2fma(nbT[q], Q[q].jt, v2fma(nbB[q], Q[q].jb, Q[q].h0));
+  }
+#pragma unroll
+  for (int st = 0; st < 4; ++st) {
+    const int s = st == 0 ? 0 : (st == 3 ? 2 : 1);
+    if (WAVES && st != 2) {
+      float u[NW];  // each waveform once per stage time, shared by the pairs
+#pragma unroll
+      for (int w = 0; w < NW; ++w) u[w] = w < nw ? W[w].unit(step, s, dtf) : 0.f;
+#pragma unroll
+      for (int q = 0; q < NP; ++q) {
+        V2 h = Q[q].h0;
+#pragma unroll
+        for (int w = 0; w < NW; ++w)
+          if (w < nw) h = v2fma(HD[w][q], bc2(u[w]), h);
+        hb[q] = v2fma(nbT[q], Q[q].jt, v2fma(nbB[q], Q[q].jb, h));
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < NP; ++q) {
+      const V2 ms = st == 0 ? mp[q] : v2fma(kp[q], bc2(st == 3 ? 6.f : 3.f), mp[q]);
+      kp[q] = rhs2<DIAG>(Q[q], ms, hb[q]);
+      if (st == 0) acc[q] = kp[q];
+      else if (st == 3) acc[q] = v2add(acc[q], kp[q]);
+      else acc[q] = v2fma(kp[q], bc2(2.f), acc[q]);
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < NP; ++q) mp[q] = v2renorm(v2add(mp[q], acc[q]));
 }
 
 struct Args {
@@ -613,14 +690,21 @@ template <int L> __device__ __forceinline__ int log_channels(int mode) {
 #ifndef CMTJ_BATCH_MINB_PACKED
 #define CMTJ_BATCH_MINB_PACKED CMTJ_BATCH_MINB
 #endif
+#ifndef CMTJ_BATCH_MINB_WIDE
+#define CMTJ_BATCH_MINB_WIDE 3  // packed 3- and 4-layer variants (best of 3/4/5 measured)
+#endif
 
+// Layer-packed RK4: 2-4 layers, only constant / wave fields, uniaxial
+// anisotropy (on an axis or off it), diagonal demag and bilinear IEC.
 template <int L, int SOLVER, int FEAT>
 __host__ __device__ constexpr bool packed_variant() {
-  return L == 2 && SOLVER == CMTJ_RK4 && (FEAT & ~CMTJ_FEAT_WAVES) == 0;
+  return L >= 2 && SOLVER == CMTJ_RK4 && (FEAT & ~(CMTJ_FEAT_WAVES | CMTJ_FEAT_OFFAXIS)) == 0;
 }
 template <int L, int SOLVER, int FEAT>
 __host__ __device__ constexpr int min_blocks() {
-  return FEAT == CMTJ_FEAT_ALL ? 1 : (packed_variant<L, SOLVER, FEAT>() ? CMTJ_BATCH_MINB_PACKED : CMTJ_BATCH_MINB);
+  return FEAT == CMTJ_FEAT_ALL ? 1
+         : (packed_variant<L, SOLVER, FEAT>() ? (L == 2 ? CMTJ_BATCH_MINB_PACKED : CMTJ_BATCH_MINB_WIDE)
+                                               : CMTJ_BATCH_MINB);
 }
 
 template <int L, int SOLVER, int FEAT, int NW>
@@ -642,13 +726,15 @@ __global__ void __launch_bounds__(128, (min_blocks<L, SOLVER, FEAT>())) k_batch(
   // Packed two-layer RK4 for the variants with only constant / wave fields,
   // uniaxial anisotropy, diagonal demag and bilinear IEC.
   constexpr bool kPacked = packed_variant<L, SOLVER, FEAT>();
+  constexpr bool kDiag = Feat<FEAT>::diag;
+  constexpr int NP = (L + 1) / 2;  // layer pairs of the packed path
   static_assert(!kPacked || Feat<FEAT>::prescale, "the packed path reads pre-scaled fields");
 
   // junction-lifetime registers
   LayerP<FEAT> P[L];
   WaveR<L> W[NW > 0 ? NW : 1];
-  PairP Q;                      // kPacked: both layers' constants
-  V2 HD[NW > 0 ? NW : 1];       // kPacked: each wave's field direction x amplitude, both layers
+  PairC<kDiag> Q[NP];                  // kPacked: each layer pair's constants
+  V2 HD[NW > 0 ? NW : 1][NP];          // kPacked: each wave's field direction x amplitude, per pair
   int nw = 0;
   F3 m[L];
   int32_t jid = -1;
@@ -696,10 +782,14 @@ __global__ void __launch_bounds__(128, (min_blocks<L, SOLVER, FEAT>())) k_batch(
                 if (w < nw) W[w].load(J.waves[w], hs);
             }
             if constexpr (kPacked) {
-              Q.load(P[0], P[1]);
 #pragma unroll
-              for (int w = 0; w < NW; ++w)
-                if (w < nw) HD[w] = pack2(W[w].hdir[0], W[w].hdir[1]);
+              for (int q = 0; q < NP; ++q) {
+                Q[q].template load<FEAT, L>(P, q);
+#pragma unroll
+                for (int w = 0; w < NW; ++w)
+                  if (w < nw)
+                    HD[w][q] = pack2(W[w].hdir[2 * q], 2 * q + 1 < L ? W[w].hdir[2 * q + 1] : f3(0.f, 0.f, 0.f));
+              }
             }
             step = S.step;
             if (step == 0) {
@@ -754,16 +844,30 @@ __global__ void __launch_bounds__(128, (min_blocks<L, SOLVER, FEAT>())) k_batch(
       for (int w = 0; w < NW; ++w)
         if (w < nw) quiet = quiet && W[w].off_during(step, stop);
       if constexpr (kPacked) {
-        // RK4 on both layers at once (the scalar RK4 below, lane by lane);
-        // a quiet burst forms the field base once per step.
-        V2 mp = pack2(m[0], m[1]);
-        if (quiet) {
-          for (; step < stop; ++step) packed_rk4_step<false, NW>(mp, Q, W, HD, nw, step, dtf);
+        // RK4 on layer pairs (the scalar RK4 below, lane by lane); a quiet
+        // burst forms the field base once per step
+        V2 mp[NP];
+#pragma unroll
+        for (int q = 0; q < NP; ++q) mp[q] = pack2(m[2 * q], 2 * q + 1 < L ? m[2 * q + 1] : f3(0.f, 0.f, 1.f));
+        if constexpr (L == 2) {
+          if (quiet) {
+            for (; step < stop; ++step) packed_rk4_step<kDiag, false, NW>(mp[0], Q[0], W, &HD[0][0], nw, step, dtf);
+          } else {
+            for (; step < stop; ++step)
+              packed_rk4_step<kDiag, F::waves, NW>(mp[0], Q[0], W, &HD[0][0], nw, step, dtf);
+          }
         } else {
-          for (; step < stop; ++step) packed_rk4_step<F::waves, NW>(mp, Q, W, HD, nw, step, dtf);
+          if (quiet) {
+            for (; step < stop; ++step) packed_rk4_step_pairs<L, kDiag, false, NW>(mp, Q, W, HD, nw, step, dtf);
+          } else {
+            for (; step < stop; ++step) packed_rk4_step_pairs<L, kDiag, F::waves, NW>(mp, Q, W, HD, nw, step, dtf);
+          }
         }
-        m[0] = lane0(mp);
-        m[1] = lane1(mp);
+#pragma unroll
+        for (int q = 0; q < NP; ++q) {
+          m[2 * q] = lane0(mp[q]);
+          if (2 * q + 1 < L) m[2 * q + 1] = lane1(mp[q]);
+        }
       } else {
       for (; step < stop; ++step) {
       if (SOLVER == CMTJ_RK4) {

@@ -31,7 +31,8 @@ def build_variant(minb, layers=(2,)):
     B.build()
     out = os.path.join(B.BUILD, "tune_mb%d" % minb)
     os.makedirs(out, exist_ok=True)
-    flags = ["-DCMTJ_BATCH_MINB=%d" % minb, "-DCMTJ_BATCH_MINB_PACKED=%d" % minb]
+    flags = ["-DCMTJ_BATCH_MINB=%d" % minb, "-DCMTJ_BATCH_MINB_PACKED=%d" % minb,
+             "-DCMTJ_BATCH_MINB_WIDE=%d" % minb]
     tuned = {"batch_f32_l%d.cu" % L for L in layers}
     objs = []
     jobs = []
@@ -54,17 +55,26 @@ def build_variant(minb, layers=(2,)):
     return lib
 
 
-def time_library(lib, n_h, n_draw, steps, reps):
-    """Runs in a fresh process: loads `lib` and times one PIMM batch."""
+def time_library(lib, n_h, n_draw, steps, reps, workload="pimm"):
+    """Runs in a fresh process: loads `lib` and times one batch: the 2-layer
+    PIMM sweep, or (workload "vsd") the uneven 1-4-layer spin-diode sweep
+    at its own durations."""
     import numpy as np
     import torch
     from . import _abi
     _abi.LIB_PATH = lib
     from . import batch, sweeps
     dt = 1e-13
-    spec, ns = sweeps.pimm_config(n_h=n_h, n_draw=n_draw, dt=dt, total=steps * dt)
-    low = batch.lower(spec, dt, ns)
-    run = batch.BatchRun(low, dt, batch.SolverMode.RK4, batch.LOG_MIX, 10)
+    if workload == "vsd":
+        spec, ns = sweeps.vsd_config(dt=dt)
+        low = batch.lower(spec, dt, ns)
+        run = batch.BatchRun(low, dt, batch.SolverMode.RK4, batch.LOG_NONE, 0, red_every=1)
+        layer_steps = float((ns * spec.n_layers).sum())
+    else:
+        spec, ns = sweeps.pimm_config(n_h=n_h, n_draw=n_draw, dt=dt, total=steps * dt)
+        low = batch.lower(spec, dt, ns)
+        run = batch.BatchRun(low, dt, batch.SolverMode.RK4, batch.LOG_MIX, 10)
+        layer_steps = float(spec.n * ns * 2)
     zero = torch.zeros_like(run.d_s)
     times = []
     for k in range(reps + 1):
@@ -80,8 +90,8 @@ def time_library(lib, n_h, n_draw, steps, reps):
             times.append(a.elapsed_time(b))
     st = run.state()
     best = min(times)
-    return {"lib": lib, "ms": times, "best_ms": best, "layer_steps_per_s": spec.n * ns * 2 / (best / 1e3),
-            "all_ok": bool(np.all(st["status"] == 0))}
+    return {"lib": lib, "workload": workload, "ms": times, "best_ms": best,
+            "layer_steps_per_s": layer_steps / (best / 1e3), "all_ok": bool(np.all(st["status"] == 0))}
 
 
 def main(argv=None):
@@ -92,16 +102,18 @@ def main(argv=None):
     ap.add_argument("--n-h", type=int, default=512)
     ap.add_argument("--n-draw", type=int, default=512)
     ap.add_argument("--reps", type=int, default=3)
+    ap.add_argument("--workload", default="pimm", choices=["pimm", "vsd"])
     ap.add_argument("--time-lib", help=argparse.SUPPRESS)
     a = ap.parse_args(argv)
     if a.time_lib:
-        print(json.dumps(time_library(a.time_lib, a.n_h, a.n_draw, a.steps, a.reps)), flush=True)
+        print(json.dumps(time_library(a.time_lib, a.n_h, a.n_draw, a.steps, a.reps, a.workload)), flush=True)
         return
     results = []
     for mb in a.minb:
         lib = build_variant(mb, a.layers)
         out = subprocess.run([sys.executable, "-m", "cmtj_gb300.tune", "--time-lib", lib, "--steps", str(a.steps),
-                              "--n-h", str(a.n_h), "--n-draw", str(a.n_draw), "--reps", str(a.reps)],
+                              "--n-h", str(a.n_h), "--n-draw", str(a.n_draw), "--reps", str(a.reps),
+                              "--workload", a.workload],
                              capture_output=True, text=True, cwd=os.path.dirname(B.PKG))
         if out.returncode:
             raise RuntimeError(out.stderr)
