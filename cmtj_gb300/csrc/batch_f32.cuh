@@ -691,7 +691,7 @@ template <int L> __device__ __forceinline__ int log_channels(int mode) {
 #define CMTJ_BATCH_MINB_PACKED CMTJ_BATCH_MINB
 #endif
 #ifndef CMTJ_BATCH_MINB_WIDE
-#define CMTJ_BATCH_MINB_WIDE 3  // packed 3- and 4-layer variants (best of 3/4/5 measured)
+#define CMTJ_BATCH_MINB_WIDE 2  // packed 3- and 4-layer variants (best of 2/3/4/5 measured)
 #endif
 
 // Layer-packed RK4: 2-4 layers, only constant / wave fields, uniaxial
