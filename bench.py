@@ -124,7 +124,9 @@ class ClockSampler:
         mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({names[k] for r in self.rows for k in range(4) if r[3 + k].lower() == "active"})
-        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+        pw = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_min_mhz": min(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "power_w_max": max(pw) if pw else None,
                 "reasons": reasons, "samples": len(self.rows)}
 
 
@@ -372,13 +374,14 @@ def main():
         torch.distributed.barrier()
     a = torch.cuda.Event(enable_timing=True)
     b = torch.cuda.Event(enable_timing=True)
-    a.record(stream)
-    for k in range(args.steps):
-        e2e_step(k)
-    for e in out_done:
-        stream.wait_event(e)
-    b.record(stream)
-    torch.cuda.synchronize()
+    with ClockSampler(local) as e2e_clk:
+        a.record(stream)
+        for k in range(args.steps):
+            e2e_step(k)
+        for e in out_done:
+            stream.wait_event(e)
+        b.record(stream)
+        torch.cuda.synchronize()
     e2e_s = a.elapsed_time(b) / 1e3
     if world > 1:
         t = torch.tensor([e2e_s], device="cuda")
@@ -388,7 +391,8 @@ def main():
     e2e = {"value": world * layer_steps * args.steps / e2e_s, "unit": UNIT,
            "h2d_bytes_per_step": int(h_j.numel() + h_l.numel()),
            "d2h_bytes_per_step": int(h_spec.numel() * 4 + h_state.numel()),
-           "pipelining": "two device buffer sets; copies of one step overlap the neighbouring step's compute"}
+           "pipelining": "two device buffer sets; copies of one step overlap the neighbouring step's compute",
+           "clocks": e2e_clk.summary()}
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
