@@ -327,15 +327,17 @@ def main():
     # --- end to end through the C ABI with host buffers (pinned): H2D of
     # the junction/layer records, the batched run, the device FFT, D2H of
     # the spectra and final states, every step.  Two device buffer sets
-    # alternate, so step k's copies overlap step k-1's compute on a copy
-    # stream; every copy stays inside the timed region.
+    # alternate, so step k's upload and step k-1's download overlap the
+    # neighbouring compute; every copy stays inside the timed region.
     h_j = torch.from_numpy(low.junctions.view(np.uint8).copy()).pin_memory()
     h_l = torch.from_numpy(low.layers.view(np.uint8).copy()).pin_memory()
     runs = [run, batch.BatchRun(low, DT, batch.SolverMode.RK4, batch.LOG_MIX, LOG_EVERY, log_axis=0)]
     specs = [d_spec, torch.empty_like(d_spec)]
     h_specs = [torch.empty(d_spec.shape, dtype=torch.float32).pin_memory() for _ in range(2)]
     h_states = [torch.empty(run.d_s.shape, dtype=run.d_s.dtype).pin_memory() for _ in range(2)]
-    copy_stream = torch.cuda.Stream()
+    # uploads and downloads on their own streams (one copy engine each way),
+    # so step k+1's upload never queues behind step k's download
+    up_stream, down_stream = torch.cuda.Stream(), torch.cuda.Stream()
     out_done = [None, None]  # per buffer set: its last outputs are on the host
 
     def spectrum_of(r, out):
@@ -346,13 +348,13 @@ def main():
     def e2e_step(k):
         q = k % 2
         r = runs[q]
-        with torch.cuda.stream(copy_stream):
+        with torch.cuda.stream(up_stream):
             if out_done[q] is not None:
-                copy_stream.wait_event(out_done[q])
+                up_stream.wait_event(out_done[q])
             r.d_j.copy_(h_j, non_blocking=True)
             r.d_l.copy_(h_l, non_blocking=True)
             inputs = torch.cuda.Event()
-            inputs.record(copy_stream)
+            inputs.record(up_stream)
         stream.wait_event(inputs)
         with torch.cuda.stream(stream):
             r.d_s.copy_(state0)
@@ -360,12 +362,12 @@ def main():
             spectrum_of(r, specs[q])
             computed = torch.cuda.Event()
             computed.record(stream)
-        with torch.cuda.stream(copy_stream):
-            copy_stream.wait_event(computed)
+        with torch.cuda.stream(down_stream):
+            down_stream.wait_event(computed)
             h_specs[q].copy_(specs[q], non_blocking=True)
             h_states[q].copy_(r.d_s, non_blocking=True)
             out_done[q] = torch.cuda.Event()
-            out_done[q].record(copy_stream)
+            out_done[q].record(down_stream)
 
     for k in range(max(2, args.warmup // 2)):
         e2e_step(k)
@@ -582,6 +584,30 @@ def other_workloads():
                               "reductions": "plain and Butterworth-weighted <I R>, every step"}
     del run, low, spec
     torch.cuda.empty_cache()
+    # R(H) sweep of the 2-layer MTJ: 64 fields over +-800 kA/m along x, 1 ns
+    # at dt = 1e-13 with R logged every step; one FP64 plain launch and one
+    # FP32 batched launch, and the mean R over the last 20 % of each
+    from cmtj_gb300 import engine
+    js = [cases.mtj_rh_point(cm, hx=float(h), total=1e-9)[0] for h in np.linspace(-800e3, 800e3, 64)]
+    js32 = [cases.mtj_rh_point(cm, hx=float(h), total=1e-9)[0] for h in np.linspace(-800e3, 800e3, 64)]
+    plan = engine.plan_run(1e-9, DT, DT)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    engine.run_junctions(js, plan, batch.SolverMode.RK4)
+    torch.cuda.synchronize()
+    el64 = time.perf_counter() - t0
+    spec = batch.BatchSpec.from_junctions(js32)
+    run = batch.BatchRun(batch.lower(spec, DT, plan.total_iterations), DT, batch.SolverMode.RK4, batch.LOG_R, 1)
+    el32 = _timed_run(run)
+    log32 = run.d_log.cpu().numpy()
+    tail = plan.total_iterations // 5
+    r64 = np.array([np.mean(j.getLogArrays()["R_free_ref"][-tail:]) for j in js])
+    r32 = np.array([np.mean(run.log_of(k, log32)[-tail:, 0].astype(np.float64)) for k in range(len(js))])
+    ls = 64.0 * plan.total_iterations * 2
+    out["rh_sweep_64"] = {"fp64_plain_layer_steps_per_s": ls / el64, "fp32_batched_layer_steps_per_s": ls / el32,
+                          "max_abs_dR_mean_ohm": float(np.max(np.abs(r32 - r64))),
+                          "sample": "64 fields x 10,000 steps, R logged every step, mean over the last 2,000"}
+    del run
     # 16-junction series stack, FP64 plain form
     js = [cases._stt_junction(cm, 1.0 + 0.02 * k, 1e3 + 50 * k, (0.1, 0.2, 1), (1, 0, 0)) for k in range(16)]
     s = cm.stack.SeriesStack(js)
