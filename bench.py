@@ -233,7 +233,9 @@ def cpu_baseline(budget_s=15.0):
     oracle_harness.run_oracle(js, n_steps * DT, DT, DT * LOG_EVERY, threads=cores)
     el = time.perf_counter() - t0
     rate = n2 * n_steps * 2 / el
+    ref_fpls, fcount = flops_per_layer_step()
     return {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+            "reference_flop_per_layer_step": ref_fpls, "reference_flop_breakdown": fcount,
             "sample": "%d PIMM junctions x %d RK4 steps (full 5 ns solves) on %d threads (%.1f s)"
                       % (n2, n_steps, cores, el)}
 
@@ -424,7 +426,6 @@ def measure_rest(run, low, spec, n_steps, kern_ms, fft_ms, lib):
     from cmtj_gb300 import batch, engine
     out = {}
     # roofline of the dominant kernel (the FP32 batch integrator)
-    ref_fpls, fcount = flops_per_layer_step()
     quiet = pimm_quiet_fraction(n_steps)
     fpls = fp32_flops_per_layer_step(2, 1, quiet)
     n = spec.n
@@ -452,8 +453,6 @@ def measure_rest(run, low, spec, n_steps, kern_ms, fft_ms, lib):
                        "flop_per_layer_step": fpls,
                        "flop_model": "171 per layer-step in quiet bursts, 201 while the pulse is on; "
                                      "quiet share %.5f" % quiet,
-                       "reference_flop_per_layer_step": ref_fpls,
-                       "reference_flop_breakdown_add_mul_div_sqrt_trans": fcount,
                        "peak_source": "measured FP32 FMA probe on this GPU, best of scalar FFMA and packed FFMA2 "
                                       "(MEASURED_PEAKS.json has no FP32 figure)",
                        "peak_scalar_ffma": peaks["cmtj_probe_fp32_peak"],
@@ -527,6 +526,10 @@ def measure_rest(run, low, spec, n_steps, kern_ms, fft_ms, lib):
     out["serving"] = serving_leg(fp64_batch)
     out["other_workloads"] = other_workloads()
     out["cpu_baseline"] = cpu_baseline()
+    # the reference's own arithmetic per layer-step, counted in the CPU leg
+    out["roofline"]["reference_flop_per_layer_step"] = out["cpu_baseline"].pop("reference_flop_per_layer_step")
+    out["roofline"]["reference_flop_breakdown_add_mul_div_sqrt_trans"] = out["cpu_baseline"].pop(
+        "reference_flop_breakdown")
     return out
 
 
