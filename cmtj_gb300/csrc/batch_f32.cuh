@@ -91,7 +91,7 @@ template <int FEAT> struct LayerP {
   F3 ref, ref2;
   int rtype, flags;
   float sttc, sttp, sttl, sttb, sttk, i0, fl0, dl0, fl20, dl20;  // sttc carries dt (dt/6 for RK4)
-  float sigc, t0;
+  float sigc, t0, sig;  // sig = sqrt(sigc * t0): the thermal scale at constant T
   uint32_t seed_lo, seed_hi;
   uint64_t nstep0;
 
@@ -181,6 +181,7 @@ template <int FEAT> struct LayerP {
     }
     sigc = r.sig_c;
     t0 = r.t0;
+    sig = sqrtf(fmaxf(sigc * t0, 0.f));
     seed_lo = r.seed_lo;
     seed_hi = r.seed_hi;
     nstep0 = ((uint64_t)r.noise_step_hi << 32) | r.noise_step_lo;
@@ -922,8 +923,8 @@ __global__ void __launch_bounds__(128, (min_blocks<L, SOLVER, FEAT>())) k_batch(
         F3 f[L], g[L], dW[L], mn[L];
 #pragma unroll
         for (int l = 0; l < L; ++l) {
-          const float T0 = F::swaves ? P[l].t0 + d[l].dT : P[l].t0;
-          const float sigma = sqrtf(fmaxf(P[l].sigc * T0, 0.f));
+          // without scalar waves T is constant: sigma was formed at load
+          const float sigma = F::swaves ? sqrtf(fmaxf(P[l].sigc * (P[l].t0 + d[l].dT), 0.f)) : P[l].sig;
           if (sigma > 0.f) {
             float g0, g1, g2;
             cmtj_gaussian3_f32(P[l].seed_lo, P[l].seed_hi, P[l].nstep0 + step, g0, g1, g2);

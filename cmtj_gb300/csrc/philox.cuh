@@ -54,11 +54,12 @@ __device__ __forceinline__ void cmtj_gaussian3_f32(uint32_t seed_lo, uint32_t se
   const float s = 2.3283064365386963e-10f;
   const float u0 = ((float)w.x + 0.5f) * s, u1 = ((float)w.y + 0.5f) * s;
   const float u2 = ((float)w.z + 0.5f) * s, u3 = ((float)w.w + 0.5f) * s;
-  // (float)w rounds to 24 bits, so u may round to exactly 1.0 (r = 0);
-  // logf keeps -2 log(u) >= 0 near u = 1, where __logf's absolute error
-  // could turn it negative.
-  const float r0 = sqrtf(-2.0f * logf(u0));
-  const float r1 = sqrtf(-2.0f * logf(u2));
+  // (float)w rounds to 24 bits, so u may round to exactly 1.0 (r = 0).
+  // __logf (the hardware log2 scaled by ln 2) has a small absolute error
+  // near u = 1 that can make -2 log(u) slightly negative there; the clamp
+  // keeps r >= 0.  The draws only have to be right in distribution.
+  const float r0 = sqrtf(fmaxf(-2.0f * __logf(u0), 0.f));
+  const float r1 = sqrtf(fmaxf(-2.0f * __logf(u2), 0.f));
   float s0, c0, s1, c1;
   sincospif(2.0f * u1, &s0, &c0);
   sincospif(2.0f * u3, &s1, &c1);
