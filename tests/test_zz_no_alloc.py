@@ -77,3 +77,33 @@ def test_noalloc_rejects_slot_beyond_static_array(gpu_lib):
     rc = lib.cmtj_batch_run_f32_noalloc(dummy, dummy, dummy, dummy, 1, 1, 0, p.ctypes.data, None, 64, 0, None)
     assert rc == _abi.CMTJ_ERR_LIMIT
     assert "outside [0, 64)" in _abi.last_error(lib)
+
+
+@pytest.mark.gpu
+def test_noalloc_launch_replays_from_a_cuda_graph(gpu_lib):
+    """Captured into a CUDA graph (no allocation may happen while a stream
+    is being captured) and replayed twice: each replay gives the direct
+    launch's bits."""
+    torch = engine.torch()
+    lib = _abi.load()
+    run = batch.BatchRun(_mixed_batch(), 1e-13, cmtj_gb300.SolverMode.RK4, batch.LOG_M, 10)
+    zero_state = torch.zeros_like(run.d_s)
+    run.d_s.copy_(zero_state)
+    _run_noalloc(run, lib, slot=5)  # direct launch; also resolves the static ticket's address
+    torch.cuda.synchronize()
+    want_state = run.state().copy()
+    want_log = run.d_log.cpu().numpy().copy()
+    graph = torch.cuda.CUDAGraph()
+    side = torch.cuda.Stream()
+    with torch.cuda.stream(side):
+        with torch.cuda.graph(graph, stream=side):
+            run.d_s.copy_(zero_state)
+            _run_noalloc(run, lib, slot=5)
+    for _ in range(2):
+        run.d_log.zero_()
+        graph.replay()
+        torch.cuda.synchronize()
+        st = run.state()
+        assert np.all(st["status"] == 0) and np.all(st["step"] == 2000)
+        assert np.array_equal(st["m"], want_state["m"])
+        assert np.array_equal(run.d_log.cpu().numpy(), want_log)
