@@ -244,13 +244,15 @@ def lower(junctions, plan, solver, calculate_energies):
         for l in j.layers:
             lower_layer(l, larr[off], tables)
             off += 1
-    width = _abi.log_width(max(j.layerNo for j in junctions), calculate_energies)
-    params = make_params(plan, solver, calculate_energies, width)
+    max_layers = max(j.layerNo for j in junctions)
+    width = _abi.log_width(max_layers, calculate_energies)
+    params = make_params(plan, solver, calculate_energies, width, max_layers)
     return Lowered(jarr, larr, tables.array(), params, width)
 
 
-def make_params(plan, solver, calculate_energies, width):
+def make_params(plan, solver, calculate_energies, width, max_layers=0):
     p = np.zeros(1, dtype=_abi.SIM_PARAMS_DTYPE)
+    p["max_layers"] = max_layers
     p["time_step"] = plan.time_step
     p["total_iterations"] = plan.total_iterations
     p["write_every"] = plan.write_every

@@ -3,7 +3,7 @@
 Each translation unit under csrc/ is compiled by nvcc in parallel and the
 objects are linked into cmtj_gb300/_build/libcmtj_gpu.so (CUDA runtime
 linked statically, so the library does not depend on which libcudart the
-host process loaded).  The FP64 plain-form unit is compiled with
+host process loaded).  The FP64 plain-form units are compiled with
 --fmad=false: its arithmetic must round exactly like the reference's.
 """
 import concurrent.futures
@@ -23,6 +23,7 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + INCLUD
 UNITS = {
     "abi.cu": [],
     "plain_f64.cu": ["--fmad=false"],
+    "plain_lanes_f64.cu": ["--fmad=false"],
     "stack_f64.cu": ["--fmad=false"],
     "group_f64.cu": ["--fmad=false"],
     "batch_f32.cu": [],

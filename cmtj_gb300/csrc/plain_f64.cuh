@@ -112,6 +112,34 @@ static __device__ __forceinline__ D3 axial(const cmtj_layer_t &L, int slot, doub
   return d3(drv(L.drv[slot], t, dc), drv(L.drv[slot + 1], t, dc), drv(L.drv[slot + 2], t, dc));
 }
 
+// One out-of-line copy of the driver dispatch for callers that reach it
+// only for the few time-dependent slots.
+static __device__ __noinline__ double drv_call(const cmtj_driver_t &d, double time, DriverCtx dc) {
+  return drv(d, time, dc);
+}
+
+// Driver slot s at `time`.  Bit s of dyn marks a slot whose driver is not
+// CMTJ_DRV_CONSTANT; the other slots return constantValue, which is what
+// drv() returns for them, without the dispatch.  dyn = ~0u evaluates every
+// slot through drv().
+static __device__ __forceinline__ double slot_at(const cmtj_layer_t &L, int s, double time, const DriverCtx &dc,
+                                                 uint32_t dyn) {
+  if (dyn == 0xffffffffu) return drv(L.drv[s], time, dc);
+  return ((dyn >> s) & 1u) ? drv_call(L.drv[s], time, dc) : L.drv[s].constantValue;
+}
+static __device__ __forceinline__ D3 axial_at(const cmtj_layer_t &L, int s, double time, const DriverCtx &dc,
+                                              uint32_t dyn) {
+  return d3(slot_at(L, s, time, dc, dyn), slot_at(L, s + 1, time, dc, dyn), slot_at(L, s + 2, time, dc, dyn));
+}
+
+// Bit s set when driver slot s of L is time-dependent (not CMTJ_DRV_CONSTANT).
+static __device__ __forceinline__ uint32_t dynamic_slots(const cmtj_layer_t &L) {
+  uint32_t m = 0;
+  for (int s = 0; s < CMTJ_NUM_SLOTS; ++s)
+    if (L.drv[s].update != CMTJ_DRV_CONSTANT) m |= 1u << s;
+  return m;
+}
+
 // Values the reference keeps on the Layer as side effects of the last field
 // evaluation and logs with calculateEnergies (junction.hpp:1589-1613).
 struct Side {
@@ -121,7 +149,8 @@ struct Side {
 
 // calculateHeff + solveLLG (junction.hpp:580-815, 855-864).
 static __device__ D3 rhs(const cmtj_layer_t &L, const cmtj_constants_t &c, double time, const D3 &m, const D3 &bottom,
-                  const D3 &top, const DriverCtx &dc, Side *side, const cmtj_driver_t *cur = nullptr) {
+                  const D3 &top, const DriverCtx &dc, Side *side, const cmtj_driver_t *cur = nullptr,
+                  uint32_t dyn = 0xffffffffu) {
   const double Ms = L.Ms;
   const uint32_t zt = L.zero_terms;
   // --- calculateHeff (580-622).  Terms the host marked identically zero
@@ -131,11 +160,11 @@ static __device__ D3 rhs(const cmtj_layer_t &L, const cmtj_constants_t &c, doubl
   D3 Hdipole = zero3();
   if (!(zt & CMTJ_ZERO_DIPOLE))
     Hdipole = tensor_mul(bottom, L.dipole_bottom, L.ms_over_mu0) + tensor_mul(top, L.dipole_top, L.ms_over_mu0);
-  const D3 Hext = axial(L, CMTJ_SLOT_HEXT, time, dc);
-  const D3 Hoe = axial(L, CMTJ_SLOT_HOE, time, dc);
+  const D3 Hext = axial_at(L, CMTJ_SLOT_HEXT, time, dc, dyn);
+  const D3 Hoe = axial_at(L, CMTJ_SLOT_HOE, time, dc, dyn);
   const D3 Hdemag = tensor_mul(m, L.demag, L.ms_over_mu0);
-  const double Jb = drv(L.drv[CMTJ_SLOT_IEC_BOTTOM], time, dc);
-  const double Jt = drv(L.drv[CMTJ_SLOT_IEC_TOP], time, dc);
+  const double Jb = slot_at(L, CMTJ_SLOT_IEC_BOTTOM, time, dc, dyn);
+  const double Jt = slot_at(L, CMTJ_SLOT_IEC_TOP, time, dc, dyn);
   const double Mst = Ms * L.thickness;
   D3 Hiec = zero3();
   if (zt & CMTJ_ZERO_J2) {
@@ -144,25 +173,25 @@ static __device__ D3 rhs(const cmtj_layer_t &L, const cmtj_constants_t &c, doubl
     else if (!zb) Hiec = (bottom * Jb) / Mst;
     else if (!ztop) Hiec = (top * Jt) / Mst;
   } else {
-    const double J2b = drv(L.drv[CMTJ_SLOT_IECQ_BOTTOM], time, dc);
-    const double J2t = drv(L.drv[CMTJ_SLOT_IECQ_TOP], time, dc);
+    const double J2b = slot_at(L, CMTJ_SLOT_IECQ_BOTTOM, time, dc, dyn);
+    const double J2t = slot_at(L, CMTJ_SLOT_IECQ_TOP, time, dc, dyn);
     Hiec = (bottom * (Jb + 2 * J2b * dot(bottom, m))) / Mst + (top * (Jt + 2 * J2t * dot(top, m))) / Mst;
   }
   D3 Hidmi = zero3();
   if (!(zt & CMTJ_ZERO_IDMI)) {
-    const D3 Db = axial(L, CMTJ_SLOT_IDMI_BOTTOM, time, dc);
-    const D3 Dt = axial(L, CMTJ_SLOT_IDMI_TOP, time, dc);
+    const D3 Db = axial_at(L, CMTJ_SLOT_IDMI_BOTTOM, time, dc, dyn);
+    const D3 Dt = axial_at(L, CMTJ_SLOT_IDMI_TOP, time, dc, dyn);
     Hidmi = smul(-1.0, cross(Db, bottom)) / Mst + smul(-1.0, cross(Dt, top)) / Mst;
   }
   const D3 anis = load3(L.anis);
-  const double K = drv(L.drv[CMTJ_SLOT_ANIS], time, dc);
+  const double K = slot_at(L, CMTJ_SLOT_ANIS, time, dc, dyn);
   const D3 Hanis = anis * ((2 * K) * dot(anis, m) / Ms);
-  const D3 Hdmi = axial(L, CMTJ_SLOT_HDMI, time, dc);
-  const D3 Hres = axial(L, CMTJ_SLOT_HRES, time, dc);
+  const D3 Hdmi = axial_at(L, CMTJ_SLOT_HDMI, time, dc, dyn);
+  const D3 Hres = axial_at(L, CMTJ_SLOT_HRES, time, dc, dyn);
   double K2 = 0.0;
   D3 H = Hext + Hanis;
   if (!(zt & CMTJ_ZERO_K2)) {
-    K2 = drv(L.drv[CMTJ_SLOT_ANIS2], time, dc);
+    K2 = slot_at(L, CMTJ_SLOT_ANIS2, time, dc, dyn);
     H = H + anis * ((4 * K2) * cube_rn(dot(anis, m)) / Ms);
   }
   H = H + Hiec;
@@ -192,7 +221,7 @@ static __device__ D3 rhs(const cmtj_layer_t &L, const cmtj_constants_t &c, doubl
   else if (L.referenceType == CMTJ_REF_TOP) reference = top;
   else if (L.referenceType == CMTJ_REF_BOTTOM) reference = bottom;
   if (L.includeSTT) {
-    const double I = drv(cur ? *cur : L.drv[CMTJ_SLOT_CURRENT], time, dc);
+    const double I = cur ? drv(*cur, time, dc) : slot_at(L, CMTJ_SLOT_CURRENT, time, dc, dyn);
     if (side) side->I = I;
     const double aJ = c.hbar * I / (c.echarge * L.Ms * L.thickness);
     double eta = 0;
@@ -209,12 +238,12 @@ static __device__ D3 rhs(const cmtj_layer_t &L, const cmtj_constants_t &c, doubl
   } else if (L.includeSOT) {
     double Hdl = 0, Hfl = 0, Hdl2 = 0, Hfl2 = 0;
     if (L.dynamicSOT) {
-      Hdl = drv(L.drv[CMTJ_SLOT_DL], time, dc);
-      Hfl = drv(L.drv[CMTJ_SLOT_FL], time, dc);
-      Hdl2 = drv(L.drv[CMTJ_SLOT_DL2], time, dc);
-      Hfl2 = drv(L.drv[CMTJ_SLOT_FL2], time, dc);
+      Hdl = slot_at(L, CMTJ_SLOT_DL, time, dc, dyn);
+      Hfl = slot_at(L, CMTJ_SLOT_FL, time, dc, dyn);
+      Hdl2 = slot_at(L, CMTJ_SLOT_DL2, time, dc, dyn);
+      Hfl2 = slot_at(L, CMTJ_SLOT_FL2, time, dc, dyn);
     } else {
-      const double I = drv(cur ? *cur : L.drv[CMTJ_SLOT_CURRENT], time, dc);
+      const double I = cur ? drv(*cur, time, dc) : slot_at(L, CMTJ_SLOT_CURRENT, time, dc, dyn);
       if (side) side->I = I;
       Hdl = L.dampingLikeTorque * I;
       Hfl = L.fieldLikeTorque * I;
@@ -248,9 +277,9 @@ static __device__ __forceinline__ D3 stoch_torque(const cmtj_layer_t &L, const c
 
 // getStochasticLangevinVector (junction.hpp:1111-1128).
 static __device__ __forceinline__ D3 langevin(const cmtj_layer_t &L, const cmtj_constants_t &c, double time,
-                                       uint32_t i, const DriverCtx &dc) {
+                                       uint32_t i, const DriverCtx &dc, uint32_t dyn = 0xffffffffu) {
   if (!L.temperatureSet) return zero3();
-  const double temp = drv(L.drv[CMTJ_SLOT_TEMPERATURE], time, dc);
+  const double temp = slot_at(L, CMTJ_SLOT_TEMPERATURE, time, dc, dyn);
   const double mainFactor = (2 * L.damping * c.kB * temp) / (L.Ms * L.cellVolume * c.gyro);
   const double sigma = sqrt(mainFactor);
   double g0, g1, g2;

@@ -1,0 +1,19 @@
+// Launcher of the lane-per-layer FP64 fixed-step kernel (plain_lanes_f64.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "../../include/cmtj_gpu.h"
+
+namespace cmtjd {
+
+// Lanes per junction for a batch whose junctions have at most max_layers
+// layers (0 or out of range: CMTJ_MAX_LAYERS).
+int plain_lanes_group(int max_layers);
+
+// RK4, Euler-Heun or Heun over n_junctions junctions (arguments as
+// cmtj_run_simulation_f64, already checked).
+cudaError_t plain_lanes_launch(const cmtj_junction_t *d_junctions, int32_t n_junctions, cmtj_layer_t *d_layers,
+                               const double *d_tables, const cmtj_sim_params_t &p, double *d_log, uint32_t *d_status,
+                               cudaStream_t stream);
+
+}  // namespace cmtjd

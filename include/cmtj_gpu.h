@@ -189,6 +189,10 @@ typedef struct cmtj_sim_params {
   cmtj_constants_t c;
   double total_time, write_frequency;
   uint64_t max_attempts;     /* Dormand-Prince: step attempts before CMTJ_STATUS_LIMIT */
+  int32_t max_layers;        /* fixed step: an upper bound on n_layers over the
+                                batch (0: CMTJ_MAX_LAYERS); a junction with more
+                                layers gets CMTJ_STATUS_BAD_INPUT            */
+  int32_t reserved;
 } cmtj_sim_params_t;
 
 /* Log row layout (per junction, per row): for each layer l, either 3
