@@ -75,7 +75,7 @@ SIM_PARAMS_DTYPE = np.dtype(
     [("time_step", "<f8"), ("total_iterations", "<u4"), ("write_every", "<u4"), ("n_log", "<u4"),
      ("solver", "<i4"), ("calculate_energies", "<i4"), ("log_width", "<i4"),
      ("c", CONSTANTS_DTYPE), ("total_time", "<f8"), ("write_frequency", "<f8"), ("max_attempts", "<u8"),
-     ("max_layers", "<i4"), ("reserved", "<i4")],
+     ("max_layers", "<i4"), ("lanes_per_layer", "<i4")],
     align=True)
 
 # Order of cmtj_struct_sizes() output.

@@ -10,8 +10,23 @@
 namespace cmtjd {
 
 
+struct DriverCtx;
+
+// A 3-vector held whole by one lane.  The physics below is written once
+// for any vector type V with this interface (plain_lanes_f64.cu adds one
+// that spreads the components over lanes).
 struct D3 {
   double x, y, z;
+  static constexpr int kLanes = 1;  // lanes per layer
+  static __device__ __forceinline__ D3 zero();
+  static __device__ __forceinline__ D3 load(const double *p);
+  static __device__ __forceinline__ D3 make(double x, double y, double z);
+  static __device__ __forceinline__ D3 axial(const cmtj_layer_t &L, int s, double t, const DriverCtx &dc, uint32_t dyn);
+};
+
+template <class T>
+struct NoDeduce {
+  using type = T;
 };
 static __device__ __forceinline__ D3 d3(double x, double y, double z) {
   D3 r;
@@ -32,10 +47,12 @@ static __device__ __forceinline__ D3 cross(const D3 &a, const D3 &b) {
 }
 static __device__ __forceinline__ D3 load3(const double *p) { return d3(p[0], p[1], p[2]); }
 
-// CVector::normalize (cvector.hpp:185-192); pow(v, 2) is v*v.
-static __device__ __forceinline__ D3 normalized(const D3 &v) {
-  const double mag = sqrt(v.x * v.x + v.y * v.y + v.z * v.z);
-  if (mag != 0) return d3(v.x / mag, v.y / mag, v.z / mag);
+// CVector::normalize (cvector.hpp:185-192); pow(v, 2) is v*v, and
+// dot(v, v) forms x*x + y*y + z*z in that order.
+template <class V>
+static __device__ __forceinline__ V normalized(const V &v) {
+  const double mag = sqrt(dot(v, v));
+  if (mag != 0) return v / mag;
   return v;
 }
 
@@ -132,6 +149,13 @@ static __device__ __forceinline__ D3 axial_at(const cmtj_layer_t &L, int s, doub
   return d3(slot_at(L, s, time, dc, dyn), slot_at(L, s + 1, time, dc, dyn), slot_at(L, s + 2, time, dc, dyn));
 }
 
+__device__ __forceinline__ D3 D3::zero() { return zero3(); }
+__device__ __forceinline__ D3 D3::load(const double *p) { return load3(p); }
+__device__ __forceinline__ D3 D3::make(double x, double y, double z) { return d3(x, y, z); }
+__device__ __forceinline__ D3 D3::axial(const cmtj_layer_t &L, int s, double t, const DriverCtx &dc, uint32_t dyn) {
+  return axial_at(L, s, t, dc, dyn);
+}
+
 // Bit s set when driver slot s of L is time-dependent (not CMTJ_DRV_CONSTANT).
 static __device__ __forceinline__ uint32_t dynamic_slots(const cmtj_layer_t &L) {
   uint32_t m = 0;
@@ -142,31 +166,34 @@ static __device__ __forceinline__ uint32_t dynamic_slots(const cmtj_layer_t &L) 
 
 // Values the reference keeps on the Layer as side effects of the last field
 // evaluation and logs with calculateEnergies (junction.hpp:1589-1613).
-struct Side {
+template <class V>
+struct SideT {
   double K, K2, Jb, Jt, I;
-  D3 Hext, Hiec, Hanis, Hdemag, Hfl, Hdl;
+  V Hext, Hiec, Hanis, Hdemag, Hfl, Hdl;
 };
+using Side = SideT<D3>;
 
 // calculateHeff + solveLLG (junction.hpp:580-815, 855-864).
-static __device__ D3 rhs(const cmtj_layer_t &L, const cmtj_constants_t &c, double time, const D3 &m, const D3 &bottom,
-                  const D3 &top, const DriverCtx &dc, Side *side, const cmtj_driver_t *cur = nullptr,
-                  uint32_t dyn = 0xffffffffu) {
+template <class V>
+static __device__ V rhs(const cmtj_layer_t &L, const cmtj_constants_t &c, double time, const V &m, const V &bottom,
+                        const V &top, const DriverCtx &dc, typename NoDeduce<SideT<V>>::type *side,
+                        const cmtj_driver_t *cur = nullptr, uint32_t dyn = 0xffffffffu) {
   const double Ms = L.Ms;
   const uint32_t zt = L.zero_terms;
   // --- calculateHeff (580-622).  Terms the host marked identically zero
   // (CMTJ_ZERO_*), and IEC / IDMI against a zero neighbour vector, are left
   // out of the sum: adding an exact zero changes no value.
   const bool zb = is_zero3(bottom), ztop = is_zero3(top);
-  D3 Hdipole = zero3();
+  V Hdipole = V::zero();
   if (!(zt & CMTJ_ZERO_DIPOLE))
     Hdipole = tensor_mul(bottom, L.dipole_bottom, L.ms_over_mu0) + tensor_mul(top, L.dipole_top, L.ms_over_mu0);
-  const D3 Hext = axial_at(L, CMTJ_SLOT_HEXT, time, dc, dyn);
-  const D3 Hoe = axial_at(L, CMTJ_SLOT_HOE, time, dc, dyn);
-  const D3 Hdemag = tensor_mul(m, L.demag, L.ms_over_mu0);
+  const V Hext = V::axial(L, CMTJ_SLOT_HEXT, time, dc, dyn);
+  const V Hoe = V::axial(L, CMTJ_SLOT_HOE, time, dc, dyn);
+  const V Hdemag = tensor_mul(m, L.demag, L.ms_over_mu0);
   const double Jb = slot_at(L, CMTJ_SLOT_IEC_BOTTOM, time, dc, dyn);
   const double Jt = slot_at(L, CMTJ_SLOT_IEC_TOP, time, dc, dyn);
   const double Mst = Ms * L.thickness;
-  D3 Hiec = zero3();
+  V Hiec = V::zero();
   if (zt & CMTJ_ZERO_J2) {
     // Jx + 2*0*dot = Jx exactly
     if (!zb && !ztop) Hiec = (bottom * Jb) / Mst + (top * Jt) / Mst;
@@ -177,19 +204,19 @@ static __device__ D3 rhs(const cmtj_layer_t &L, const cmtj_constants_t &c, doubl
     const double J2t = slot_at(L, CMTJ_SLOT_IECQ_TOP, time, dc, dyn);
     Hiec = (bottom * (Jb + 2 * J2b * dot(bottom, m))) / Mst + (top * (Jt + 2 * J2t * dot(top, m))) / Mst;
   }
-  D3 Hidmi = zero3();
+  V Hidmi = V::zero();
   if (!(zt & CMTJ_ZERO_IDMI)) {
-    const D3 Db = axial_at(L, CMTJ_SLOT_IDMI_BOTTOM, time, dc, dyn);
-    const D3 Dt = axial_at(L, CMTJ_SLOT_IDMI_TOP, time, dc, dyn);
+    const V Db = V::axial(L, CMTJ_SLOT_IDMI_BOTTOM, time, dc, dyn);
+    const V Dt = V::axial(L, CMTJ_SLOT_IDMI_TOP, time, dc, dyn);
     Hidmi = smul(-1.0, cross(Db, bottom)) / Mst + smul(-1.0, cross(Dt, top)) / Mst;
   }
-  const D3 anis = load3(L.anis);
+  const V anis = V::load(L.anis);
   const double K = slot_at(L, CMTJ_SLOT_ANIS, time, dc, dyn);
-  const D3 Hanis = anis * ((2 * K) * dot(anis, m) / Ms);
-  const D3 Hdmi = axial_at(L, CMTJ_SLOT_HDMI, time, dc, dyn);
-  const D3 Hres = axial_at(L, CMTJ_SLOT_HRES, time, dc, dyn);
+  const V Hanis = anis * ((2 * K) * dot(anis, m) / Ms);
+  const V Hdmi = V::axial(L, CMTJ_SLOT_HDMI, time, dc, dyn);
+  const V Hres = V::axial(L, CMTJ_SLOT_HRES, time, dc, dyn);
   double K2 = 0.0;
-  D3 H = Hext + Hanis;
+  V H = Hext + Hanis;
   if (!(zt & CMTJ_ZERO_K2)) {
     K2 = slot_at(L, CMTJ_SLOT_ANIS2, time, dc, dyn);
     H = H + anis * ((4 * K2) * cube_rn(dot(anis, m)) / Ms);
@@ -212,12 +239,12 @@ static __device__ D3 rhs(const cmtj_layer_t &L, const cmtj_constants_t &c, doubl
   // --- solveLLG (716-815)
   const double GYRO = c.gyro;
   const double damping = L.damping;
-  const D3 prod = cross(m, H);
-  const D3 prod2 = cross(m, prod);
+  const V prod = cross(m, H);
+  const V prod2 = cross(m, prod);
   const double convTerm = L.conv_term;  // 1 / (1 + damping^2)
-  const D3 dmdt = prod + prod2 * damping;
-  D3 reference = zero3();
-  if (L.referenceType == CMTJ_REF_FIXED) reference = load3(L.ref);
+  const V dmdt = prod + prod2 * damping;
+  V reference = V::zero();
+  if (L.referenceType == CMTJ_REF_FIXED) reference = V::load(L.ref);
   else if (L.referenceType == CMTJ_REF_TOP) reference = top;
   else if (L.referenceType == CMTJ_REF_BOTTOM) reference = bottom;
   if (L.includeSTT) {
@@ -232,8 +259,8 @@ static __device__ D3 rhs(const cmtj_layer_t &L, const cmtj_constants_t &c, doubl
       eta = (L.spinPolarisation * slonSq) / (slonSq + 1 + (slonSq - 1) * dot(m, reference));
     }
     const double sttTerm = GYRO * aJ * eta;
-    const D3 fieldLike = cross(m, reference);
-    const D3 dampingLike = cross(m, fieldLike);
+    const V fieldLike = cross(m, reference);
+    const V dampingLike = cross(m, fieldLike);
     return (dmdt * -GYRO + dampingLike * -sttTerm * L.kappa + fieldLike * sttTerm * L.beta) * convTerm;
   } else if (L.includeSOT) {
     double Hdl = 0, Hfl = 0, Hdl2 = 0, Hfl2 = 0;
@@ -248,43 +275,45 @@ static __device__ D3 rhs(const cmtj_layer_t &L, const cmtj_constants_t &c, doubl
       Hdl = L.dampingLikeTorque * I;
       Hfl = L.fieldLikeTorque * I;
     }
-    const D3 ref2 = load3(L.ref2);
+    const V ref2 = V::load(L.ref2);
     if (side) {
       side->Hfl = reference * (Hfl - damping * Hdl);
       side->Hdl = reference * (Hdl + damping * Hfl);
     }
-    const D3 cm_p = cross(m, reference);
-    const D3 ccm_p = cross(m, cm_p);
-    const D3 cm_s = cross(m, ref2);
-    const D3 ccm_s = cross(m, cm_s);
-    const D3 flp = cm_p * (Hfl - damping * Hdl);
-    const D3 dlp = ccm_p * (Hdl + damping * Hfl);
-    const D3 fls = cm_s * (Hfl2 - damping * Hdl2);
-    const D3 dls = ccm_s * (Hdl2 + damping * Hfl2);
+    const V cm_p = cross(m, reference);
+    const V ccm_p = cross(m, cm_p);
+    const V cm_s = cross(m, ref2);
+    const V ccm_s = cross(m, cm_s);
+    const V flp = cm_p * (Hfl - damping * Hdl);
+    const V dlp = ccm_p * (Hdl + damping * Hfl);
+    const V fls = cm_s * (Hfl2 - damping * Hdl2);
+    const V dls = ccm_s * (Hdl2 + damping * Hfl2);
     return (dmdt + flp + dlp + fls + dls) * -GYRO * convTerm;
   }
   return dmdt * -GYRO * convTerm;
 }
 
 // stochasticTorque (junction.hpp:824-831).
-static __device__ __forceinline__ D3 stoch_torque(const cmtj_layer_t &L, const cmtj_constants_t &c, const D3 &m,
-                                           const D3 &dW) {
+template <class V>
+static __device__ __forceinline__ V stoch_torque(const cmtj_layer_t &L, const cmtj_constants_t &c, const V &m,
+                                                 const V &dW) {
   const double convTerm = L.stoch_conv;  // -gyro / (1 + damping^2)
-  const D3 th = cross(m, dW);
-  const D3 th2 = cross(m, th);
+  const V th = cross(m, dW);
+  const V th2 = cross(m, th);
   return (th + th2 * L.damping) * convTerm;
 }
 
 // getStochasticLangevinVector (junction.hpp:1111-1128).
-static __device__ __forceinline__ D3 langevin(const cmtj_layer_t &L, const cmtj_constants_t &c, double time,
+template <class V = D3>
+static __device__ __forceinline__ V langevin(const cmtj_layer_t &L, const cmtj_constants_t &c, double time,
                                        uint32_t i, const DriverCtx &dc, uint32_t dyn = 0xffffffffu) {
-  if (!L.temperatureSet) return zero3();
+  if (!L.temperatureSet) return V::zero();
   const double temp = slot_at(L, CMTJ_SLOT_TEMPERATURE, time, dc, dyn);
   const double mainFactor = (2 * L.damping * c.kB * temp) / (L.Ms * L.cellVolume * c.gyro);
   const double sigma = sqrt(mainFactor);
   double g0, g1, g2;
   cmtj_gaussian3_f64(L.seed_lo, L.seed_hi, L.noise_step + i, g0, g1, g2);
-  return d3(g0, g1, g2) * sigma;
+  return V::make(g0, g1, g2) * sigma;
 }
 
 

@@ -10,6 +10,10 @@ namespace cmtjd {
 // layers (0 or out of range: CMTJ_MAX_LAYERS).
 int plain_lanes_group(int max_layers);
 
+// Lanes per layer the launcher uses (1 or 4) for this batch on a GPU with
+// sm_count SMs.
+int plain_lanes_per_layer(const cmtj_sim_params_t &p, int32_t n_junctions, int sm_count);
+
 // RK4, Euler-Heun or Heun over n_junctions junctions (arguments as
 // cmtj_run_simulation_f64, already checked).
 cudaError_t plain_lanes_launch(const cmtj_junction_t *d_junctions, int32_t n_junctions, cmtj_layer_t *d_layers,

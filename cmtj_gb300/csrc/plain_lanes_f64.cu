@@ -1,24 +1,30 @@
-// FP64 plain form, fixed-step solvers (RK4, Euler-Heun, Heun): one lane per
-// layer.
+// FP64 plain form, fixed-step solvers (RK4, Euler-Heun, Heun): layers
+// side by side on lanes.
 //
 // The fixed-step runners of Junction::runSimulation (core/junction.hpp:
 // 1668-1815) step every layer of a junction from the magnetisations its
 // neighbours had at the start of the step (Heun's corrector: from their
 // predictions), so the layers of one step are independent of each other.
-// Here each layer runs on its own lane of a G-lane group (G = 1, 2, 4 or 8,
-// at least the junction's layer count); the neighbours come from the
-// adjacent lanes by warp shuffle, and every lane evaluates the expressions
-// of plain_f64.cuh in the same order as the one-thread Dormand-Prince
-// kernel does, so the results do not depend on the layout.  The serial
-// chain of a step is one layer's instead of n layers'.
+// Here each layer runs on its own lane (V = D3) or on its own quad of lanes,
+// one vector component per lane (V = C3, lane3.cuh), within a group of
+// G layer slots (G = 1, 2, 4 or 8, at least the junction's layer count).
+// The neighbours come from the adjacent layer slots by warp shuffle, and
+// every lane evaluates the expressions of plain_f64.cuh in the same order
+// as the one-thread Dormand-Prince kernel does, so the results do not
+// depend on the layout.  The serial chain of a step is one layer's instead
+// of n layers'.
 //
-// The chain is latency-bound (one warp per SM issues far below the FP64
-// pipe's rate), so a block is one warp of 32/G junctions and blocks spread
-// over the SMs.  Driver slots whose driver is constant are read directly
-// (slot mask per lane), and the four RK4 stages run as a rolled loop so the
-// field code is compiled once per kernel.
+// The chain is latency-bound: a warp FP64 instruction occupies the SM
+// sub-partition's FP64 unit for the same time with one active lane or 32,
+// so idle lanes cost nothing and the quad layout, with about 2.5x fewer
+// instructions per step, is the faster one until the batch fills the GPU.
+// A block is one warp; blocks spread over the SMs.  Driver slots whose
+// driver is constant are read directly (slot mask per lane), and the four
+// RK4 stages run as a rolled loop so the field code is compiled once per
+// kernel.
 //
 // This unit is compiled with --fmad=false like plain_f64.cu.
+#include "lane3.cuh"
 #include "plain_f64.cuh"
 #include "plain_lanes.h"
 
@@ -28,44 +34,45 @@ namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
 
-__device__ __forceinline__ D3 shfl3(const D3 &v, int src) {
-  return d3(__shfl_sync(kFull, v.x, src), __shfl_sync(kFull, v.y, src), __shfl_sync(kFull, v.z, src));
-}
-
 // The columns of one layer in a log row (logLayerParams, junction.hpp:
 // 1580-1636): the energy-log side values, then m.
-__device__ __forceinline__ void layer_cols(double *r, const Side &s, const D3 &m, bool energies) {
-  int col = 0;
+template <class V>
+__device__ __forceinline__ void layer_cols(double *r, const SideT<V> &s, const V &m, bool energies) {
+  double *mcol = r;
   if (energies) {
-    r[col++] = s.K;
-    r[col++] = s.K2;
-    r[col++] = s.Jb;
-    r[col++] = s.Jt;
-    r[col++] = s.I;
-    const D3 v[7] = {s.Hext, s.Hiec, s.Hanis, s.Hdemag, zero3(), s.Hfl, s.Hdl};
-#pragma unroll
-    for (int q = 0; q < 7; ++q) {
-      r[col++] = v[q].x;
-      r[col++] = v[q].y;
-      r[col++] = v[q].z;
+    if (scalar_owner(m)) {
+      r[0] = s.K;
+      r[1] = s.K2;
+      r[2] = s.Jb;
+      r[3] = s.Jt;
+      r[4] = s.I;
     }
+    store3(r + 5, s.Hext);
+    store3(r + 8, s.Hiec);
+    store3(r + 11, s.Hanis);
+    store3(r + 14, s.Hdemag);
+    store3(r + 17, V::zero());
+    store3(r + 20, s.Hfl);
+    store3(r + 23, s.Hdl);
+    mcol = r + 26;
   }
-  r[col++] = m.x;
-  r[col++] = m.y;
-  r[col] = m.z;
+  store3(mcol, m);
 }
 
-template <int SOLVER>
+template <int SOLVER, class V>
 __global__ void __launch_bounds__(32)
     k_plain_lanes(const cmtj_junction_t *__restrict__ junctions, int32_t n_junctions,
                   const cmtj_layer_t *__restrict__ params, cmtj_layer_t *layers, const double *__restrict__ tables,
                   cmtj_sim_params_t p, int G, double *__restrict__ log, uint32_t *__restrict__ status) {
   // `params` and `layers` address the same records: every field but mag is
   // read through `params`, mag is read and written through `layers` only.
+  constexpr int P = V::kLanes;  // lanes per layer
+  const int span = G * P;       // lanes per junction (<= 32)
   const int lane = threadIdx.x;
-  const int l = lane & (G - 1);
-  const int lead = lane - l;
-  const int j = blockIdx.x * (32 / G) + lane / G;
+  const int jl = lane % span;
+  const int l = jl / P;  // layer slot of this lane
+  const int lead = lane - jl;
+  const int j = blockIdx.x * (32 / span) + lane / span;
   const bool have = j < n_junctions;
   int n = 0;
   int64_t off = 0;
@@ -87,17 +94,17 @@ __global__ void __launch_bounds__(32)
   const bool energies = p.calculate_energies != 0;
   const cmtj_constants_t c = p.c;
   const int width = energies ? CMTJ_ENERGY_COLS : 3;
-  D3 mag = zero3();
+  V mag = V::zero();
   uint32_t dyn = 0;
-  Side side;
+  SideT<V> side;
   side.K = side.K2 = side.Jb = side.Jt = side.I = 0.0;
-  side.Hext = side.Hiec = side.Hanis = side.Hdemag = side.Hfl = side.Hdl = zero3();
+  side.Hext = side.Hiec = side.Hanis = side.Hdemag = side.Hfl = side.Hdl = V::zero();
   if (mine) {
-    mag = load3(layers[off + l].mag);
+    mag = V::load(layers[off + l].mag);
     dyn = dynamic_slots(L);
   }
-  const int below_src = lead + (l > 0 ? l - 1 : 0);
-  const int above_src = lead + (l + 1 < G ? l + 1 : l);
+  const int below_src = l > 0 ? lane - P : lane;
+  const int above_src = l + 1 < G ? lane + P : lane;
   double *out = have ? log + (size_t)j * p.n_log * p.log_width : nullptr;
   uint32_t row = 0;
 
@@ -106,34 +113,34 @@ __global__ void __launch_bounds__(32)
     const double t = (double)i * dt;
     const bool step = mine && run;
     // neighbours at the start of the step; zero beyond the stack's ends
-    D3 below = shfl3(mag, below_src), above = shfl3(mag, above_src);
-    if (l == 0) below = zero3();
-    if (l >= n - 1) above = zero3();
+    V below = shfl_vec(mag, below_src), above = shfl_vec(mag, above_src);
+    if (l == 0) below = V::zero();
+    if (l >= n - 1) above = V::zero();
 
     if (SOLVER == CMTJ_RK4) {
       // Layer::rk4_step (1017-1041); neighbours frozen for all four stages
       // (runMultiLayerSolver, 1680-1707)
-      D3 next = mag;
+      V next = mag;
       bool nan = false;
       if (step) {
-        D3 k = zero3(), acc = zero3();
+        V k = V::zero(), acc = V::zero();
 #pragma unroll 1
         for (int s = 0; s < 4; ++s) {
           const double ts = s == 0 ? t : (s == 3 ? t + dt : t + 0.5 * dt);
-          const D3 mi = s == 0 ? mag : (s == 3 ? mag + k : mag + k * 0.5);
+          const V mi = s == 0 ? mag : (s == 3 ? mag + k : mag + k * 0.5);
           const DriverCtx dc = {tables, i, s == 0 ? 0 : (s == 3 ? 2 : 1)};
           k = rhs(L, c, ts, mi, below, above, dc, (s == 3 && energies) ? &side : nullptr, nullptr, dyn) * dt;
           acc = s == 0 ? k : acc + (s == 3 ? k : k * 2.0);
         }
         next = normalized(mag + acc / 6.0);
-        nan = isnan(next.x);
+        nan = x_is_nan(next);
       }
       // rk4_step throws at the first layer whose m is NaN: the layers below
       // it keep this step's update, the layers above it do not
-      const unsigned group = (G == 32 ? kFull : ((1u << G) - 1u)) << lead;
+      const unsigned group = (span == 32 ? kFull : ((1u << span) - 1u)) << lead;
       const unsigned bad = __ballot_sync(kFull, nan) & group;
       if (bad) {
-        const int first = __ffs(bad) - 1 - lead;
+        const int first = (__ffs(bad) - 1 - lead) / P;
         if (step && l <= first) mag = next;
         if (run) code = CMTJ_STATUS_NAN;
         run = false;
@@ -144,31 +151,31 @@ __global__ void __launch_bounds__(32)
       // eulerHeunSolverStep (1709-1754)
       if (step) {
         const DriverCtx d0 = {tables, i, 0};
-        const D3 dW = langevin(L, c, t, i, d0, dyn);
-        const D3 f = rhs(L, c, t, mag, below, above, d0, energies ? &side : nullptr, nullptr, dyn);
-        const D3 g = stoch_torque(L, c, mag, dW);
-        const D3 mNext = mag + g * sqrt(dt);
-        const D3 g2 = stoch_torque(L, c, mNext, dW);
+        const V dW = langevin<V>(L, c, t, i, d0, dyn);
+        const V f = rhs(L, c, t, mag, below, above, d0, energies ? &side : nullptr, nullptr, dyn);
+        const V g = stoch_torque(L, c, mag, dW);
+        const V mNext = mag + g * sqrt(dt);
+        const V g2 = stoch_torque(L, c, mNext, dW);
         mag = normalized(mag + f * dt + smul(0.5, g + g2) * sqrt(dt));
       }
     } else {
       // heunSolverStep (1756-1815): the corrector sees the neighbours'
       // predictions
-      D3 fn = zero3(), gn = zero3(), dW = zero3(), pred = zero3();
+      V fn = V::zero(), gn = V::zero(), dW = V::zero(), pred = V::zero();
       if (step) {
         const DriverCtx d0 = {tables, i, 0};
         fn = rhs(L, c, t, mag, below, above, d0, nullptr, nullptr, dyn);
-        dW = langevin(L, c, t, i, d0, dyn);
+        dW = langevin<V>(L, c, t, i, d0, dyn);
         gn = stoch_torque(L, c, mag, dW);
         pred = mag + fn * dt + gn * sqrt(dt);
       }
-      D3 pb = shfl3(pred, below_src), pa = shfl3(pred, above_src);
-      if (l == 0) pb = zero3();
-      if (l >= n - 1) pa = zero3();
+      V pb = shfl_vec(pred, below_src), pa = shfl_vec(pred, above_src);
+      if (l == 0) pb = V::zero();
+      if (l >= n - 1) pa = V::zero();
       if (step) {
         const DriverCtx d2 = {tables, i, 2};
-        const D3 f2 = rhs(L, c, t + dt, pred, pb, pa, d2, energies ? &side : nullptr, nullptr, dyn);
-        const D3 g2 = stoch_torque(L, c, pred, dW);
+        const V f2 = rhs(L, c, t + dt, pred, pb, pa, d2, energies ? &side : nullptr, nullptr, dyn);
+        const V g2 = stoch_torque(L, c, pred, dW);
         mag = mag + smul(0.5 * dt, fn + f2) + smul(0.5, gn + g2) * sqrt(dt);
         mag = normalized(mag);
       }
@@ -176,32 +183,36 @@ __global__ void __launch_bounds__(32)
 
     if (!(i % p.write_every)) {
       // magnetoresistance (calculateMagnetoresistance 1865-1867,
-      // stripMagnetoResistance 1835-1857) from the layer lanes
-      const D3 m1 = shfl3(mag, lead + (G > 1 ? 1 : 0));
+      // stripMagnetoResistance 1835-1857) from the layer lanes; every lane
+      // takes part in the shuffles
+      const V m1 = shfl_vec(mag, l == 0 && G > 1 ? lane + P : lane);
+      const double cos01 = dot(mag, m1);
+      const double mx = comp_of(mag, 0), my = comp_of(mag, 1), mz = comp_of(mag, 2);
       double inv_x = 0.0, inv_y = 0.0;
       if (mine && mr_mode == CMTJ_MR_STRIP) {
         const cmtj_junction_t &J = junctions[j];
-        const double Rx = J.Rx0[l] + J.AMR_X[l] * (mag.x * mag.x) + J.SMR_X[l] * (mag.y * mag.y);
-        const double Ry = J.Ry0[l] + 0.5 * J.AHE[l] * mag.z + (J.AMR_Y[l] + J.SMR_Y[l]) * mag.x * mag.y;
+        const double Rx = J.Rx0[l] + J.AMR_X[l] * (mx * mx) + J.SMR_X[l] * (my * my);
+        const double Ry = J.Ry0[l] + 0.5 * J.AHE[l] * mz + (J.AMR_Y[l] + J.SMR_Y[l]) * mx * my;
         inv_x = 1. / Rx;
         inv_y = 1. / Ry;
       }
       double Rx_acc = 0.0, Ry_acc = 0.0;
       for (int q = 0; q < G; ++q) {
-        const double a = __shfl_sync(kFull, inv_x, lead + q), b = __shfl_sync(kFull, inv_y, lead + q);
+        const double a = __shfl_sync(kFull, inv_x, lead + q * P), b = __shfl_sync(kFull, inv_y, lead + q * P);
         if (q < n) {
           Rx_acc = Rx_acc + a;
           Ry_acc = Ry_acc + b;
         }
       }
+      const double cos_ref = (run && l == 0 && n == 1) ? dot(mag, V::load(L.ref)) : 0.0;
       if (run) {
         double *r = out + (size_t)row * p.log_width;
         if (mine) layer_cols(r + l * width, side, mag, energies);
-        if (l == 0) {
+        if (l == 0 && scalar_owner(mag)) {
           const cmtj_junction_t &J = junctions[j];
           double r0 = 0.0, r1 = 0.0;
           if (mr_mode == CMTJ_MR_CLASSIC) {
-            const double cosT = n == 1 ? dot(mag, load3(L.ref)) : dot(mag, m1);
+            const double cosT = n == 1 ? cos_ref : cos01;
             r0 = J.Rp + (((J.Rap - J.Rp) / 2.0) * (1.0 - cosT));
           } else if (mr_mode == CMTJ_MR_STRIP) {
             r0 = 1 / Rx_acc;
@@ -217,12 +228,8 @@ __global__ void __launch_bounds__(32)
       }
     }
   }
-  if (mine) {
-    layers[off + l].mag[0] = mag.x;
-    layers[off + l].mag[1] = mag.y;
-    layers[off + l].mag[2] = mag.z;
-  }
-  if (have && l == 0) {
+  if (mine) store3(layers[off + l].mag, mag);
+  if (have && jl == 0) {
     status[2 * j] = code;
     status[2 * j + 1] = row;
   }
@@ -239,21 +246,43 @@ int plain_lanes_group(int max_layers) {
   return CMTJ_MAX_LAYERS;
 }
 
+int plain_lanes_per_layer(const cmtj_sim_params_t &p, int32_t n_junctions, int sm_count) {
+  if (p.lanes_per_layer == 1 || p.lanes_per_layer == 4) return p.lanes_per_layer;
+  // quads while the batch holds at most two quad warps per SM sub-partition
+  const long long quad_warps = ((long long)n_junctions * plain_lanes_group(p.max_layers) * 4 + 31) / 32;
+  return quad_warps <= 2LL * 4 * sm_count ? 4 : 1;
+}
+
+template <class V>
+static void launch_solver(int solver, int blocks, cudaStream_t stream, const cmtj_junction_t *d_junctions,
+                          int32_t n_junctions, cmtj_layer_t *d_layers, const double *d_tables,
+                          const cmtj_sim_params_t &p, int G, double *d_log, uint32_t *d_status) {
+  if (solver == CMTJ_RK4)
+    k_plain_lanes<CMTJ_RK4, V><<<blocks, 32, 0, stream>>>(d_junctions, n_junctions, d_layers, d_layers, d_tables, p,
+                                                          G, d_log, d_status);
+  else if (solver == CMTJ_EULER_HEUN)
+    k_plain_lanes<CMTJ_EULER_HEUN, V><<<blocks, 32, 0, stream>>>(d_junctions, n_junctions, d_layers, d_layers,
+                                                                 d_tables, p, G, d_log, d_status);
+  else
+    k_plain_lanes<CMTJ_HEUN, V><<<blocks, 32, 0, stream>>>(d_junctions, n_junctions, d_layers, d_layers, d_tables, p,
+                                                           G, d_log, d_status);
+}
+
 cudaError_t plain_lanes_launch(const cmtj_junction_t *d_junctions, int32_t n_junctions, cmtj_layer_t *d_layers,
                                const double *d_tables, const cmtj_sim_params_t &p, double *d_log, uint32_t *d_status,
                                cudaStream_t stream) {
+  int dev = 0, sms = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return e;
   const int G = plain_lanes_group(p.max_layers);
-  const int per_block = 32 / G;
+  const int P = plain_lanes_per_layer(p, n_junctions, sms);
+  const int per_block = 32 / (G * P);
   const int blocks = (n_junctions + per_block - 1) / per_block;
-  if (p.solver == CMTJ_RK4)
-    k_plain_lanes<CMTJ_RK4><<<blocks, 32, 0, stream>>>(d_junctions, n_junctions, d_layers, d_layers, d_tables, p, G,
-                                                       d_log, d_status);
-  else if (p.solver == CMTJ_EULER_HEUN)
-    k_plain_lanes<CMTJ_EULER_HEUN><<<blocks, 32, 0, stream>>>(d_junctions, n_junctions, d_layers, d_layers, d_tables,
-                                                              p, G, d_log, d_status);
+  if (P == 4)
+    launch_solver<C3>(p.solver, blocks, stream, d_junctions, n_junctions, d_layers, d_tables, p, G, d_log, d_status);
   else
-    k_plain_lanes<CMTJ_HEUN><<<blocks, 32, 0, stream>>>(d_junctions, n_junctions, d_layers, d_layers, d_tables, p, G,
-                                                        d_log, d_status);
+    launch_solver<D3>(p.solver, blocks, stream, d_junctions, n_junctions, d_layers, d_tables, p, G, d_log, d_status);
   return cudaGetLastError();
 }
 

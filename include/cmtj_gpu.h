@@ -192,7 +192,10 @@ typedef struct cmtj_sim_params {
   int32_t max_layers;        /* fixed step: an upper bound on n_layers over the
                                 batch (0: CMTJ_MAX_LAYERS); a junction with more
                                 layers gets CMTJ_STATUS_BAD_INPUT            */
-  int32_t reserved;
+  int32_t lanes_per_layer;   /* fixed step: 1 (a layer per lane) or 4 (a layer's
+                                x, y, z on three lanes); 0: the library picks 4
+                                for batches up to two quad warps per SM
+                                sub-partition, else 1.  Results are the same. */
 } cmtj_sim_params_t;
 
 /* Log row layout (per junction, per row): for each layer l, either 3

@@ -54,3 +54,65 @@ def test_fp64_plain_batch_equals_single(gpu_lib):
     a, b = js[2].getLog(), solo.getLog()
     for k in b:
         assert a[k] == b[k], k
+
+
+def _force_lanes(monkeypatch, lanes):
+    """Lower with cmtj_sim_params_t.lanes_per_layer = lanes (1: a layer per
+    lane; 4: a layer's x, y, z on a quad of lanes)."""
+    from cmtj_gb300 import _lower
+    orig = _lower.make_params
+
+    def make_params(*a, **k):
+        p = orig(*a, **k)
+        p["lanes_per_layer"] = lanes
+        return p
+
+    monkeypatch.setattr(_lower, "make_params", make_params)
+
+
+FIXED_STEP = sorted(n for n in cases.DETERMINISTIC if not n.startswith("dp_"))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("lanes", [1, 4])
+@pytest.mark.parametrize("name", FIXED_STEP)
+def test_fp64_plain_both_layouts_match_reference(gpu_lib, monkeypatch, name, lanes):
+    _force_lanes(monkeypatch, lanes)
+    golden, gmags = load_golden(name)
+    _, log, mags = cases.run_case(cmtj_gb300, name)
+    _check(name, log, golden)
+    for lid, gm in gmags.items():
+        assert np.max(np.abs(np.asarray(mags[lid]) - gm)) <= TOL_M
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("solver", ["RK4", "EulerHeun", "Heun"])
+def test_fp64_plain_layouts_give_identical_bits(gpu_lib, monkeypatch, solver):
+    """One batch of 1- to 3-layer junctions (STT, SOT, strip and classic R,
+    time-dependent drivers, the energy log; seeded thermal noise for the
+    stochastic solvers): a layer per lane and a layer per quad of lanes give
+    the same bits in every log column and final m."""
+    from cmtj_gb300 import engine
+    mode = getattr(cmtj_gb300.SolverMode, solver)
+    names = ("mtj_rh_point", "sto", "sot_strip", "tri_layer", "energies_k2", "alt_stt_bottom", "drivers_zoo")
+    plan = engine.plan_run(3e-11, 1e-13, 2e-13)
+    runs = []
+    for lanes in (1, 4):
+        _force_lanes(monkeypatch, lanes)
+        js = []
+        for q, name in enumerate(names):
+            j, _ = cases.DETERMINISTIC[name](cmtj_gb300)
+            if solver != "RK4":
+                j.setLayerTemperatureDriver("all", cmtj_gb300.constantDriver(300.0))
+                for l, layer in enumerate(j.layers):
+                    layer.noise_seed = 7000 + 10 * q + l
+            js.append(j)
+        engine.run_junctions(js, plan, mode, calculate_energies=True)
+        runs.append(js)
+    for a, b in zip(*runs):
+        la, lb = a.getLogArrays(), b.getLogArrays()
+        assert set(la) == set(lb)
+        for k in la:
+            assert np.array_equal(la[k], lb[k]), k
+        for x, y in zip(a.layers, b.layers):
+            assert (x.mag.x, x.mag.y, x.mag.z) == (y.mag.x, y.mag.y, y.mag.z)
