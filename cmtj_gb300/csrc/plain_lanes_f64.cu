@@ -59,13 +59,14 @@ __device__ __forceinline__ void layer_cols(double *r, const SideT<V> &s, const V
   store3(mcol, m);
 }
 
-template <int SOLVER, class V>
-__global__ void __launch_bounds__(32)
-    k_plain_lanes(const cmtj_junction_t *__restrict__ junctions, int32_t n_junctions,
-                  const cmtj_layer_t *__restrict__ params, cmtj_layer_t *layers, const double *__restrict__ tables,
-                  cmtj_sim_params_t p, int G, double *__restrict__ log, uint32_t *__restrict__ status) {
-  // `params` and `layers` address the same records: every field but mag is
-  // read through `params`, mag is read and written through `layers` only.
+// The whole run of the warp's junctions.  DYN = false when no layer of the
+// warp has a time-dependent driver slot: every slot then reads its
+// constantValue, a loop invariant.
+template <int SOLVER, class V, bool DYN>
+__device__ __forceinline__ void run_lanes(const cmtj_junction_t *__restrict__ junctions, int32_t n_junctions,
+                                          const cmtj_layer_t *__restrict__ params, cmtj_layer_t *layers,
+                                          const double *__restrict__ tables, const cmtj_sim_params_t &p, int G,
+                                          double *__restrict__ log, uint32_t *__restrict__ status) {
   constexpr int P = V::kLanes;  // lanes per layer
   const int span = G * P;       // lanes per junction (<= 32)
   const int lane = threadIdx.x;
@@ -101,7 +102,7 @@ __global__ void __launch_bounds__(32)
   side.Hext = side.Hiec = side.Hanis = side.Hdemag = side.Hfl = side.Hdl = V::zero();
   if (mine) {
     mag = V::load(layers[off + l].mag);
-    dyn = dynamic_slots(L);
+    if (DYN) dyn = dynamic_slots(L);
   }
   const int below_src = l > 0 ? lane - P : lane;
   const int above_src = l + 1 < G ? lane + P : lane;
@@ -233,6 +234,28 @@ __global__ void __launch_bounds__(32)
     status[2 * j] = code;
     status[2 * j + 1] = row;
   }
+}
+
+template <int SOLVER, class V>
+__global__ void __launch_bounds__(32)
+    k_plain_lanes(const cmtj_junction_t *__restrict__ junctions, int32_t n_junctions,
+                  const cmtj_layer_t *__restrict__ params, cmtj_layer_t *layers, const double *__restrict__ tables,
+                  cmtj_sim_params_t p, int G, double *__restrict__ log, uint32_t *__restrict__ status) {
+  // `params` and `layers` address the same records: every field but mag is
+  // read through `params`, mag is read and written through `layers` only.
+  const int span = G * V::kLanes;
+  const int lane = threadIdx.x;
+  const int l = (lane % span) / V::kLanes;
+  const int j = blockIdx.x * (32 / span) + lane / span;
+  bool varying = false;
+  if (j < n_junctions) {
+    const int n = junctions[j].n_layers;
+    if (l < n && n <= G) varying = dynamic_slots(params[junctions[j].layer_offset + l]) != 0u;
+  }
+  if (__any_sync(kFull, varying))
+    run_lanes<SOLVER, V, true>(junctions, n_junctions, params, layers, tables, p, G, log, status);
+  else
+    run_lanes<SOLVER, V, false>(junctions, n_junctions, params, layers, tables, p, G, log, status);
 }
 
 }  // namespace

@@ -13,6 +13,14 @@ warm-up), and prints one JSON line per candidate plus the best.
 
 The default build uses the CMTJ_BATCH_MINB and CMTJ_BATCH_MINB_PACKED
 defaults in csrc/batch_f32.cuh.
+
+With --fp64 it times the FP64 plain form's fixed-step kernel instead, on
+the R(H) sweep of the 2-layer MTJ (Hx over +-800 kA/m, RK4, R logged every
+step), for each batch size in --n and each lane layout in --lanes (1: a
+layer per lane, 4: a layer's x, y, z on a quad of lanes, 0: the library's
+own pick), one JSON line each:
+
+    python -m cmtj_gb300.tune --fp64 [--n 1 64 1024 16384] [--lanes 0 1 4] [--steps 2000]
 """
 import argparse
 import json
@@ -94,6 +102,67 @@ def time_library(lib, n_h, n_draw, steps, reps, workload="pimm"):
             "layer_steps_per_s": layer_steps / (best / 1e3), "all_ok": bool(np.all(st["status"] == 0))}
 
 
+def rh_junctions(n, total):
+    """n 2-layer MTJs of the R(H) sweep: free Ms 1.2 T, Ku 3e5 J/m^3,
+    t 1.5 nm; reference Ms 1.5 T, Ku 1e6 J/m^3, t 2 nm; both along z,
+    alpha 0.01, demag diag(0.0024, 0.0024, 0.9952), surface 1e-16 m^2,
+    IEC J = -5e-5 J/m^2, Rp 100, Rap 200, m along +z; Hx evenly over
+    +-800 kA/m."""
+    import numpy as np
+    from . import core
+    V = core.CVector
+    demag = [V(0.0024, 0, 0), V(0, 0.0024, 0), V(0, 0, 0.9952)]
+    js = []
+    for h in np.linspace(-800e3, 800e3, n):
+        free = core.Layer("free", mag=V(0, 0, 1), anis=V(0, 0, 1), Ms=1.2, thickness=1.5e-9, cellSurface=1e-16,
+                          demagTensor=demag, damping=0.01)
+        ref = core.Layer("ref", mag=V(0, 0, 1), anis=V(0, 0, 1), Ms=1.5, thickness=2e-9, cellSurface=1e-16,
+                         demagTensor=demag, damping=0.01)
+        j = core.Junction([free, ref], 100, 200)
+        j.setLayerAnisotropyDriver("free", core.constantDriver(3e5))
+        j.setLayerAnisotropyDriver("ref", core.constantDriver(1e6))
+        j.setIECDriver("free", "ref", core.constantDriver(-5e-5))
+        j.setLayerExternalFieldDriver("all", core.AxialDriver(float(h), 0, 0))
+        js.append(j)
+    return js
+
+
+def time_fp64(n, steps, reps, lanes, dt=1e-13):
+    """Best-of-`reps` CUDA-event time of one cmtj_run_simulation_f64 launch
+    (after one warm-up launch) on the R(H) batch of n junctions."""
+    import numpy as np
+    import torch
+    from . import _abi, engine
+    from ._lower import lower, plan_run
+    from .core import SolverMode
+    plan = plan_run(steps * dt, dt, dt).for_solver(SolverMode.RK4)
+    low = lower(rh_junctions(n, steps * dt), plan, SolverMode.RK4, False)
+    low.params["lanes_per_layer"] = lanes
+    lib = engine.require_gpu()
+    d_j, d_l0 = engine.to_device(low.junctions), engine.to_device(low.layers)
+    d_log = torch.empty((n, int(low.params["n_log"][0]), low.log_width), dtype=torch.float64, device="cuda")
+    d_st = torch.zeros(2 * n, dtype=torch.int32, device="cuda")
+    times = []
+    for k in range(reps + 1):
+        d_l = d_l0.clone()
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record()
+        rc = lib.cmtj_run_simulation_f64(engine.ptr(d_j), n, engine.ptr(d_l), None, low.params.ctypes.data,
+                                         engine.ptr(d_log), engine.ptr(d_st), engine.stream_ptr())
+        b.record()
+        _abi.check(rc, lib)
+        torch.cuda.synchronize()
+        if k:
+            times.append(a.elapsed_time(b))
+    st = d_st.cpu().numpy().view(np.uint32)
+    best = min(times)
+    return {"workload": "fp64_rh", "n": n, "lanes_per_layer": lanes, "steps": steps, "ms": times, "best_ms": best,
+            "us_per_step": best * 1e3 / steps, "layer_steps_per_s": n * steps * 2 / (best / 1e3),
+            "all_ok": bool(np.all(st[0::2] == 0) and np.all(st[1::2] == steps))}
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--minb", type=int, nargs="+", default=[4, 5, 6])
@@ -103,8 +172,17 @@ def main(argv=None):
     ap.add_argument("--n-draw", type=int, default=512)
     ap.add_argument("--reps", type=int, default=3)
     ap.add_argument("--workload", default="pimm", choices=["pimm", "vsd"])
+    ap.add_argument("--fp64", action="store_true", help="time the FP64 fixed-step lane layouts instead")
+    ap.add_argument("--n", type=int, nargs="+", default=[1, 64, 1024, 16384], help="--fp64 batch sizes")
+    ap.add_argument("--lanes", type=int, nargs="+", default=[0, 1, 4], help="--fp64 lanes per layer")
     ap.add_argument("--time-lib", help=argparse.SUPPRESS)
     a = ap.parse_args(argv)
+    if a.fp64:
+        B.build()
+        for n in a.n:
+            for lanes in a.lanes:
+                print(json.dumps(time_fp64(n, a.steps, a.reps, lanes)), flush=True)
+        return
     if a.time_lib:
         print(json.dumps(time_library(a.time_lib, a.n_h, a.n_draw, a.steps, a.reps, a.workload)), flush=True)
         return
