@@ -234,7 +234,16 @@ def cpu_baseline(budget_s=15.0):
     el = time.perf_counter() - t0
     rate = n2 * n_steps * 2 / el
     ref_fpls, fcount = flops_per_layer_step()
-    return {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+    # the R(H) sweep in full (64 fields x 10 ns, 100,000 RK4 steps, m and R
+    # logged every step), one solve per task on all host cores
+    from cmtj_gb300 import tune
+    js = tune.rh_junctions(64, 1e-8)
+    t0 = time.perf_counter()
+    oracle_harness.run_oracle(js, 1e-8, DT, DT, threads=cores)
+    rh_el = time.perf_counter() - t0
+    rh = {"seconds": rh_el, "cores": cores, "layer_steps_per_s": 64 * 100_000 * 2 / rh_el,
+          "mean_R_last_2ns": [float(np.mean(j.getLogArrays()["R_free_ref"][-20_000:])) for j in js]}
+    return {"value": rate, "unit": UNIT, "cores": cores, "kind": "port", "rh_config0": rh,
             "reference_flop_per_layer_step": ref_fpls, "reference_flop_breakdown": fcount,
             "sample": "%d PIMM junctions x %d RK4 steps (full 5 ns solves) on %d threads (%.1f s)"
                       % (n2, n_steps, cores, el)}
@@ -526,6 +535,11 @@ def measure_rest(run, low, spec, n_steps, kern_ms, fft_ms, lib):
     out["serving"] = serving_leg(fp64_batch)
     out["other_workloads"] = other_workloads()
     out["cpu_baseline"] = cpu_baseline()
+    rh_cpu = out["cpu_baseline"].pop("rh_config0")
+    rh_gpu = out["other_workloads"]["rh_config0_fp64"]
+    rh_gpu["cpu_oracle"] = {k: v for k, v in rh_cpu.items() if k != "mean_R_last_2ns"}
+    rh_gpu["max_abs_dR_mean_vs_cpu_ohm"] = float(np.max(np.abs(np.array(rh_gpu.pop("mean_R_last_2ns")) -
+                                                               np.array(rh_cpu["mean_R_last_2ns"]))))
     # the reference's own arithmetic per layer-step, counted in the CPU leg
     out["roofline"]["reference_flop_per_layer_step"] = out["cpu_baseline"].pop("reference_flop_per_layer_step")
     out["roofline"]["reference_flop_breakdown_add_mul_div_sqrt_trans"] = out["cpu_baseline"].pop(
@@ -611,6 +625,26 @@ def other_workloads():
                           "max_abs_dR_mean_ohm": float(np.max(np.abs(r32 - r64))),
                           "sample": "64 fields x 10,000 steps, R logged every step, mean over the last 2,000"}
     del run
+    # The R(H) sweep in full on the FP64 plain form: 64 fields x 10 ns
+    # (100,000 RK4 steps), m and R logged every step.  Kernel time alone
+    # (CUDA events, best of one after a warm-up launch), and end to end
+    # through the public API (lowering, copies, the 512 MB log back, log
+    # columns per junction)
+    from cmtj_gb300 import tune
+    k = tune.time_fp64(64, 100_000, 1, 0)
+    js = tune.rh_junctions(64, 1e-8)
+    plan = engine.plan_run(1e-8, DT, DT)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    engine.run_junctions(js, plan, batch.SolverMode.RK4)
+    torch.cuda.synchronize()
+    el = time.perf_counter() - t0
+    out["rh_config0_fp64"] = {"kernel_s": k["best_ms"] / 1e3, "e2e_s": el, "us_per_step": k["us_per_step"],
+                              "layer_steps_per_s_kernel": k["layer_steps_per_s"], "all_ok": k["all_ok"],
+                              "mean_R_last_2ns": [float(np.mean(j.getLogArrays()["R_free_ref"][-20_000:]))
+                                                  for j in js],
+                              "sample": "64 fields x 100,000 RK4 steps, log every step"}
+    del js
     # 16-junction series stack, FP64 plain form
     js = [cases._stt_junction(cm, 1.0 + 0.02 * k, 1e3 + 50 * k, (0.1, 0.2, 1), (1, 0, 0)) for k in range(16)]
     s = cm.stack.SeriesStack(js)
