@@ -212,6 +212,42 @@ def spec_to_junctions(spec):
     return out
 
 
+def dp_junctions(cm, n=4096):
+    """n single free layers (Ms 1.2 T, Ku 3e5 J/m^3 along z, t 1.5 nm,
+    alpha 0.01, demag diag(0.0024, 0.0024, 0.9952), m tilted 0.1 from z)
+    driven by a 5 kA/m Oersted sine along x at 2-12 GHz."""
+    V = cm.CVector
+    demag = [V(0.0024, 0, 0), V(0, 0.0024, 0), V(0, 0, 0.9952)]
+    js = []
+    for k in range(n):
+        f = 2e9 + 10e9 * k / max(n - 1, 1)
+        layer = cm.Layer("free", mag=V(0.1, 0, 0.995), anis=V(0, 0, 1), Ms=1.2, thickness=1.5e-9,
+                         cellSurface=1e-16, demagTensor=demag, damping=0.01)
+        j = cm.Junction([layer])
+        j.setLayerAnisotropyDriver("free", cm.constantDriver(3e5))
+        j.setLayerOerstedFieldDriver("free", cm.AxialDriver(cm.sineDriver(0, 5e3, f, 0), cm.NullDriver(),
+                                                            cm.NullDriver()))
+        js.append(j)
+    return js
+
+
+def groups_16(cm, n_groups=64):
+    """n_groups GroupInteractions of 16 single-layer junctions each on a
+    4 x 4 grid at 60 nm pitch, Kanao et al. dipole coupling (the module's
+    default), initial m varied over junctions and groups."""
+    import group_cases
+    out = []
+    for q in range(n_groups):
+        js = [group_cases._single(cm, (0.1 + 0.01 * k, 0.2 - 0.002 * q, 0.97)) for k in range(16)]
+        pos = [cm.CVector(60e-9 * (k % 4), 60e-9 * (k // 4), 0) for k in range(16)]
+        out.append(cm.reservoir.GroupInteraction(pos, js))
+    return out
+
+
+def final_m(junctions):
+    return np.array([[(l.mag.x, l.mag.y, l.mag.z) for l in j.layers] for j in junctions])
+
+
 def cpu_baseline(budget_s=15.0):
     """The oracle (the reference's arithmetic, bit-identical on the pinned
     cases) on all host cores: a pilot of whole 5 ns PIMM solves on 2
@@ -243,7 +279,18 @@ def cpu_baseline(budget_s=15.0):
     rh_el = time.perf_counter() - t0
     rh = {"seconds": rh_el, "cores": cores, "layer_steps_per_s": 64 * 100_000 * 2 / rh_el,
           "mean_R_last_2ns": [float(np.mean(j.getLogArrays()["R_free_ref"][-20_000:])) for j in js]}
-    return {"value": rate, "unit": UNIT, "cores": cores, "kind": "port", "rh_config0": rh,
+    # Dormand-Prince and a dipole-coupled group, the same runs as the GPU legs
+    ocm = oracle_harness.oracle_module()
+    js = dp_junctions(ocm)
+    t0 = time.perf_counter()
+    oracle_harness.run_oracle(js, 5e-9, DT, 1e-11, solverMode=ocm.SolverMode.DormandPrince, threads=cores)
+    dp = {"seconds": time.perf_counter() - t0, "cores": cores, "final_m": final_m(js)}
+    gs = groups_16(ocm)
+    t0 = time.perf_counter()
+    oracle_harness.run_groups_oracle(gs, 2e-10, DT, 1e-12)
+    grp = {"seconds": time.perf_counter() - t0, "cores": 1,
+           "final_m": np.concatenate([final_m(g.junctionList) for g in gs])}
+    return {"value": rate, "unit": UNIT, "cores": cores, "kind": "port", "rh_config0": rh, "dp": dp, "group": grp,
             "reference_flop_per_layer_step": ref_fpls, "reference_flop_breakdown": fcount,
             "sample": "%d PIMM junctions x %d RK4 steps (full 5 ns solves) on %d threads (%.1f s)"
                       % (n2, n_steps, cores, el)}
@@ -540,6 +587,11 @@ def measure_rest(run, low, spec, n_steps, kern_ms, fft_ms, lib):
     rh_gpu["cpu_oracle"] = {k: v for k, v in rh_cpu.items() if k != "mean_R_last_2ns"}
     rh_gpu["max_abs_dR_mean_vs_cpu_ohm"] = float(np.max(np.abs(np.array(rh_gpu.pop("mean_R_last_2ns")) -
                                                                np.array(rh_cpu["mean_R_last_2ns"]))))
+    for key, leg in (("dp", "dormand_prince_fmr_4096"), ("group", "groups_dipole_64x16")):
+        cpu = out["cpu_baseline"].pop(key)
+        gpu = out["other_workloads"][leg]
+        gpu["max_abs_dm_vs_oracle"] = float(np.max(np.abs(gpu.pop("final_m") - cpu.pop("final_m"))))
+        gpu["cpu_oracle"] = cpu
     # the reference's own arithmetic per layer-step, counted in the CPU leg
     out["roofline"]["reference_flop_per_layer_step"] = out["cpu_baseline"].pop("reference_flop_per_layer_step")
     out["roofline"]["reference_flop_breakdown_add_mul_div_sqrt_trans"] = out["cpu_baseline"].pop(
@@ -645,6 +697,30 @@ def other_workloads():
                                                   for j in js],
                               "sample": "64 fields x 100,000 RK4 steps, log every step"}
     del js
+    # Dormand-Prince: 4096 sine-driven free layers, 5 ns, adaptive steps
+    js = dp_junctions(cm)
+    plan = engine.plan_run(5e-9, DT, 1e-11)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    engine.run_junctions(js, plan, cm.SolverMode.DormandPrince)
+    torch.cuda.synchronize()
+    out["dormand_prince_fmr_4096"] = {"seconds": time.perf_counter() - t0, "final_m": final_m(js),
+                                      "rows_logged": int(js[0].logLength),
+                                      "sample": "4096 free layers under a 2-12 GHz Oersted sine, 5 ns, FP64 "
+                                                "plain form, one launch"}
+    # dipole-coupled groups (cmtj.reservoir.GroupInteraction): 64 groups of
+    # 16 junctions, 2000 steps, one launch
+    from cmtj_gb300 import reservoir
+    gs = groups_16(cm)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    reservoir.run_groups(gs, 2e-10, DT, 1e-12)
+    torch.cuda.synchronize()
+    el = time.perf_counter() - t0
+    out["groups_dipole_64x16"] = {"seconds": el, "layer_steps_per_s": 64 * 16 * 2000 / el,
+                                  "final_m": np.concatenate([final_m(g.junctionList) for g in gs]),
+                                  "sample": "64 groups of 16 junctions on a 4x4 grid, Kanao dipole coupling, "
+                                            "2000 RK4 steps, FP64 plain form, one CTA per group"}
     # 16-junction series stack, FP64 plain form
     js = [cases._stt_junction(cm, 1.0 + 0.02 * k, 1e3 + 50 * k, (0.1, 0.2, 1), (1, 0, 0)) for k in range(16)]
     s = cm.stack.SeriesStack(js)
@@ -669,11 +745,12 @@ def serving_leg(fp64_rate, n_requests=200, rate_hz=200.0):
     continuous batching (cmtj_gb300.serving).  Latency = completion minus
     arrival, wall clock."""
     from cmtj_gb300 import serving
+    f64_fraction = 0.05
     fifo = serving.ServingEngine(hbm_budget_bytes=8 << 30, chunk_steps=4000, policy="fifo")
     t0 = time.perf_counter()
-    done_fifo = fifo.run(serving.make_trace(n_requests, rate_hz=rate_hz, seed=3))
+    done_fifo = fifo.run(serving.make_trace(n_requests, rate_hz=rate_hz, seed=3, f64_fraction=f64_fraction))
     fifo_summary = serving.summary(done_fifo, time.perf_counter() - t0)
-    reqs = serving.make_trace(n_requests, rate_hz=rate_hz, seed=3)
+    reqs = serving.make_trace(n_requests, rate_hz=rate_hz, seed=3, f64_fraction=f64_fraction)
     eng = serving.ServingEngine(hbm_budget_bytes=8 << 30, chunk_steps=4000, policy="sjf")
     t0 = time.perf_counter()
     done = eng.run(reqs)
@@ -681,9 +758,14 @@ def serving_leg(fp64_rate, n_requests=200, rate_hz=200.0):
     out = serving.summary(done, wall)
     out["policy"] = "sjf: smallest layer-steps first among arrived requests"
     out["fifo"] = {k: fifo_summary[k] for k in ("p50_ms", "p99_ms", "layer_steps_per_s", "wall_s")}
+    lat64 = [r.latency for r in done if r.precision == "f64"]
+    if lat64:
+        out["fp64_requests"] = {"count": len(lat64), "p50_ms": float(np.percentile(lat64, 50) * 1e3),
+                                "p99_ms": float(np.percentile(lat64, 99) * 1e3),
+                                "each": "64 two-layer MTJs, 2 ns RK4 (20,000 steps), FP64 plain form"}
     offered = sum(r.layer_steps for r in done)
-    out.update({"trace": "%d requests, Poisson %.0f req/s, 64-16384 solves, 2-40 ns, pimm/pbit/vsd mix"
-                         % (n_requests, rate_hz),
+    out.update({"trace": "%d requests, Poisson %.0f req/s, 64-16384 solves, 2-40 ns, pimm/pbit/vsd mix, "
+                         "%.0f%% of requests FP64 plain" % (n_requests, rate_hz, 100 * f64_fraction),
                 "offered_layer_steps": offered,
                 "offered_over_span": offered / max(done[-1].arrival, 1e-9),
                 "ticks": eng.stats["ticks"], "host_s": eng.stats["host_s"],

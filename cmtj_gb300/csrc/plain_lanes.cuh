@@ -1,0 +1,202 @@
+// Device building blocks of the FP64 fixed-step runners with a junction's
+// layers side by side on lanes (plain_lanes_f64.cu, stack_f64.cu).
+//
+// A junction holds `span` = G * P consecutive lanes of one warp: G layer
+// slots (at least its layer count) of P lanes each (P = 1 for D3, 4 for C3).
+// Every function here is called by every lane of the warp, in uniform
+// control flow: the warp shuffles and ballots below name the whole warp.
+// Lanes that have nothing to compute pass step = false.
+#pragma once
+#include "lane3.cuh"
+#include "plain_f64.cuh"
+
+namespace cmtjd {
+
+constexpr unsigned kWarpAll = 0xffffffffu;
+
+struct LaneGeo {
+  int lane;       // lane in the warp
+  int jl;         // lane within the junction's span
+  int l;          // layer slot of this lane
+  int lead;       // warp lane of the junction's first lane
+  int span;       // lanes per junction
+  int below_src;  // lane holding the same component of layer l - 1
+  int above_src;  // ... of layer l + 1
+  unsigned group; // the junction's lanes
+};
+
+template <class V>
+__device__ __forceinline__ LaneGeo lane_geo(int G) {
+  constexpr int P = V::kLanes;
+  LaneGeo g;
+  g.span = G * P;
+  g.lane = threadIdx.x & 31;
+  g.jl = g.lane % g.span;
+  g.l = g.jl / P;
+  g.lead = g.lane - g.jl;
+  g.below_src = g.l > 0 ? g.lane - P : g.lane;
+  g.above_src = g.l + 1 < G ? g.lane + P : g.lane;
+  g.group = (g.span == 32 ? kWarpAll : ((1u << g.span) - 1u)) << g.lead;
+  return g;
+}
+
+// One iteration of the fixed-step runner (RK4, Euler-Heun or Heun;
+// core/junction.hpp:1668-1815) for the lane's layer of a junction whose
+// n layers step (1 under runSingleLayerSolver).  cur overrides the current
+// driver (stacks).  Returns the first layer whose m became NaN (RK4: the
+// layers above it keep their start-of-step m, as when rk4_step throws), or
+// -1.
+template <int SOLVER, class V>
+__device__ __forceinline__ int lane_step(const cmtj_layer_t &L, const cmtj_constants_t &c, V &mag,
+                                         SideT<V> &side, bool step, const LaneGeo &g, int n, uint32_t i, double t,
+                                         double dt, const double *tables, bool energies,
+                                         const cmtj_driver_t *cur, uint32_t dyn) {
+  // neighbours at the start of the step; zero beyond the stack's ends
+  V below = shfl_vec(mag, g.below_src), above = shfl_vec(mag, g.above_src);
+  if (g.l == 0) below = V::zero();
+  if (g.l >= n - 1) above = V::zero();
+  if (SOLVER == CMTJ_RK4) {
+    // Layer::rk4_step (1017-1041); neighbours frozen for all four stages
+    // (runMultiLayerSolver, 1680-1707)
+    V next = mag;
+    bool nan = false;
+    if (step) {
+      V k = V::zero(), acc = V::zero();
+#pragma unroll 1
+      for (int s = 0; s < 4; ++s) {
+        const double ts = s == 0 ? t : (s == 3 ? t + dt : t + 0.5 * dt);
+        const V mi = s == 0 ? mag : (s == 3 ? mag + k : mag + k * 0.5);
+        const DriverCtx dc = {tables, i, s == 0 ? 0 : (s == 3 ? 2 : 1)};
+        k = rhs(L, c, ts, mi, below, above, dc, (s == 3 && energies) ? &side : nullptr, cur, dyn) * dt;
+        acc = s == 0 ? k : acc + (s == 3 ? k : k * 2.0);
+      }
+      next = normalized(mag + acc / 6.0);
+      nan = x_is_nan(next);
+    }
+    const unsigned bad = __ballot_sync(kWarpAll, nan) & g.group;
+    if (bad) {
+      const int first = (__ffs(bad) - 1 - g.lead) / V::kLanes;
+      if (step && g.l <= first) mag = next;
+      return first;
+    }
+    if (step) mag = next;
+  } else if (SOLVER == CMTJ_EULER_HEUN) {
+    // eulerHeunSolverStep (1709-1754)
+    if (step) {
+      const DriverCtx d0 = {tables, i, 0};
+      const V dW = langevin<V>(L, c, t, i, d0, dyn);
+      const V f = rhs(L, c, t, mag, below, above, d0, energies ? &side : nullptr, cur, dyn);
+      const V gt = stoch_torque(L, c, mag, dW);
+      const V mNext = mag + gt * sqrt(dt);
+      const V g2 = stoch_torque(L, c, mNext, dW);
+      mag = normalized(mag + f * dt + smul(0.5, gt + g2) * sqrt(dt));
+    }
+  } else {
+    // heunSolverStep (1756-1815): the corrector sees the neighbours'
+    // predictions
+    V fn = V::zero(), gn = V::zero(), dW = V::zero(), pred = V::zero();
+    if (step) {
+      const DriverCtx d0 = {tables, i, 0};
+      fn = rhs(L, c, t, mag, below, above, d0, nullptr, cur, dyn);
+      dW = langevin<V>(L, c, t, i, d0, dyn);
+      gn = stoch_torque(L, c, mag, dW);
+      pred = mag + fn * dt + gn * sqrt(dt);
+    }
+    V pb = shfl_vec(pred, g.below_src), pa = shfl_vec(pred, g.above_src);
+    if (g.l == 0) pb = V::zero();
+    if (g.l >= n - 1) pa = V::zero();
+    if (step) {
+      const DriverCtx d2 = {tables, i, 2};
+      const V f2 = rhs(L, c, t + dt, pred, pb, pa, d2, energies ? &side : nullptr, cur, dyn);
+      const V g2 = stoch_torque(L, c, pred, dW);
+      mag = mag + smul(0.5 * dt, fn + f2) + smul(0.5, gn + g2) * sqrt(dt);
+      mag = normalized(mag);
+    }
+  }
+  return -1;
+}
+
+// The columns of one layer in a log row (logLayerParams, junction.hpp:
+// 1580-1636): the energy-log side values, then m.
+template <class V>
+__device__ __forceinline__ void layer_cols(double *r, const SideT<V> &s, const V &m, bool energies) {
+  double *mcol = r;
+  if (energies) {
+    if (scalar_owner(m)) {
+      r[0] = s.K;
+      r[1] = s.K2;
+      r[2] = s.Jb;
+      r[3] = s.Jt;
+      r[4] = s.I;
+    }
+    store3(r + 5, s.Hext);
+    store3(r + 8, s.Hiec);
+    store3(r + 11, s.Hanis);
+    store3(r + 14, s.Hdemag);
+    store3(r + 17, V::zero());
+    store3(r + 20, s.Hfl);
+    store3(r + 23, s.Hdl);
+    mcol = r + 26;
+  }
+  store3(mcol, m);
+}
+
+// cos of the angle the CLASSIC magnetoresistance uses (calculate-
+// Magnetoresistance 1865-1867): m0 . ref for one layer, m0 . m1 otherwise;
+// valid on the lanes of layer 0.
+template <class V>
+__device__ __forceinline__ double classic_cos(const cmtj_layer_t &L, const V &mag, const LaneGeo &g, int n, int G,
+                                              bool layer0) {
+  const V m1 = shfl_vec(mag, g.l == 0 && G > 1 ? g.lane + V::kLanes : g.lane);
+  const double c01 = dot(mag, m1);
+  const double cref = (layer0 && n == 1) ? dot(mag, V::load(L.ref)) : 0.0;
+  return n == 1 ? cref : c01;
+}
+
+// One log row of the junction (logLayerParams, junction.hpp:1580-1636, and
+// the R columns of stripMagnetoResistance 1835-1857).  write: the junction
+// logs this step (the same on all its lanes); mine: the lane holds a layer.
+template <class V>
+__device__ __forceinline__ void lane_log_row(double *r, bool write, bool mine, const cmtj_junction_t *junctions,
+                                             int j, const cmtj_layer_t &L, const V &mag, const SideT<V> &side,
+                                             const LaneGeo &g, int n, int G, int mr_mode, bool energies, double t) {
+  const int width = energies ? CMTJ_ENERGY_COLS : 3;
+  const double cosT = classic_cos(L, mag, g, n, G, write && g.l == 0);
+  const double mx = comp_of(mag, 0), my = comp_of(mag, 1), mz = comp_of(mag, 2);
+  double inv_x = 0.0, inv_y = 0.0;
+  if (write && mine && mr_mode == CMTJ_MR_STRIP) {
+    const cmtj_junction_t &J = junctions[j];
+    const double Rx = J.Rx0[g.l] + J.AMR_X[g.l] * (mx * mx) + J.SMR_X[g.l] * (my * my);
+    const double Ry = J.Ry0[g.l] + 0.5 * J.AHE[g.l] * mz + (J.AMR_Y[g.l] + J.SMR_Y[g.l]) * mx * my;
+    inv_x = 1. / Rx;
+    inv_y = 1. / Ry;
+  }
+  double Rx_acc = 0.0, Ry_acc = 0.0;
+  for (int q = 0; q < G; ++q) {
+    const double a = __shfl_sync(kWarpAll, inv_x, g.lead + q * V::kLanes);
+    const double b = __shfl_sync(kWarpAll, inv_y, g.lead + q * V::kLanes);
+    if (q < n) {
+      Rx_acc = Rx_acc + a;
+      Ry_acc = Ry_acc + b;
+    }
+  }
+  if (!write) return;
+  if (mine) layer_cols(r + g.l * width, side, mag, energies);
+  if (g.jl == 0) {
+    const cmtj_junction_t &J = junctions[j];
+    double r0 = 0.0, r1 = 0.0;
+    if (mr_mode == CMTJ_MR_CLASSIC) {
+      r0 = J.Rp + (((J.Rap - J.Rp) / 2.0) * (1.0 - cosT));
+    } else if (mr_mode == CMTJ_MR_STRIP) {
+      r0 = 1 / Rx_acc;
+      r1 = 1 / Ry_acc;
+    }
+    double *rr = r + n * width;
+    rr[0] = r0;
+    rr[1] = r1;
+    rr[2] = 0.0;
+    rr[3] = t;
+  }
+}
+
+}  // namespace cmtjd

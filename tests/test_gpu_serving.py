@@ -57,3 +57,31 @@ def test_serving_policy_changes_order_not_results(gpu_lib):
     assert states[0].keys() == states[1].keys()
     for k in states[0]:
         assert np.array_equal(states[0][k]["m"], states[1][k]["m"]), k
+
+
+@pytest.mark.gpu
+def test_serving_fp64_requests_same_alone_and_in_mix(gpu_lib):
+    """FP64 plain requests run on their own stream beside the FP32 ticks;
+    each one's junctions end in the same bits as the same junctions run
+    alone through engine.run_junctions."""
+    from cmtj_gb300 import engine
+
+    def trace():
+        return serving.make_trace(6, rate_hz=400.0, seed=21, min_solves=64, max_solves=256, t_min=2e-10,
+                                  t_max=4e-10, f64_fraction=0.5)
+
+    mix = trace()
+    assert {r.precision for r in mix} == {"f32", "f64"}
+    done = serving.ServingEngine(hbm_budget_bytes=64 << 20, chunk_steps=500).run(mix)
+    assert all(r.done_at is not None for r in done)
+    checked = 0
+    for a, b in zip(sorted(done, key=lambda r: r.arrival), trace()):
+        if a.precision != "f64":
+            continue
+        plan = engine.plan_run(b.total_time, b.time_step, b.total_time)
+        engine.run_junctions(b.junctions, plan, b.solver)
+        for x, y in zip(a.junctions, b.junctions):
+            for lx, ly in zip(x.layers, y.layers):
+                assert (lx.mag.x, lx.mag.y, lx.mag.z) == (ly.mag.x, ly.mag.y, ly.mag.z)
+        checked += 1
+    assert checked >= 1
