@@ -2,32 +2,21 @@
 //
 // Stack::runSimulationKCL / runSimulationNonKCL (core/stack.hpp:317-423)
 // with SeriesStack / ParallelStack coupling and resistance (425-480).  One
-// CTA runs one stack, one thread per junction; the shared per-step values
-// (frozen magnetisations, coupling strengths, the coupled current) pass
-// through shared memory, and every sum the reference forms serially is
-// formed serially by one thread in the same order, so results keep the
-// reference's rounding.  Compiled with --fmad=false like plain_f64.cu.
+// CTA runs one stack.  The shared per-step values (frozen magnetisations,
+// coupling strengths, the coupled current) pass through shared memory, and
+// every sum the reference forms serially is formed serially by one thread
+// in the same order, so results keep the reference's rounding.
+//
+// k_stack_lanes (stack_lanes_f64.cu) steps each junction with its layers on
+// lanes, like the single-junction kernel; k_stack_f64 here, one thread per
+// junction, runs the stacks too wide for a CTA of lanes.  Compiled with
+// --fmad=false like plain_f64.cu.
 #include "plain_f64.cuh"
+#include "stack_common.cuh"
 
 using namespace cmtjd;
 
 namespace {
-
-constexpr int kMaxStack = 256;
-
-// getEffectiveCouplingStrength (stack.hpp:432-439 series, 461-468 parallel).
-__device__ __forceinline__ double coupling(const cmtj_stack_t &S, const double *cs, int order, const D3 &m1,
-                                           const D3 &m2, const D3 &p1, const D3 &p2) {
-  const double c = S.n_coupling == 1 ? cs[0] : cs[order];
-  const double m1c = dot(m1, p1);
-  const double m2c = dot(m2, p2);
-  return S.kind == CMTJ_STACK_SERIES ? c * (m1c + m2c) : c * (m1c - m2c);
-}
-
-// getPhaseOffset: series phaseOffset * order, parallel phaseOffset.
-__device__ __forceinline__ double phase_offset(const cmtj_stack_t &S, int order) {
-  return S.kind == CMTJ_STACK_SERIES ? S.phase_offset * order : S.phase_offset;
-}
 
 __global__ void __launch_bounds__(kMaxStack) k_stack_f64(const cmtj_stack_t *__restrict__ stacks,
                                                          const double *__restrict__ couplings,
@@ -210,6 +199,15 @@ extern "C" int cmtj_run_stack_f64(const cmtj_stack_t *d_stacks, int32_t n_stacks
   if (p->write_every == 0 || (p->solver != CMTJ_RK4 && p->solver != CMTJ_EULER_HEUN)) {
     cmtj_set_error("cmtj_run_stack_f64: write_every must be >= 1 and the solver RK4 or Euler-Heun");
     return CMTJ_ERR_ARG;
+  }
+  // layers on lanes when the widest stack fits a CTA of lanes
+  const cudaError_t e = cmtjd::stack_lanes_launch(d_stacks, n_stacks, d_couplings, d_junctions, d_top_bottom,
+                                                  d_layers, d_tables, *p, d_log, d_stack_log, stack_width,
+                                                  max_junctions, d_status, cmtj_stream(stream));
+  if (e == cudaSuccess) return CMTJ_OK;
+  if (e != cudaErrorNotSupported) {
+    cmtj_set_error("launch of k_stack_lanes failed: %s", cudaGetErrorString(e));
+    return CMTJ_ERR_CUDA;
   }
   const int threads = (max_junctions + 31) / 32 * 32;
   k_stack_f64<<<n_stacks, threads, 0, cmtj_stream(stream)>>>(d_stacks, d_couplings, d_junctions, d_top_bottom,

@@ -228,8 +228,10 @@ int cmtj_struct_sizes(int32_t *sizes, int32_t n);
 /* FP64 plain form.                                                        */
 /* ---------------------------------------------------------------------- */
 /* Junction::runSimulation (core/junction.hpp:1948-2056) for n_junctions
- * independent junctions, FP64, one device thread per junction, arithmetic
- * in the reference's order with no FMA contraction.
+ * independent junctions, FP64, arithmetic in the reference's order with no
+ * FMA contraction.  Fixed step: each junction's layers side by side on
+ * lanes (p->max_layers, p->lanes_per_layer choose the layout, not the
+ * result); Dormand-Prince: one device thread per junction.
  *   d_junctions  [n_junctions] cmtj_junction_t           (device, read)
  *   d_layers     [total layers] cmtj_layer_t; .mag is updated in place
  *   d_tables     custom-driver tables (device, may be NULL)
@@ -262,7 +264,9 @@ typedef struct cmtj_stack {
 } cmtj_stack_t;
 
 /* Stack::runSimulation (stack.hpp:311-423) for n_stacks stacks, one CTA
- * each.  d_top_bottom[2*j] / [2*j+1]: index (within junction j) of the
+ * each; each junction's layers on lanes when the widest stack fits a
+ * 256-thread CTA that way, else one thread per junction (same results).
+ * d_top_bottom[2*j] / [2*j+1]: index (within junction j) of the
  * topId layer and of the bottomId layer (-1: use cmtj_stack_t.pol).
  * Junction logs as cmtj_run_simulation_f64; the stack log is
  * [n_stacks][p->n_log][stack_width] doubles per row: Resistance,

@@ -45,3 +45,69 @@ def test_stack_matches_reference(gpu_lib, name):
         assert set(a) == set(b)
         for k in b:
             _close(a[k], b[k], k)
+
+
+def _force_params(monkeypatch, **fields):
+    """Lower with the given cmtj_sim_params_t fields overridden."""
+    from cmtj_gb300 import _lower
+    orig = _lower.make_params
+
+    def make_params(*a, **k):
+        p = orig(*a, **k)
+        for f, v in fields.items():
+            p[f] = v
+        return p
+
+    monkeypatch.setattr(_lower, "make_params", make_params)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("lanes", [1, 4])
+@pytest.mark.parametrize("name", sorted(cases.STACKS))
+def test_stack_both_layouts_match_reference(gpu_lib, monkeypatch, name, lanes):
+    """The stack kernel with a layer per lane and with a layer's x, y, z on
+    a quad of lanes, against the reference's logs."""
+    _force_params(monkeypatch, lanes_per_layer=lanes)
+    gs, gj = _load(name)
+    slog, jlogs = cases.run_stack_case(cmtj_gb300, name)
+    for k in gs:
+        _close(slog[k], gs[k], k)
+    for a, b in zip(jlogs, gj):
+        for k in b:
+            _close(a[k], b[k], k)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", ["kcl", "delayed", "nondelayed", "kcl_thermal"])
+def test_wide_stack_thread_per_junction_equals_lanes(gpu_lib, monkeypatch, mode):
+    """40 bilayer junctions in one stack.  Told that a junction may hold 8
+    layers, the stack no longer fits a CTA of lanes and runs one thread per
+    junction (k_stack_f64); otherwise its layers run on lanes
+    (k_stack_lanes).  Both give the same bits in every log."""
+    def build():
+        js = [cases._stt_bilayer(cmtj_gb300, 1.0 + 0.01 * k, 1e3 + 40 * k, (0.1 + 0.005 * k, 0.2, 1))
+              for k in range(40)]
+        if mode == "kcl_thermal":
+            for q, j in enumerate(js):
+                j.setLayerTemperatureDriver("all", cmtj_gb300.constantDriver(300.0))
+                for l, layer in enumerate(j.layers):
+                    layer.noise_seed = 9000 + 10 * q + l
+        s = cmtj_gb300.stack.SeriesStack(js, useKCL=mode.startswith("kcl"), phaseOffset=0.1)
+        if mode == "nondelayed":
+            s.setDelayed(False)
+        s.setCouplingStrength(0.05)
+        s.setCoupledCurrentDriver(cmtj_gb300.sineDriver(1e10, 4e10, 3e9, 0))
+        s.runSimulation(5e-11, 1e-13, 1e-12)
+        return s
+
+    on_lanes = build()
+    _force_params(monkeypatch, max_layers=8, lanes_per_layer=1)
+    per_thread = build()
+    a, b = on_lanes.getLog(), per_thread.getLog()
+    assert a.keys() == b.keys()
+    for k in a:
+        assert np.array_equal(np.asarray(a[k]), np.asarray(b[k])), k
+    for q in range(40):
+        la, lb = on_lanes.getLog(q), per_thread.getLog(q)
+        for k in la:
+            assert np.array_equal(np.asarray(la[k]), np.asarray(lb[k])), (q, k)
