@@ -24,9 +24,11 @@ UNITS = {
     "abi.cu": [],
     "plain_f64.cu": ["--fmad=false"],
     "plain_lanes_f64.cu": ["--fmad=false"],
+    "dp_quads_f64.cu": ["--fmad=false"],
     "stack_f64.cu": ["--fmad=false"],
     "stack_lanes_f64.cu": ["--fmad=false"],
     "group_f64.cu": ["--fmad=false"],
+    "group_lanes_f64.cu": ["--fmad=false"],
     "batch_f32.cu": [],
     "batch_f32_l1.cu": [],
     "batch_f32_l2.cu": [],

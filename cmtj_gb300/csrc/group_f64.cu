@@ -1,8 +1,9 @@
 // Dipole-coupled junction groups, FP64 plain form.
 //
 // GroupInteraction::runSimulation (core/reservoir.hpp:185-230) with
-// stepFunctionalSolver (130-151): one CTA runs one group, one thread per
-// junction.  Each step the top-layer magnetisations are frozen in shared
+// stepFunctionalSolver (130-151): one CTA runs one group.  This kernel runs
+// one thread per junction, for groups too wide for k_group_lanes
+// (group_lanes_f64.cu), which steps each junction with its layers on lanes.  Each step the top-layer magnetisations are frozen in shared
 // memory; every junction sums the interaction fields from all others in
 // index order, sets the sum as its top layer's reserved interaction field
 // (the HRES driver slots, as setLayerReservedInteractionField does) and
@@ -10,33 +11,12 @@
 // dipole tensors) is fixed and comes from the host, formed with the
 // reference's own libm; only the m-dependent part is evaluated here, in the
 // reference's operand order.  Compiled with --fmad=false like plain_f64.cu.
+#include "group_common.cuh"
 #include "plain_f64.cuh"
 
 using namespace cmtjd;
 
 namespace {
-
-constexpr int kMaxGroup = 256;
-
-// computeDipoleInteraction (reservoir.hpp:77-97) for fixed rij, |rij|^3,
-// |rij|^5: prefactor * (3 (m.rij) rij / r5 - m / r3).
-__device__ __forceinline__ D3 dipole_term(const cmtj_pair_t &q, const D3 &m) {
-  const D3 rij = d3(q.g[0], q.g[1], q.g[2]);
-  const double r3 = q.g[3], r5 = q.g[4];
-  const double s = 3 * (m.x * rij.x + m.y * rij.y + m.z * rij.z);
-  const D3 a = smul(s, rij) / r5;
-  const D3 c = a - m / r3;
-  return smul(q.scale, c);
-}
-
-// calculate_tensor_interaction (junction.hpp:64-72) with the fixed tensor of
-// getDipoleTensorFromRelPositions and Ms V / mu0.
-__device__ __forceinline__ D3 noumra_term(const cmtj_pair_t &q, const D3 &m) {
-  const double *t = q.g;
-  const D3 r = d3(t[0] * m.x + t[1] * m.y + t[2] * m.z, t[3] * m.x + t[4] * m.y + t[5] * m.z,
-                  t[6] * m.x + t[7] * m.y + t[8] * m.z);
-  return r * q.scale;
-}
 
 __global__ void __launch_bounds__(kMaxGroup) k_group_f64(const cmtj_group_t *__restrict__ groups,
                                                          const cmtj_pair_t *__restrict__ pairs,
@@ -79,15 +59,7 @@ __global__ void __launch_bounds__(kMaxGroup) k_group_f64(const cmtj_group_t *__r
     }
     __syncthreads();
     if (mine) {
-      D3 H = zero3();
-      if (G.interaction != CMTJ_INTERACTION_NULL) {
-        for (int k = 0; k < N; ++k) {
-          if (k == j) continue;
-          const D3 mk = d3(s_m[k][0], s_m[k][1], s_m[k][2]);
-          H = H + (G.interaction == CMTJ_INTERACTION_DIPOLE ? dipole_term(row_pairs[k], mk)
-                                                            : noumra_term(row_pairs[k], mk));
-        }
-      }
+      const D3 H = interaction_field(G.interaction, row_pairs, s_m, N, j);
       Ls[ti].drv[CMTJ_SLOT_HRES + 0].constantValue = H.x;
       Ls[ti].drv[CMTJ_SLOT_HRES + 1].constantValue = H.y;
       Ls[ti].drv[CMTJ_SLOT_HRES + 2].constantValue = H.z;
@@ -131,6 +103,14 @@ extern "C" int cmtj_run_group_f64(const cmtj_group_t *d_groups, int32_t n_groups
   if (p->write_every == 0 || (p->solver != CMTJ_RK4 && p->solver != CMTJ_EULER_HEUN && p->solver != CMTJ_HEUN)) {
     cmtj_set_error("cmtj_run_group_f64: write_every must be >= 1 and the solver RK4, Euler-Heun or Heun");
     return CMTJ_ERR_ARG;
+  }
+  // layers on lanes when the widest group fits a CTA of lanes
+  const cudaError_t e = cmtjd::group_lanes_launch(d_groups, n_groups, d_pairs, d_junctions, d_top, d_layers, d_tables,
+                                                  *p, d_log, max_junctions, d_status, cmtj_stream(stream));
+  if (e == cudaSuccess) return CMTJ_OK;
+  if (e != cudaErrorNotSupported) {
+    cmtj_set_error("launch of k_group_lanes failed: %s", cudaGetErrorString(e));
+    return CMTJ_ERR_CUDA;
   }
   const int threads = (max_junctions + 31) / 32 * 32;
   k_group_f64<<<n_groups, threads, 0, cmtj_stream(stream)>>>(d_groups, d_pairs, d_junctions, d_top, d_layers,

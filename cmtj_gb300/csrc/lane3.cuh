@@ -89,6 +89,11 @@ static __device__ __forceinline__ bool scalar_owner(const D3 &) { return true; }
 static __device__ __forceinline__ bool x_is_nan(const C3 &a) { return (threadIdx.x & 3) == 0 && isnan(a.v); }
 static __device__ __forceinline__ bool x_is_nan(const D3 &a) { return isnan(a.x); }
 
+// isnan of the x component, on every lane of the quad.
+static __device__ __forceinline__ bool x_nan_all(const C3 &a) {
+  return (__ballot_sync(quad_mask(), x_is_nan(a)) & quad_mask()) != 0u;
+}
+
 // The same component of the vector another lane holds.
 static __device__ __forceinline__ C3 shfl_vec(const C3 &a, int src) { return C3{__shfl_sync(0xffffffffu, a.v, src)}; }
 static __device__ __forceinline__ D3 shfl_vec(const D3 &a, int src) {

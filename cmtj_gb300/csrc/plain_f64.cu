@@ -10,8 +10,10 @@
 //
 // The fixed-step solvers run one lane per layer (plain_lanes_f64.cu).  The
 // Dormand-Prince loop (core/junction.hpp:1982-2045) runs here, one thread
-// per junction: each layer's step sees the step size the previous layer's
-// step chose, so its layers cannot run side by side.  The state of a
+// per junction, for large batches, and with a layer's x, y, z on a quad of
+// lanes for the rest (dp_quads_f64.cu): each layer's step sees the step
+// size the previous layer's step chose, so its layers cannot run side by
+// side.  The state of a
 // junction lives in the thread's registers / local memory; layer parameters
 // and drivers are read from the caller's cmtj_layer_t array through L1.
 #include "plain_f64.cuh"
@@ -146,6 +148,18 @@ extern "C" int cmtj_run_simulation_f64(const cmtj_junction_t *d_junctions, int32
         cmtjd::plain_lanes_launch(d_junctions, n_junctions, d_layers, d_tables, *p, d_log, d_status, cmtj_stream(stream));
     if (e != cudaSuccess) {
       cmtj_set_error("launch of k_plain_lanes failed: %s", cudaGetErrorString(e));
+      return CMTJ_ERR_CUDA;
+    }
+    return CMTJ_OK;
+  }
+  int dev = 0, sms = 0;
+  CMTJ_CUDA_TRY(cudaGetDevice(&dev));
+  CMTJ_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  if (cmtjd::dp_quads_pick(*p, n_junctions, sms)) {
+    const cudaError_t e =
+        cmtjd::dp_quads_launch(d_junctions, n_junctions, d_layers, d_tables, *p, d_log, d_status, cmtj_stream(stream));
+    if (e != cudaSuccess) {
+      cmtj_set_error("launch of k_dp_quads failed: %s", cudaGetErrorString(e));
       return CMTJ_ERR_CUDA;
     }
     return CMTJ_OK;

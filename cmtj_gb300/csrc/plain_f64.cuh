@@ -177,7 +177,8 @@ using Side = SideT<D3>;
 template <class V>
 static __device__ V rhs(const cmtj_layer_t &L, const cmtj_constants_t &c, double time, const V &m, const V &bottom,
                         const V &top, const DriverCtx &dc, typename NoDeduce<SideT<V>>::type *side,
-                        const cmtj_driver_t *cur = nullptr, uint32_t dyn = 0xffffffffu) {
+                        const cmtj_driver_t *cur = nullptr, uint32_t dyn = 0xffffffffu,
+                        const double *hres = nullptr) {
   const double Ms = L.Ms;
   const uint32_t zt = L.zero_terms;
   // --- calculateHeff (580-622).  Terms the host marked identically zero
@@ -214,7 +215,9 @@ static __device__ V rhs(const cmtj_layer_t &L, const cmtj_constants_t &c, double
   const double K = slot_at(L, CMTJ_SLOT_ANIS, time, dc, dyn);
   const V Hanis = anis * ((2 * K) * dot(anis, m) / Ms);
   const V Hdmi = V::axial(L, CMTJ_SLOT_HDMI, time, dc, dyn);
-  const V Hres = V::axial(L, CMTJ_SLOT_HRES, time, dc, dyn);
+  // hres: the reserved interaction field a group sets for this step (the
+  // value its constant HRES drivers would return)
+  const V Hres = hres ? V::make(hres[0], hres[1], hres[2]) : V::axial(L, CMTJ_SLOT_HRES, time, dc, dyn);
   double K2 = 0.0;
   V H = Hext + Hanis;
   if (!(zt & CMTJ_ZERO_K2)) {
@@ -396,41 +399,45 @@ static __device__ bool junction_step(int n, const cmtj_layer_t *Ls, D3 *mag, D3 
   return true;
 }
 
+// isnan of a vector's x component, on every lane that holds the vector.
+static __device__ __forceinline__ bool x_nan_all(const D3 &a) { return isnan(a.x); }
+
 // Layer::dormand_prince_step (junction.hpp:866-1002) of one layer: tries a
 // step of size ts from time t, sets ts to the next step size (whether the
 // step is accepted or not) and updates the layer's PID state in place.
 // Returns accepted; nan is set when an accepted m is NaN.  Custom drivers
 // are rejected by the host (their tables hold fixed-step times only).
+template <class V>
 static __device__ bool dp_layer(const cmtj_layer_t &L, cmtj_adaptive_t &ap, const cmtj_constants_t &c, double t,
-                                double &ts, D3 &mag, const D3 &bottom, const D3 &top, const double *tables,
-                                Side *side, bool &nan) {
+                                double &ts, V &mag, const V &bottom, const V &top, const double *tables,
+                                typename NoDeduce<SideT<V>>::type *side, bool &nan) {
   const DriverCtx dc = {tables, 0u, 0};
-  const D3 m_t = mag;
+  const V m_t = mag;
   const double c2 = 1.0 / 5.0, c3 = 3.0 / 10.0, c4 = 4.0 / 5.0, c5 = 8.0 / 9.0, c6 = 1.0, c7 = 1.0;
-  const D3 k1 = rhs(L, c, t, m_t, bottom, top, dc, nullptr) * ts;
-  const D3 k2 = rhs(L, c, t + c2 * ts, m_t + k1 * (c2), bottom, top, dc, nullptr) * ts;
-  const D3 k3 = rhs(L, c, t + c3 * ts, m_t + k1 * (3.0 / 40.0) + k2 * (9.0 / 40.0), bottom, top, dc, nullptr) * ts;
-  const D3 k4 = rhs(L, c, t + c4 * ts, m_t + k1 * (44.0 / 45.0) + k2 * (-56.0 / 15.0) + k3 * (32.0 / 9.0), bottom,
+  const V k1 = rhs(L, c, t, m_t, bottom, top, dc, nullptr) * ts;
+  const V k2 = rhs(L, c, t + c2 * ts, m_t + k1 * (c2), bottom, top, dc, nullptr) * ts;
+  const V k3 = rhs(L, c, t + c3 * ts, m_t + k1 * (3.0 / 40.0) + k2 * (9.0 / 40.0), bottom, top, dc, nullptr) * ts;
+  const V k4 = rhs(L, c, t + c4 * ts, m_t + k1 * (44.0 / 45.0) + k2 * (-56.0 / 15.0) + k3 * (32.0 / 9.0), bottom,
                     top, dc, nullptr) * ts;
-  const D3 k5 = rhs(L, c, t + c5 * ts,
+  const V k5 = rhs(L, c, t + c5 * ts,
                     m_t + k1 * (19372.0 / 6561.0) + k2 * (-25360.0 / 2187.0) + k3 * (64448.0 / 6561.0) +
                         k4 * (-212.0 / 729.0),
                     bottom, top, dc, nullptr) * ts;
-  const D3 k6 = rhs(L, c, t + c6 * ts,
+  const V k6 = rhs(L, c, t + c6 * ts,
                     m_t + k1 * (9017.0 / 3168.0) + k2 * (-355.0 / 33.0) + k3 * (46732.0 / 5247.0) +
                         k4 * (49.0 / 176.0) + k5 * (-5103.0 / 18656.0),
                     bottom, top, dc, nullptr) * ts;
-  const D3 k7 = rhs(L, c, t + c7 * ts,
+  const V k7 = rhs(L, c, t + c7 * ts,
                     m_t + k1 * (35.0 / 384.0) + k3 * (500.0 / 1113.0) + k4 * (125.0 / 192.0) +
                         k5 * (-2187.0 / 6784.0) + k6 * (11.0 / 84.0),
                     bottom, top, dc, side) * ts;
-  const D3 m5 = m_t + k1 * (35.0 / 384.0) + k3 * (500.0 / 1113.0) + k4 * (125.0 / 192.0) +
+  const V m5 = m_t + k1 * (35.0 / 384.0) + k3 * (500.0 / 1113.0) + k4 * (125.0 / 192.0) +
                 k5 * (-2187.0 / 6784.0) + k6 * (11.0 / 84.0);
-  const D3 m4 = m_t + k1 * (5179.0 / 57600.0) + k3 * (7571.0 / 16695.0) + k4 * (393.0 / 640.0) +
+  const V m4 = m_t + k1 * (5179.0 / 57600.0) + k3 * (7571.0 / 16695.0) + k4 * (393.0 / 640.0) +
                 k5 * (-92097.0 / 339200.0) + k6 * (187.0 / 2100.0) + k7 * (1.0 / 40.0);
-  const D3 err = m5 - m4;
-  const double err_norm = sqrt(err.x * err.x + err.y * err.y + err.z * err.z);
-  const double tol = ap.abs_tol + ap.rel_tol * sqrt(m_t.x * m_t.x + m_t.y * m_t.y + m_t.z * m_t.z);
+  const V err = m5 - m4;
+  const double err_norm = sqrt(dot(err, err));  // x*x + y*y + z*z
+  const double tol = ap.abs_tol + ap.rel_tol * sqrt(dot(m_t, m_t));
   double ratio = err_norm / tol;
   if (tol < 1e-15 || isnan(ratio) || isinf(ratio)) ratio = 10.0;
   double factor;
@@ -450,7 +457,7 @@ static __device__ bool dp_layer(const cmtj_layer_t &L, cmtj_adaptive_t &ap, cons
   ts = next;
   if (ratio <= 1.0) {
     mag = normalized(m5);
-    if (isnan(mag.x)) nan = true;
+    if (x_nan_all(mag)) nan = true;
     return true;
   }
   return false;

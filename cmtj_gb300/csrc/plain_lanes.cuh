@@ -1,5 +1,6 @@
 // Device building blocks of the FP64 fixed-step runners with a junction's
-// layers side by side on lanes (plain_lanes_f64.cu, stack_f64.cu).
+// layers side by side on lanes (plain_lanes_f64.cu, stack_lanes_f64.cu,
+// group_lanes_f64.cu).
 //
 // A junction holds `span` = G * P consecutive lanes of one warp: G layer
 // slots (at least its layer count) of P lanes each (P = 1 for D3, 4 for C3).
@@ -43,14 +44,14 @@ __device__ __forceinline__ LaneGeo lane_geo(int G) {
 // One iteration of the fixed-step runner (RK4, Euler-Heun or Heun;
 // core/junction.hpp:1668-1815) for the lane's layer of a junction whose
 // n layers step (1 under runSingleLayerSolver).  cur overrides the current
-// driver (stacks).  Returns the first layer whose m became NaN (RK4: the
-// layers above it keep their start-of-step m, as when rk4_step throws), or
-// -1.
+// driver (stacks), hres the reserved interaction field (groups).  Returns
+// the first layer whose m became NaN (RK4: the layers above it keep their
+// start-of-step m, as when rk4_step throws), or -1.
 template <int SOLVER, class V>
 __device__ __forceinline__ int lane_step(const cmtj_layer_t &L, const cmtj_constants_t &c, V &mag,
                                          SideT<V> &side, bool step, const LaneGeo &g, int n, uint32_t i, double t,
                                          double dt, const double *tables, bool energies,
-                                         const cmtj_driver_t *cur, uint32_t dyn) {
+                                         const cmtj_driver_t *cur, uint32_t dyn, const double *hres = nullptr) {
   // neighbours at the start of the step; zero beyond the stack's ends
   V below = shfl_vec(mag, g.below_src), above = shfl_vec(mag, g.above_src);
   if (g.l == 0) below = V::zero();
@@ -67,7 +68,7 @@ __device__ __forceinline__ int lane_step(const cmtj_layer_t &L, const cmtj_const
         const double ts = s == 0 ? t : (s == 3 ? t + dt : t + 0.5 * dt);
         const V mi = s == 0 ? mag : (s == 3 ? mag + k : mag + k * 0.5);
         const DriverCtx dc = {tables, i, s == 0 ? 0 : (s == 3 ? 2 : 1)};
-        k = rhs(L, c, ts, mi, below, above, dc, (s == 3 && energies) ? &side : nullptr, cur, dyn) * dt;
+        k = rhs(L, c, ts, mi, below, above, dc, (s == 3 && energies) ? &side : nullptr, cur, dyn, hres) * dt;
         acc = s == 0 ? k : acc + (s == 3 ? k : k * 2.0);
       }
       next = normalized(mag + acc / 6.0);
@@ -85,7 +86,7 @@ __device__ __forceinline__ int lane_step(const cmtj_layer_t &L, const cmtj_const
     if (step) {
       const DriverCtx d0 = {tables, i, 0};
       const V dW = langevin<V>(L, c, t, i, d0, dyn);
-      const V f = rhs(L, c, t, mag, below, above, d0, energies ? &side : nullptr, cur, dyn);
+      const V f = rhs(L, c, t, mag, below, above, d0, energies ? &side : nullptr, cur, dyn, hres);
       const V gt = stoch_torque(L, c, mag, dW);
       const V mNext = mag + gt * sqrt(dt);
       const V g2 = stoch_torque(L, c, mNext, dW);
@@ -97,7 +98,7 @@ __device__ __forceinline__ int lane_step(const cmtj_layer_t &L, const cmtj_const
     V fn = V::zero(), gn = V::zero(), dW = V::zero(), pred = V::zero();
     if (step) {
       const DriverCtx d0 = {tables, i, 0};
-      fn = rhs(L, c, t, mag, below, above, d0, nullptr, cur, dyn);
+      fn = rhs(L, c, t, mag, below, above, d0, nullptr, cur, dyn, hres);
       dW = langevin<V>(L, c, t, i, d0, dyn);
       gn = stoch_torque(L, c, mag, dW);
       pred = mag + fn * dt + gn * sqrt(dt);
@@ -107,7 +108,7 @@ __device__ __forceinline__ int lane_step(const cmtj_layer_t &L, const cmtj_const
     if (g.l >= n - 1) pa = V::zero();
     if (step) {
       const DriverCtx d2 = {tables, i, 2};
-      const V f2 = rhs(L, c, t + dt, pred, pb, pa, d2, energies ? &side : nullptr, cur, dyn);
+      const V f2 = rhs(L, c, t + dt, pred, pb, pa, d2, energies ? &side : nullptr, cur, dyn, hres);
       const V g2 = stoch_torque(L, c, pred, dW);
       mag = mag + smul(0.5 * dt, fn + f2) + smul(0.5, gn + g2) * sqrt(dt);
       mag = normalized(mag);

@@ -20,4 +20,11 @@ cudaError_t plain_lanes_launch(const cmtj_junction_t *d_junctions, int32_t n_jun
                                const double *d_tables, const cmtj_sim_params_t &p, double *d_log, uint32_t *d_status,
                                cudaStream_t stream);
 
+// Dormand-Prince with one junction per quad of lanes (dp_quads_f64.cu):
+// whether the launcher takes it for this batch, and the launch.
+bool dp_quads_pick(const cmtj_sim_params_t &p, int32_t n_junctions, int sm_count);
+cudaError_t dp_quads_launch(const cmtj_junction_t *d_junctions, int32_t n_junctions, cmtj_layer_t *d_layers,
+                            const double *d_tables, const cmtj_sim_params_t &p, double *d_log, uint32_t *d_status,
+                            cudaStream_t stream);
+
 }  // namespace cmtjd

@@ -3,8 +3,9 @@ bound at python/cmtj.cpp:428-445).
 
 GroupInteraction keeps the reference's constructor checks, interaction
 functions, per-step semantics and per-junction logs.  Its run is one device
-launch (cmtj_run_group_f64): one CTA per group, one thread per junction, the
-FP64 plain form's device physics.  The pair geometry the interaction uses
+launch (cmtj_run_group_f64): one CTA per group, each junction's layers on
+lanes (one thread per junction for groups too wide for that), the FP64
+plain form's device physics.  The pair geometry the interaction uses
 (separations and their 3rd and 5th powers, or the dipole tensors) never
 changes during a run, so the host forms it once here with the same libm
 calls and operand order as the reference, and the device evaluates only the

@@ -308,8 +308,10 @@ typedef struct cmtj_pair {
   double scale;
 } cmtj_pair_t;                  /* 80 bytes */
 
-/* GroupInteraction::runSimulation for n_groups groups, one CTA each, one
- * thread per junction.  Every step: each junction's field from all others'
+/* GroupInteraction::runSimulation for n_groups groups, one CTA each; each
+ * junction's layers on lanes when the widest group fits a 256-thread CTA
+ * that way, else one thread per junction (same results).  Every step: each
+ * junction's field from all others'
  * top-layer magnetisations (frozen at step start) is summed in index order
  * and set as its top layer's reserved interaction field (the HRES driver
  * slots, setLayerReservedInteractionField), then every junction steps.

@@ -70,13 +70,12 @@ def _force_lanes(monkeypatch, lanes):
     monkeypatch.setattr(_lower, "make_params", make_params)
 
 
-FIXED_STEP = sorted(n for n in cases.DETERMINISTIC if not n.startswith("dp_"))
-
-
 @pytest.mark.gpu
 @pytest.mark.parametrize("lanes", [1, 4])
-@pytest.mark.parametrize("name", FIXED_STEP)
+@pytest.mark.parametrize("name", sorted(cases.DETERMINISTIC))
 def test_fp64_plain_both_layouts_match_reference(gpu_lib, monkeypatch, name, lanes):
+    """Fixed step: a layer per lane / a layer per quad.  Dormand-Prince: a
+    junction per thread / a junction per quad."""
     _force_lanes(monkeypatch, lanes)
     golden, gmags = load_golden(name)
     _, log, mags = cases.run_case(cmtj_gb300, name)
@@ -116,3 +115,38 @@ def test_fp64_plain_layouts_give_identical_bits(gpu_lib, monkeypatch, solver):
             assert np.array_equal(la[k], lb[k]), k
         for x, y in zip(a.layers, b.layers):
             assert (x.mag.x, x.mag.y, x.mag.z) == (y.mag.x, y.mag.y, y.mag.z)
+
+
+@pytest.mark.gpu
+def test_dormand_prince_layouts_give_identical_bits(gpu_lib, monkeypatch):
+    """64 sine-driven free layers under Dormand-Prince: one thread per
+    junction and one quad of lanes per junction take the same adaptive steps
+    and give the same bits."""
+    from cmtj_gb300 import engine
+    V = cmtj_gb300.CVector
+
+    def build():
+        js = []
+        for k in range(64):
+            demag = [V(0.0024, 0, 0), V(0, 0.0024, 0), V(0, 0, 0.9952)]
+            layer = cmtj_gb300.Layer("free", mag=V(0.1, 0, 0.995), anis=V(0, 0, 1), Ms=1.2, thickness=1.5e-9,
+                                     cellSurface=1e-16, demagTensor=demag, damping=0.01)
+            j = cmtj_gb300.Junction([layer])
+            j.setLayerAnisotropyDriver("free", cmtj_gb300.constantDriver(3e5))
+            j.setLayerOerstedFieldDriver("free", cmtj_gb300.AxialDriver(
+                cmtj_gb300.sineDriver(0, 5e3, 2e9 + 1.5e8 * k, 0), cmtj_gb300.NullDriver(), cmtj_gb300.NullDriver()))
+            js.append(j)
+        return js
+
+    runs = []
+    for lanes in (1, 4):
+        _force_lanes(monkeypatch, lanes)
+        js = build()
+        engine.run_junctions(js, engine.plan_run(1e-9, 1e-13, 1e-11), cmtj_gb300.SolverMode.DormandPrince)
+        runs.append(js)
+    for a, b in zip(*runs):
+        la, lb = a.getLogArrays(), b.getLogArrays()
+        for k in la:
+            assert np.array_equal(la[k], lb[k]), k
+        assert (a.layers[0].mag.x, a.layers[0].mag.y, a.layers[0].mag.z) == \
+               (b.layers[0].mag.x, b.layers[0].mag.y, b.layers[0].mag.z)

@@ -103,3 +103,73 @@ def test_group_fp64_gpu_matches_reference(gpu_lib, name):
                 assert np.max(np.abs(a - v)) <= 1e-9, (name, k, col)
             else:
                 assert np.max(np.abs(a - v)) <= 1e-9 * max(np.max(np.abs(v)), 1e-300), (name, k, col)
+
+
+def _force_params(monkeypatch, **fields):
+    """Lower with the given cmtj_sim_params_t fields overridden."""
+    from cmtj_gb300 import _lower
+    orig = _lower.make_params
+
+    def make_params(*a, **k):
+        p = orig(*a, **k)
+        for f, v in fields.items():
+            p[f] = v
+        return p
+
+    monkeypatch.setattr(_lower, "make_params", make_params)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("lanes", [1, 4])
+@pytest.mark.parametrize("name", sorted(group_cases.CASES))
+def test_group_both_layouts_match_reference(gpu_lib, monkeypatch, name, lanes):
+    """The group kernel with a layer per lane and with a layer's x, y, z on a
+    quad of lanes, against the reference's logs."""
+    _force_params(monkeypatch, lanes_per_layer=lanes)
+    got = group_cases.run_case(cm, name)
+    for k, cols in _golden(name).items():
+        for col, v in cols.items():
+            a = got[k][col]
+            if col == "time":
+                assert np.array_equal(a, v)
+            elif col.endswith(("_mx", "_my", "_mz")):
+                assert np.max(np.abs(a - v)) <= 1e-9, (name, k, col)
+            else:
+                assert np.max(np.abs(a - v)) <= 1e-9 * max(np.max(np.abs(v)), 1e-300), (name, k, col)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", ["dipole", "noumra_thermal"])
+def test_wide_group_thread_per_junction_equals_lanes(gpu_lib, monkeypatch, mode):
+    """40 bilayer junctions on a 4 x 10 grid.  Told that a junction may hold
+    8 layers, the group no longer fits a CTA of lanes and runs one thread
+    per junction (k_group_f64); otherwise its layers run on lanes
+    (k_group_lanes).  Both give the same bits in every log and leave the
+    same reserved interaction field on every top layer."""
+    def build():
+        js = [group_cases._bilayer(cm, (0.3 - 0.01 * k, 0.05 * (k % 3), 0.95)) for k in range(40)]
+        if mode == "noumra_thermal":
+            for q, j in enumerate(js):
+                j.setLayerTemperatureDriver("all", cm.constantDriver(300.0))
+                for l, layer in enumerate(j.layers):
+                    layer.noise_seed = 5000 + 10 * q + l
+        pos = [cm.CVector(70e-9 * (k % 4), 70e-9 * (k // 4), 0) for k in range(40)]
+        g = cm.reservoir.GroupInteraction(pos, js)
+        if mode == "noumra_thermal":
+            g.setInteractionFunction(cm.reservoir.computeDipoleInteractionNoumra)
+        g.runSimulation(3e-11, 1e-13, 1e-12)
+        return g
+
+    on_lanes = build()
+    _force_params(monkeypatch, max_layers=8, lanes_per_layer=1)
+    per_thread = build()
+    for q in range(40):
+        la, lb = on_lanes.getLog(q), per_thread.getLog(q)
+        assert la.keys() == lb.keys()
+        for k in la:
+            assert np.array_equal(np.asarray(la[k]), np.asarray(lb[k])), (q, k)
+        a = on_lanes.junctionList[q].getLayer("free")
+        b = per_thread.junctionList[q].getLayer("free")
+        assert (a.mag.x, a.mag.y, a.mag.z) == (b.mag.x, b.mag.y, b.mag.z)
+        ha, hb = a.axial["hres"], b.axial["hres"]
+        assert [d.getCurrentScalarValue(0.0) for d in ha.drivers] == [d.getCurrentScalarValue(0.0) for d in hb.drivers]
