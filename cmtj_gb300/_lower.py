@@ -105,91 +105,91 @@ class TableBuilder:
         return np.concatenate(self.chunks)
 
 
-def _fill_driver(rec, d, tables):
+def _driver_record(d, tables):
+    """One cmtj_driver_t as a tuple in DRIVER_DTYPE field order."""
     if d.update == UpdateType.custom:
         if tables is None:
             raise RuntimeError("custom drivers need a run plan")
-        rec["update"] = _abi.DRV_TABLE
-        rec["table_offset"] = tables.add(d)
-        return
-    rec["update"] = int(d.update)
-    rec["table_offset"] = 0
-    for f in ("constantValue", "amplitude", "frequency", "phase", "period", "cycle", "timeStart", "timeStop",
-              "edgeTime", "steadyTime"):
-        rec[f] = getattr(d, f)
+        return (_abi.DRV_TABLE, 0, tables.add(d), 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0)
+    return (int(d.update), 0, 0, d.constantValue, d.amplitude, d.frequency, d.phase, d.period, d.cycle,
+            d.timeStart, d.timeStop, d.edgeTime, d.steadyTime)
 
 
 def _tensor9(rows):
-    return np.array([[r.x, r.y, r.z] for r in rows], dtype=np.float64).ravel()
+    return [v for r in rows for v in (r.x, r.y, r.z)]
 
 
-def lower_layer(layer, rec, tables=None):
-    rec["mag"] = (layer.mag.x, layer.mag.y, layer.mag.z)
-    rec["anis"] = (layer.anis.x, layer.anis.y, layer.anis.z)
-    rec["ref"] = tuple(layer.referenceLayer)
-    rec["ref2"] = tuple(layer.secondaryReferenceLayer)
-    rec["demag"] = _tensor9(layer.demagTensor)
-    rec["dipole_top"] = _tensor9(layer.dipoleTop)
-    rec["dipole_bottom"] = _tensor9(layer.dipoleBottom)
-    rec["Ms"] = layer.Ms
-    rec["thickness"] = layer.thickness
-    rec["cellSurface"] = layer.cellSurface
-    rec["cellVolume"] = layer.cellVolume
-    rec["damping"] = layer.damping
-    rec["fieldLikeTorque"] = layer.fieldLikeTorque
-    rec["dampingLikeTorque"] = layer.dampingLikeTorque
-    rec["slonczewski"] = layer.SlonczewskiSpacerLayerParameter
-    rec["beta"] = layer.beta
-    rec["kappa"] = layer.kappa
-    rec["spinPolarisation"] = layer.spinPolarisation
-    rec["referenceType"] = int(layer.referenceType)
-    rec["includeSTT"] = int(layer.includeSTT)
-    rec["includeSOT"] = int(layer.includeSOT)
-    rec["dynamicSOT"] = int(layer.dynamicSOT)
-    rec["alternativeSTT"] = int(layer.alternativeSTT)
-    rec["temperatureSet"] = int(layer.temperatureSet)
-    rec["seed_lo"] = layer.noise_seed & 0xFFFFFFFF
-    rec["seed_hi"] = (layer.noise_seed >> 32) & 0xFFFFFFFF
-    rec["noise_step"] = layer.noise_step
-    ap = rec["adaptive"]
-    a = layer.adaptiveParams
-    for f in ("abs_tol", "rel_tol", "max_factor", "min_factor", "safety_factor", "ki", "kp", "kd",
-              "prev_error_ratio", "integral_error"):
-        ap[f] = getattr(a, f)
-    ap["use_pid_control"] = int(bool(a.use_pid_control))
-    drv = rec["drv"]
-    for name, idx in _SCALAR_INDEX.items():
-        _fill_driver(drv[idx], layer.scalar[name], tables)
-    for name, base in _AXIAL_SLOTS.items():
-        for k in range(3):
-            _fill_driver(drv[base + k], layer.axial[name].drivers[k], tables)
-    derive_layer(rec)
+_LAYER_SCALARS = (("Ms", "Ms"), ("thickness", "thickness"), ("cellSurface", "cellSurface"),
+                  ("cellVolume", "cellVolume"), ("damping", "damping"), ("fieldLikeTorque", "fieldLikeTorque"),
+                  ("dampingLikeTorque", "dampingLikeTorque"), ("slonczewski", "SlonczewskiSpacerLayerParameter"),
+                  ("beta", "beta"), ("kappa", "kappa"), ("spinPolarisation", "spinPolarisation"),
+                  ("noise_step", "noise_step"))
+_LAYER_FLAGS = ("includeSTT", "includeSOT", "dynamicSOT", "alternativeSTT", "temperatureSet")
+_ADAPTIVE_FIELDS = ("abs_tol", "rel_tol", "max_factor", "min_factor", "safety_factor", "ki", "kp", "kd",
+                    "prev_error_ratio", "integral_error")
 
 
-def _const_zero(d):
-    return int(d["update"]) == _abi.DRV_CONSTANT and float(d["constantValue"]) == 0.0
+def lower_layers(layers, larr, tables=None):
+    """cmtj_layer_t records of `layers` into larr (same length), column by
+    column; custom drivers are tabulated in layer order, scalar slots before
+    axial ones."""
+    larr["mag"] = [(l.mag.x, l.mag.y, l.mag.z) for l in layers]
+    larr["anis"] = [(l.anis.x, l.anis.y, l.anis.z) for l in layers]
+    larr["ref"] = [tuple(l.referenceLayer) for l in layers]
+    larr["ref2"] = [tuple(l.secondaryReferenceLayer) for l in layers]
+    larr["demag"] = [_tensor9(l.demagTensor) for l in layers]
+    larr["dipole_top"] = [_tensor9(l.dipoleTop) for l in layers]
+    larr["dipole_bottom"] = [_tensor9(l.dipoleBottom) for l in layers]
+    for field, attr in _LAYER_SCALARS:
+        larr[field] = [getattr(l, attr) for l in layers]
+    larr["referenceType"] = [int(l.referenceType) for l in layers]
+    for field in _LAYER_FLAGS:
+        larr[field] = [int(getattr(l, field)) for l in layers]
+    larr["seed_lo"] = [l.noise_seed & 0xFFFFFFFF for l in layers]
+    larr["seed_hi"] = [(l.noise_seed >> 32) & 0xFFFFFFFF for l in layers]
+    ap = larr["adaptive"]
+    for field in _ADAPTIVE_FIELDS:
+        ap[field] = [getattr(l.adaptiveParams, field) for l in layers]
+    ap["use_pid_control"] = [int(bool(l.adaptiveParams.use_pid_control)) for l in layers]
+    slots = []
+    for l in layers:
+        row = [None] * _abi.NUM_SLOTS
+        for name, idx in _SCALAR_INDEX.items():
+            row[idx] = _driver_record(l.scalar[name], tables)
+        for name, base in _AXIAL_SLOTS.items():
+            for k in range(3):
+                row[base + k] = _driver_record(l.axial[name].drivers[k], tables)
+        slots.extend(row)
+    if layers:
+        larr["drv"] = np.array(slots, dtype=_abi.DRIVER_DTYPE).reshape(len(layers), _abi.NUM_SLOTS)
+    derive_layers(larr)
 
 
-def derive_layer(rec):
-    """The derived fields of a cmtj_layer_t record: the reference's constant
-    sub-expressions, evaluated once in FP64 exactly as it writes them, and
-    the CMTJ_ZERO_* mask of field terms that are identically zero."""
+def _const_zero(drv, slot):
+    return (drv["update"][:, slot] == _abi.DRV_CONSTANT) & (drv["constantValue"][:, slot] == 0.0)
+
+
+def derive_layers(larr):
+    """The derived fields of cmtj_layer_t records: the reference's constant
+    sub-expressions, evaluated once in FP64 exactly as it writes them
+    (element-wise numpy arithmetic rounds each operation like the scalar
+    form), and the CMTJ_ZERO_* mask of field terms that are identically
+    zero."""
     c = _constants.snapshot()
-    d = float(rec["damping"])
-    rec["conv_term"] = 1 / (1 + d * d)
-    rec["stoch_conv"] = -c["gyro"] / (1. + d * d)
-    rec["ms_over_mu0"] = float(rec["Ms"]) / c["mu0"]
-    z = 0
-    if not np.any(rec["dipole_top"]) and not np.any(rec["dipole_bottom"]):
-        z |= _abi.ZERO_DIPOLE
-    drv = rec["drv"]
-    if all(_const_zero(drv[_abi.SLOT_IDMI_TOP + k]) and _const_zero(drv[_abi.SLOT_IDMI_BOTTOM + k]) for k in range(3)):
-        z |= _abi.ZERO_IDMI
-    if _const_zero(drv[_abi.SLOT_ANIS2]):
-        z |= _abi.ZERO_K2
-    if _const_zero(drv[_abi.SLOT_IECQ_TOP]) and _const_zero(drv[_abi.SLOT_IECQ_BOTTOM]):
-        z |= _abi.ZERO_J2
-    rec["zero_terms"] = z
+    d = larr["damping"]
+    larr["conv_term"] = 1 / (1 + d * d)
+    larr["stoch_conv"] = -c["gyro"] / (1. + d * d)
+    larr["ms_over_mu0"] = larr["Ms"] / c["mu0"]
+    drv = larr["drv"]
+    z = np.zeros(len(larr), dtype=np.uint32)
+    z[~np.any(larr["dipole_top"] != 0, axis=1) & ~np.any(larr["dipole_bottom"] != 0, axis=1)] |= _abi.ZERO_DIPOLE
+    idmi = np.ones(len(larr), dtype=bool)
+    for k in range(3):
+        idmi &= _const_zero(drv, _abi.SLOT_IDMI_TOP + k) & _const_zero(drv, _abi.SLOT_IDMI_BOTTOM + k)
+    z[idmi] |= _abi.ZERO_IDMI
+    z[_const_zero(drv, _abi.SLOT_ANIS2)] |= _abi.ZERO_K2
+    z[_const_zero(drv, _abi.SLOT_IECQ_TOP) & _const_zero(drv, _abi.SLOT_IECQ_BOTTOM)] |= _abi.ZERO_J2
+    larr["zero_terms"] = z
 
 
 def lower_junction(junction, rec, layer_offset):
@@ -241,9 +241,8 @@ def lower(junctions, plan, solver, calculate_energies):
     off = 0
     for k, j in enumerate(junctions):
         lower_junction(j, jarr[k], off)
-        for l in j.layers:
-            lower_layer(l, larr[off], tables)
-            off += 1
+        off += j.layerNo
+    lower_layers([l for j in junctions for l in j.layers], larr, tables)
     max_layers = max(j.layerNo for j in junctions)
     width = _abi.log_width(max_layers, calculate_energies)
     params = make_params(plan, solver, calculate_energies, width, max_layers)

@@ -194,7 +194,7 @@ def run_stacks(stacks, totalTime, timeStep=1e-13, writeFrequency=1e-11):
     junctions = [j for s in stacks for j in s.junctionList]
     low = lower(junctions, plan, solver, False)
     # the stack's current driver goes through the same lowering (tables for callbacks)
-    from ._lower import TableBuilder, _fill_driver
+    from ._lower import TableBuilder, _driver_record
     tables = TableBuilder(plan, solver)
     base = 0 if low.tables is None else low.tables.size
     srec = np.zeros(len(stacks), dtype=STACK_DTYPE)
@@ -213,7 +213,7 @@ def run_stacks(stacks, totalTime, timeStep=1e-13, writeFrequency=1e-11):
         couplings.extend(s.couplingStrength)
         srec[k]["phase_offset"] = s.phaseOffset
         srec[k]["pol"] = pol
-        _fill_driver(srec[k]["current"], s.currentDriver, tables)
+        srec[k]["current"] = _driver_record(s.currentDriver, tables)
         if srec[k]["current"]["update"] == abi.DRV_TABLE:
             srec[k]["current"]["table_offset"] += base
         for q, (t, b) in enumerate(tb):
