@@ -15,8 +15,10 @@ Each junction's kernel variant comes from its own features and its state is
 saved and restored exactly between ticks, so a request's results are the
 same bits alone or in any mix, at any tick length.
 
-FP64 plain-form requests (Junction objects) run on their own stream through
-cmtj_run_simulation_f64, overlapping the FP32 ticks.
+FP64 plain-form requests (Junction objects) run through
+cmtj_run_simulation_f64 on a small pool of their own streams, overlapping
+the FP32 ticks and one another; their inputs go up asynchronously from
+pinned memory, so admitting one never waits for another's kernel.
 """
 import threading
 import time
@@ -127,11 +129,14 @@ class ServingEngine:
         self.policy = policy
         self.stream = self.t.cuda.Stream()
         self.streams = [self.t.cuda.Stream() for _ in range(max(1, n_streams))]
-        self.stream64 = self.t.cuda.Stream()
+        # FP64 plain requests: a few streams so that they overlap one another
+        # and the FP32 ticks, taken in turn
+        self.streams64 = [self.t.cuda.Stream() for _ in range(4)]
+        self._next64 = 0
         # one 64-byte work ticket per launch group of a tick
         self.tickets = self.t.zeros(256 * 16, dtype=self.t.int32, device="cuda")
         self.active = []     # FP32 requests on the device: (req, slot, meta)
-        self.active64 = []   # (req, lowered, log, status, event)
+        self.active64 = []   # (req, lowered, layers, log, status, event, plan, buffers kept alive)
         self._next_id = 0
         self.params = np.zeros(1, dtype=batch.F32_PARAMS_DTYPE)
         self.stats = {"ticks": 0, "host_s": 0.0, "device_wait_s": 0.0, "admit_s": 0.0}
@@ -195,28 +200,41 @@ class ServingEngine:
         return True
 
     def _admit_f64(self, req, now):
+        """Lower the request's junctions and launch their FP64 plain run on
+        the next FP64 stream.  The host copies are pinned and asynchronous:
+        the loop never waits for an earlier FP64 request's kernel."""
         plan = engine.plan_run(req.total_time, req.time_step, req.total_time if req.total_time > 0 else 1.0)
         solver = req.junctions[0].getSolver(req.solver)
         from ._lower import lower
         low = lower(req.junctions, plan, solver, False)
-        with self.t.cuda.stream(self.stream64):
-            d_j, d_l = engine.to_device(low.junctions), engine.to_device(low.layers)
-            d_tab = engine.to_device(low.tables) if low.tables is not None else None
+        stream = self.streams64[self._next64 % len(self.streams64)]
+        self._next64 += 1
+        pinned = []
+
+        def up(arr):
+            h = self.t.from_numpy(np.ascontiguousarray(arr).view(np.uint8).reshape(-1).copy()).pin_memory()
+            pinned.append(h)
+            return h.to("cuda", non_blocking=True)
+
+        with self.t.cuda.stream(stream):
+            d_j, d_l = up(low.junctions), up(low.layers)
+            d_tab = up(low.tables) if low.tables is not None else None
             n = len(req.junctions)
             d_log = self.t.empty((n, max(plan.n_log, 1), low.log_width), dtype=self.t.float64, device="cuda")
             d_st = self.t.zeros(2 * n, dtype=self.t.int32, device="cuda")
             rc = self.lib.cmtj_run_simulation_f64(engine.ptr(d_j), n, engine.ptr(d_l), engine.ptr(d_tab),
                                                   low.params.ctypes.data, engine.ptr(d_log), engine.ptr(d_st),
-                                                  engine.stream_ptr(self.stream64))
+                                                  engine.stream_ptr(stream))
             _abi.check(rc, self.lib)
             ev = self.t.cuda.Event()
-            ev.record(self.stream64)
+            ev.record(stream)
         req.id = self._next_id
         self._next_id += 1
         req.admitted_at = now
         req.n = n
         req.layer_steps = float(n * plan.total_iterations * np.mean([j.layerNo for j in req.junctions]))
-        self.active64.append((req, low, d_l, d_log, d_st, ev, plan))
+        # the device and pinned buffers stay referenced until the event
+        self.active64.append((req, low, d_l, d_log, d_st, ev, plan, (d_j, d_tab, pinned)))
         return True
 
     # ------------------------------------------------------------ ticks
@@ -312,7 +330,7 @@ class ServingEngine:
         self.active = keep
         keep64 = []
         for item in self.active64:
-            req, low, d_l, d_log, d_st, ev, plan = item
+            req, low, d_l, d_log, d_st, ev, plan, _ = item
             if ev.query():
                 low.layers = d_l.cpu().numpy().view(_abi.LAYER_DTYPE).copy()
                 from ._lower import apply_results
@@ -363,7 +381,8 @@ class ServingEngine:
                 wait = pending[qi].arrival - now()
                 if wait > 0:
                     time.sleep(min(wait, 0.01))
-        self.stream64.synchronize()
+        for st in self.streams64:
+            st.synchronize()
         return pending
 
 
