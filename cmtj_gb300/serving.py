@@ -148,6 +148,12 @@ class ServingEngine:
         self.ahead = 2
 
     # ------------------------------------------------------------ admission
+    def _pinned(self, arr):
+        """The bytes of a numpy array in pinned host memory, for an
+        asynchronous copy (PyTorch's pinned allocator keeps the block until
+        the copy that reads it is done)."""
+        return self.t.from_numpy(np.ascontiguousarray(arr).view(np.uint8).reshape(-1).copy()).pin_memory()
+
     def _admit(self, req, now):
         if req.precision == "f64":
             return self._admit_f64(req, now)
@@ -177,13 +183,15 @@ class ServingEngine:
             if v < 0:
                 raise ValueError("no FP32 kernel variant for layers=%d features=0x%x" % (nl, code))
             variant[(L * (1 << 24) + own) == key] = v
+        # asynchronous copies from pinned memory, in stream order after the
+        # ticks in flight (the slots are free) and before the next tick
+        # (which waits for the group rebuild recorded after them)
         with self.t.cuda.stream(self.stream):
             JB, LB, SB = (batch.F32_JUNCTION_DTYPE.itemsize, batch.F32_LAYER_DTYPE.itemsize,
                           batch.F32_STATE_DTYPE.itemsize)
-            self.pool.d_j[slot * JB:(slot + n) * JB].copy_(self.t.from_numpy(jr.view(np.uint8)), non_blocking=False)
-            self.pool.d_l[4 * slot * LB:4 * (slot + n) * LB].copy_(self.t.from_numpy(lay.view(np.uint8)),
-                                                                   non_blocking=False)
-            self.pool.d_s[slot * SB:(slot + n) * SB].copy_(self.t.from_numpy(st.view(np.uint8)), non_blocking=False)
+            self.pool.d_j[slot * JB:(slot + n) * JB].copy_(self._pinned(jr), non_blocking=True)
+            self.pool.d_l[4 * slot * LB:4 * (slot + n) * LB].copy_(self._pinned(lay), non_blocking=True)
+            self.pool.d_s[slot * SB:(slot + n) * SB].copy_(self._pinned(st), non_blocking=True)
         req.id = self._next_id
         self._next_id += 1
         req.admitted_at = now
@@ -212,7 +220,7 @@ class ServingEngine:
         pinned = []
 
         def up(arr):
-            h = self.t.from_numpy(np.ascontiguousarray(arr).view(np.uint8).reshape(-1).copy()).pin_memory()
+            h = self._pinned(arr)
             pinned.append(h)
             return h.to("cuda", non_blocking=True)
 
@@ -252,7 +260,8 @@ class ServingEngine:
         with self.t.cuda.stream(self.stream):
             for key, parts in sorted(groups.items()):
                 order = np.concatenate(parts).astype(np.int32)
-                built.append((key, engine.to_device(order), int(order.size)))
+                built.append((key, self._pinned(order).to("cuda", non_blocking=True).view(self.t.int32),
+                              int(order.size)))
         ev = self.t.cuda.Event()
         ev.record(self.stream)  # admission copies and the order uploads
         self._groups = (built, ev)
