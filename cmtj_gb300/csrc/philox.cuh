@@ -47,23 +47,29 @@ __device__ __forceinline__ void cmtj_gaussian3_f64(uint32_t seed_lo, uint32_t se
   g2 = r1 * cos(a1);
 }
 
-// FP32 draws (batched form): the same words, transformed in single precision.
+// FP32 draws (batched form): the same words, transformed in single
+// precision with the hardware approximations; the draws only have to be
+// right in distribution.  Box-Muller with the radius uniforms at 32-bit
+// resolution, (w + 0.5) 2^-32 (tails to 6.8 sigma), and the angle uniforms
+// from the top 23 bits as v in [-1/2, 1/2) (an angle in [-pi, pi), where the
+// hardware sine and cosine are most accurate; the Gaussian pair is
+// rotation invariant).  __logf has a small absolute error near u = 1 that
+// can make -2 log(u) slightly negative; the radius is 0 there.
+__device__ __forceinline__ float cmtj_bm_radius(uint32_t w) {
+  const float u = ((float)w + 0.5f) * 2.3283064365386963e-10f;
+  const float x = -2.0f * __logf(u);
+  return x > 0.f ? x * rsqrtf(x) : 0.f;
+}
+__device__ __forceinline__ float cmtj_bm_angle(uint32_t w) {
+  return 6.2831853f * (__uint_as_float(0x3f800000u | (w >> 9)) - 1.5f);
+}
 __device__ __forceinline__ void cmtj_gaussian3_f32(uint32_t seed_lo, uint32_t seed_hi, uint64_t step,
                                                    float &g0, float &g1, float &g2) {
   const uint4 w = cmtj_thermal_words(seed_lo, seed_hi, step);
-  const float s = 2.3283064365386963e-10f;
-  const float u0 = ((float)w.x + 0.5f) * s, u1 = ((float)w.y + 0.5f) * s;
-  const float u2 = ((float)w.z + 0.5f) * s, u3 = ((float)w.w + 0.5f) * s;
-  // (float)w rounds to 24 bits, so u may round to exactly 1.0 (r = 0).
-  // __logf (the hardware log2 scaled by ln 2) has a small absolute error
-  // near u = 1 that can make -2 log(u) slightly negative there; the clamp
-  // keeps r >= 0.  The draws only have to be right in distribution.
-  const float r0 = sqrtf(fmaxf(-2.0f * __logf(u0), 0.f));
-  const float r1 = sqrtf(fmaxf(-2.0f * __logf(u2), 0.f));
-  float s0, c0, s1, c1;
-  sincospif(2.0f * u1, &s0, &c0);
-  sincospif(2.0f * u3, &s1, &c1);
+  const float r0 = cmtj_bm_radius(w.x), r1 = cmtj_bm_radius(w.z);
+  float s0, c0;
+  __sincosf(cmtj_bm_angle(w.y), &s0, &c0);
   g0 = r0 * c0;
   g1 = r0 * s0;
-  g2 = r1 * c1;
+  g2 = r1 * __cosf(cmtj_bm_angle(w.w));
 }

@@ -65,8 +65,9 @@ def build_variant(minb, layers=(2,)):
 
 def time_library(lib, n_h, n_draw, steps, reps, workload="pimm"):
     """Runs in a fresh process: loads `lib` and times one batch: the 2-layer
-    PIMM sweep, or (workload "vsd") the uneven 1-4-layer spin-diode sweep
-    at its own durations."""
+    PIMM sweep, (workload "vsd") the uneven 1-4-layer spin-diode sweep at
+    its own durations, or (workload "pbit") the thermal single-layer p-bit
+    sweep, n_h currents x n_draw junctions, Euler-Heun at 300 K."""
     import numpy as np
     import torch
     from . import _abi
@@ -78,6 +79,13 @@ def time_library(lib, n_h, n_draw, steps, reps, workload="pimm"):
         low = batch.lower(spec, dt, ns)
         run = batch.BatchRun(low, dt, batch.SolverMode.RK4, batch.LOG_NONE, 0, red_every=1)
         layer_steps = float((ns * spec.n_layers).sum())
+    elif workload == "pbit":
+        # n_h currents x n_draw junctions, `steps` Euler-Heun steps each at 300 K
+        spec, _, _ = sweeps.pbit_config(n_j=n_h, n_per=n_draw, dt=dt, t_min=steps * dt, t_max=steps * dt)
+        ns = np.full(spec.n, steps, dtype=np.int64)
+        low = batch.lower(spec, dt, ns)
+        run = batch.BatchRun(low, dt, batch.SolverMode.EulerHeun, batch.LOG_NONE, 0)
+        layer_steps = float(spec.n * steps)
     else:
         spec, ns = sweeps.pimm_config(n_h=n_h, n_draw=n_draw, dt=dt, total=steps * dt)
         low = batch.lower(spec, dt, ns)
@@ -171,7 +179,7 @@ def main(argv=None):
     ap.add_argument("--n-h", type=int, default=512)
     ap.add_argument("--n-draw", type=int, default=512)
     ap.add_argument("--reps", type=int, default=3)
-    ap.add_argument("--workload", default="pimm", choices=["pimm", "vsd"])
+    ap.add_argument("--workload", default="pimm", choices=["pimm", "vsd", "pbit"])
     ap.add_argument("--fp64", action="store_true", help="time the FP64 fixed-step lane layouts instead")
     ap.add_argument("--n", type=int, nargs="+", default=[1, 64, 1024, 16384], help="--fp64 batch sizes")
     ap.add_argument("--lanes", type=int, nargs="+", default=[0, 1, 4], help="--fp64 lanes per layer")
