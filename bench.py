@@ -244,6 +244,26 @@ def groups_16(cm, n_groups=64):
     return out
 
 
+def pimm_procedure_case(cm):
+    """PIMM_procedure over a list of 64 two-layer MTJs (the R(H) sweep's
+    junction with Ku(free) over 1e5..6e5 J/m^3), 10 fields over +-300 kA/m
+    along x, 0.5 ns per point, 1 kA/m Oersted step."""
+    import cases
+    from cmtj_gb300 import procedures
+    js = []
+    for k in range(64):
+        j, _ = cases.mtj_rh_point(cm, hx=0.0)
+        j.setLayerAnisotropyDriver("free", cm.constantDriver(1e5 + 5e5 * k / 63))
+        js.append(j)
+    H = np.linspace(-300e3, 300e3, 10)
+    RP = procedures.ResistanceParameters
+    kw = dict(Hvecs=np.stack([H, 0 * H, 0 * H], 1), int_step=DT,
+              resistance_params=[RP(Rxx0=100, Rxy0=5, Ramr=-0.24, Rahe=-0.3, Rsmr=-0.46, w=3e-5, l=2e-5)] * 2,
+              Hoe_excitation=1e3, simulation_duration=5e-10, disturbance=0.0, take_last_n=50, max_frequency=80e9,
+              disable_tqdm=True)
+    return js, kw
+
+
 def final_m(junctions):
     return np.array([[(l.mag.x, l.mag.y, l.mag.z) for l in j.layers] for j in junctions])
 
@@ -290,7 +310,21 @@ def cpu_baseline(budget_s=15.0):
     oracle_harness.run_groups_oracle(gs, 2e-10, DT, 1e-12)
     grp = {"seconds": time.perf_counter() - t0, "cores": 1,
            "final_m": np.concatenate([final_m(g.junctionList) for g in gs])}
+    # PIMM_procedure with the oracle as its FP64 runner
+    from cmtj_gb300 import procedures
+    js, kw = pimm_procedure_case(ocm)
+    run_f64 = procedures._run_f64
+    procedures._run_f64 = lambda junctions, duration, int_step: oracle_harness.run_oracle(
+        junctions, duration, int_step, int_step, threads=cores)
+    try:
+        t0 = time.perf_counter()
+        res = procedures.PIMM_procedure(js, precision="f64", **kw)
+        proc = {"seconds": time.perf_counter() - t0, "cores": cores,
+                "spectra": np.stack([r[0] for r in res])}
+    finally:
+        procedures._run_f64 = run_f64
     return {"value": rate, "unit": UNIT, "cores": cores, "kind": "port", "rh_config0": rh, "dp": dp, "group": grp,
+            "procedure": proc,
             "reference_flop_per_layer_step": ref_fpls, "reference_flop_breakdown": fcount,
             "sample": "%d PIMM junctions x %d RK4 steps (full 5 ns solves) on %d threads (%.1f s)"
                       % (n2, n_steps, cores, el)}
@@ -592,6 +626,12 @@ def measure_rest(run, low, spec, n_steps, kern_ms, fft_ms, lib):
         gpu = out["other_workloads"][leg]
         gpu["max_abs_dm_vs_oracle"] = float(np.max(np.abs(gpu.pop("final_m") - cpu.pop("final_m"))))
         gpu["cpu_oracle"] = cpu
+    cpu = out["cpu_baseline"].pop("procedure")
+    gpu = out["other_workloads"]["pimm_procedure_64x10"]
+    ref = cpu.pop("spectra")
+    gpu["max_rel_spectrum_diff_fp64_vs_oracle"] = float(np.max(np.abs(gpu.pop("spectra_f64") - ref)) / np.max(ref))
+    gpu["max_rel_spectrum_diff_fp32_vs_oracle"] = float(np.max(np.abs(gpu.pop("spectra_f32") - ref)) / np.max(ref))
+    gpu["cpu_oracle"] = cpu
     # the reference's own arithmetic per layer-step, counted in the CPU leg
     out["roofline"]["reference_flop_per_layer_step"] = out["cpu_baseline"].pop("reference_flop_per_layer_step")
     out["roofline"]["reference_flop_breakdown_add_mul_div_sqrt_trans"] = out["cpu_baseline"].pop(
@@ -721,6 +761,19 @@ def other_workloads():
                                   "final_m": np.concatenate([final_m(g.junctionList) for g in gs]),
                                   "sample": "64 groups of 16 junctions on a 4x4 grid, Kanao dipole coupling, "
                                             "2000 RK4 steps, FP64 plain form, one CTA per group"}
+    # PIMM_procedure (the procedure front-end) over 64 junctions x 10 fields,
+    # each point one launch for all 64 chains, FP64 plain and FP32 batched
+    from cmtj_gb300 import procedures
+    leg = {"sample": "PIMM_procedure on a list of 64 two-layer MTJs, 10 fields, 0.5 ns per point"}
+    for prec in ("f64", "f32"):
+        js, kw = pimm_procedure_case(cm)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res = procedures.PIMM_procedure(js, precision=prec, **kw)
+        torch.cuda.synchronize()
+        leg["seconds_" + prec] = time.perf_counter() - t0
+        leg["spectra_" + prec] = np.stack([r[0] for r in res])
+    out["pimm_procedure_64x10"] = leg
     # 16-junction series stack, FP64 plain form
     js = [cases._stt_junction(cm, 1.0 + 0.02 * k, 1e3 + 50 * k, (0.1, 0.2, 1), (1, 0, 0)) for k in range(16)]
     s = cm.stack.SeriesStack(js)
