@@ -3,10 +3,11 @@
 // Gaussian draws built on it.
 //
 // Stream definition (shared by every solver form, so FP32 and FP64 runs see
-// the same noise up to rounding): for a layer with key (seed_lo, seed_hi) at
-// absolute step s, one Philox block with counter {s_lo, s_hi, 0x7E4D, 0}
-// gives four words w0..w3; u_k = (w_k + 0.5) * 2^-32 lies in (0, 1); the
-// Box-Muller transform gives g0, g1 from (u0, u1) and g2 from (u2, u3).
+// the same noise up to the FP32 transform's error): for a layer with key
+// (seed_lo, seed_hi) at absolute step s, one Philox block with counter
+// {s_lo, s_hi, 0x7E4D, 0} gives four words w0..w3; u_k = (w_k + 0.5) * 2^-32
+// lies in (0, 1); the Box-Muller transform gives g0, g1 from (u0, u1) and g2
+// from (u2, u3).
 #pragma once
 #include <stdint.h>
 
@@ -48,13 +49,14 @@ __device__ __forceinline__ void cmtj_gaussian3_f64(uint32_t seed_lo, uint32_t se
 }
 
 // FP32 draws (batched form): the same words, transformed in single
-// precision with the hardware approximations; the draws only have to be
-// right in distribution.  Box-Muller with the radius uniforms at 32-bit
-// resolution, (w + 0.5) 2^-32 (tails to 6.8 sigma), and the angle uniforms
-// from the top 23 bits as v in [-1/2, 1/2) (an angle in [-pi, pi), where the
-// hardware sine and cosine are most accurate; the Gaussian pair is
-// rotation invariant).  __logf has a small absolute error near u = 1 that
-// can make -2 log(u) slightly negative; the radius is 0 there.
+// precision with the hardware approximations (the draws only have to be
+// right in distribution; they agree with the FP64 draws to a few 1e-6).
+// The radius uniforms keep 32 bits, (w + 0.5) 2^-32 (tails to 6.8 sigma).
+// The angle uniform comes from the top 23 bits as v = u - 1/2 in
+// [-1/2, 1/2), where the hardware sine and cosine are most accurate; the
+// angle 2 pi v is the FP64 angle minus pi, so the products are negated to
+// give the FP64 draws' signs.  __logf has a small absolute error near u = 1
+// that can make -2 log(u) slightly negative; the radius is 0 there.
 __device__ __forceinline__ float cmtj_bm_radius(uint32_t w) {
   const float u = ((float)w + 0.5f) * 2.3283064365386963e-10f;
   const float x = -2.0f * __logf(u);
@@ -69,7 +71,7 @@ __device__ __forceinline__ void cmtj_gaussian3_f32(uint32_t seed_lo, uint32_t se
   const float r0 = cmtj_bm_radius(w.x), r1 = cmtj_bm_radius(w.z);
   float s0, c0;
   __sincosf(cmtj_bm_angle(w.y), &s0, &c0);
-  g0 = r0 * c0;
-  g1 = r0 * s0;
-  g2 = r1 * __cosf(cmtj_bm_angle(w.w));
+  g0 = -r0 * c0;
+  g1 = -r0 * s0;
+  g2 = -r1 * __cosf(cmtj_bm_angle(w.w));
 }
