@@ -155,7 +155,7 @@ def _run_point(junctions, duration, int_step, precision):
     keys for m, R and time."""
     if precision == "f64":
         _run_f64(junctions, duration, int_step)
-        return [{k: np.asarray(v) for k, v in j.getLog().items()} for j in junctions]
+        return [j.getLogArrays() for j in junctions]
     if precision != "f32":
         raise ValueError("precision must be 'f64' or 'f32'")
     from . import batch
