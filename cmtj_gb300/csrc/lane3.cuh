@@ -24,7 +24,7 @@ static __device__ __forceinline__ bool quad_owner() { return (threadIdx.x & 3) !
 static __device__ __forceinline__ int quad_lead() { return (threadIdx.x & 31) & ~3; }
 static __device__ __forceinline__ unsigned quad_mask() { return 0xFu << quad_lead(); }
 static __device__ __forceinline__ double quad_get(double v, int k) {
-  return __shfl_sync(quad_mask(), v, quad_lead() + k);
+  return __shfl_sync(quad_mask(), v, k, 4);  // lane k of this lane's quad
 }
 
 struct C3 {
