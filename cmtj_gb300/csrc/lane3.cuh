@@ -7,9 +7,9 @@
 // three products gathered from the quad, a cross product component is
 // a_i*b_j - a_j*b_i from the quad's other two lanes, and a tensor row is
 // (t0*mx + t1*my) + t2*mz.  Values therefore do not depend on the layout.
-// A warp FP64 instruction costs the same with one active lane or 32, so
-// spreading the components cuts the instructions on a step's chain about
-// 2.5-fold.  The lanes of a quad always take the same branches (they hold
+// A step is bound by the latency of its dependent chain, and idle lanes
+// cost little, so spreading the components cuts the FP64 instructions on
+// the chain about 2.5-fold for a few shuffles.  The lanes of a quad always take the same branches (they hold
 // one layer), so the quad-masked shuffles below are always converged.
 #pragma once
 #include "plain_f64.cuh"

@@ -14,10 +14,10 @@
 // depend on the layout.  The serial chain of a step is one layer's instead
 // of n layers'.
 //
-// The chain is latency-bound: a warp FP64 instruction occupies the SM
-// sub-partition's FP64 unit for the same time with one active lane or 32,
-// so idle lanes cost nothing and the quad layout, with about 2.5x fewer
-// instructions per step, is the faster one until the batch fills the GPU.
+// A step is bound by the latency of its dependent chain of FP64 operations
+// and shuffles, not by the FP64 pipe, and idle lanes cost little, so the
+// quad layout, with about 2.5x fewer FP64 instructions on the chain, is the
+// faster one until the batch fills the GPU.
 // A block is one warp; blocks spread over the SMs.  Driver slots whose
 // driver is constant are read directly (slot mask per lane), and the four
 // RK4 stages run as a rolled loop so the field code is compiled once per
