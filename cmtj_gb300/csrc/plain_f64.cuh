@@ -324,7 +324,7 @@ static __device__ __forceinline__ V langevin(const cmtj_layer_t &L, const cmtj_c
 // for the n layers of one junction.  single_layer: runSingleLayerSolver is
 // in force (a Stack whose last junction has one layer steps only layer 0 of
 // every junction).  Returns false on a NaN magnetisation (rk4_step throws).
-static __device__ bool junction_step(int n, const cmtj_layer_t *Ls, D3 *mag, D3 *work, Side *side, uint32_t i, double t,
+static __device__ __noinline__ bool junction_step(int n, const cmtj_layer_t *Ls, D3 *mag, D3 *work, Side *side, uint32_t i, double t,
                               const cmtj_sim_params_t &p, const double *tables, const cmtj_driver_t *cur,
                               bool single_layer) {
   const cmtj_constants_t c = p.c;
