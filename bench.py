@@ -246,20 +246,23 @@ def groups_16(cm, n_groups=64):
 
 def pimm_procedure_case(cm):
     """PIMM_procedure over a list of 64 two-layer MTJs (the R(H) sweep's
-    junction with Ku(free) over 1e5..6e5 J/m^3), 10 fields over +-300 kA/m
-    along x, 0.5 ns per point, 1 kA/m Oersted step."""
+    junction with Ku(free) over 1e5..6e5 J/m^3) swept from saturation
+    downwards along +x (800 to 350 kA/m, 10 fields, no switching on the way:
+    a well-conditioned chain), 0.5 ns per point, a 20 kA/m Oersted step."""
     import cases
     from cmtj_gb300 import procedures
     js = []
     for k in range(64):
         j, _ = cases.mtj_rh_point(cm, hx=0.0)
         j.setLayerAnisotropyDriver("free", cm.constantDriver(1e5 + 5e5 * k / 63))
+        j.setLayerMagnetisation("free", cm.CVector(1, 0, 0.1))
+        j.setLayerMagnetisation("ref", cm.CVector(1, 0, 0.2))
         js.append(j)
-    H = np.linspace(-300e3, 300e3, 10)
+    H = np.linspace(800e3, 350e3, 10)
     RP = procedures.ResistanceParameters
     kw = dict(Hvecs=np.stack([H, 0 * H, 0 * H], 1), int_step=DT,
               resistance_params=[RP(Rxx0=100, Rxy0=5, Ramr=-0.24, Rahe=-0.3, Rsmr=-0.46, w=3e-5, l=2e-5)] * 2,
-              Hoe_excitation=1e3, simulation_duration=5e-10, disturbance=0.0, take_last_n=50, max_frequency=80e9,
+              Hoe_excitation=2e4, simulation_duration=5e-10, disturbance=0.0, take_last_n=50, max_frequency=80e9,
               disable_tqdm=True)
     return js, kw
 
