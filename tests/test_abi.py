@@ -44,3 +44,13 @@ def test_struct_layout_and_version(lib):
     _abi.check_layout(lib)
     assert lib.cmtj_log_width(2, 0) == _abi.log_width(2, False) == 10
     assert lib.cmtj_log_width(3, 1) == 3 * 29 + 4
+
+
+def test_feature_constants_mirror_header():
+    """The Python mirrors of the header's FP32 feature flags."""
+    src = open(os.path.join(ROOT, "include", "cmtj_gpu.h")).read()
+    defs = {k: int(v, 0) for k, v in re.findall(r"#define (CMTJ_\w+)\s+(0x[0-9a-fA-F]+|\d+)", src)}
+    from cmtj_gb300 import batch
+    for name in ("FULL_DEMAG", "DIPOLE", "IDMI", "K2", "STT", "SOT", "WAVES", "SCALAR_WAVES", "IEC2", "OFFAXIS",
+                 "ALL"):
+        assert defs["CMTJ_FEAT_" + name] == getattr(batch, "FEAT_" + name), name
