@@ -88,7 +88,7 @@ def compute_spectrum_strip(input_m, int_step, max_frequency):
 
 
 class FieldScan:
-    """linear.py:6-84 (the constructors the procedures are fed with)."""
+    """cmtj/utils/linear.py:6-124: field-vector constructors for sweeps."""
 
     @staticmethod
     def _trig_compute(theta, phi):
@@ -99,6 +99,31 @@ class FieldScan:
     def angle2vector(theta, phi, amplitude=1):
         st, ct, sp, cp = FieldScan._trig_compute(theta, phi)
         return CVector(st * cp * amplitude, st * sp * amplitude, ct * amplitude)
+
+    @staticmethod
+    def vector2angle(x, y, z):
+        """(theta, phi, r) in degrees of a cartesian vector."""
+        r = np.sqrt(x ** 2 + y ** 2 + z ** 2)
+        return np.rad2deg(np.arctan2(np.sqrt(x ** 2 + y ** 2), z)), np.rad2deg(np.arctan2(y, x)), r
+
+    @staticmethod
+    def cvector2angle(vector):
+        return FieldScan.vector2angle(vector.x, vector.y, vector.z)
+
+    @staticmethod
+    def theta_scan(start, stop, steps, amplitude, phi):
+        """Polar-angle sweep at fixed amplitude and azimuth (degrees)."""
+        span = np.linspace(start, stop, endpoint=True, num=steps)
+        st, ct, sp, cp = FieldScan._trig_compute(span, phi)
+        return span, np.vstack((st * cp * amplitude, st * sp * amplitude, ct * amplitude)).T
+
+    @staticmethod
+    def phi_scan(start, stop, steps, amplitude, theta):
+        """Azimuth sweep at fixed amplitude and polar angle (degrees)."""
+        span = np.linspace(start, stop, endpoint=True, num=steps)
+        st, ct, sp, cp = FieldScan._trig_compute(theta, span)
+        Hy = st * sp * amplitude
+        return span, np.vstack((st * cp * amplitude, Hy, ct * amplitude * np.ones_like(Hy))).T
 
     @staticmethod
     def amplitude_scan(start, stop, steps, theta, phi, back=False):
