@@ -63,7 +63,7 @@ def build_variant(minb, layers=(2,)):
     return lib
 
 
-def time_library(lib, n_h, n_draw, steps, reps, workload="pimm"):
+def time_library(lib, n_h, n_draw, steps, reps, workload="pimm", vsd_shape=(128, 1024, 5.0, 50.0)):
     """Runs in a fresh process: loads `lib` and times one batch: the 2-layer
     PIMM sweep, (workload "vsd") the uneven 1-4-layer spin-diode sweep at
     its own durations, or (workload "pbit") the thermal single-layer p-bit
@@ -75,7 +75,8 @@ def time_library(lib, n_h, n_draw, steps, reps, workload="pimm"):
     from . import batch, sweeps
     dt = 1e-13
     if workload == "vsd":
-        spec, ns = sweeps.vsd_config(dt=dt)
+        n_f, n_hv, t_lo, t_hi = vsd_shape
+        spec, ns = sweeps.vsd_config(n_f=int(n_f), n_h=int(n_hv), dt=dt, t_min=t_lo * 1e-9, t_max=t_hi * 1e-9)
         low = batch.lower(spec, dt, ns)
         run = batch.BatchRun(low, dt, batch.SolverMode.RK4, batch.LOG_NONE, 0, red_every=1)
         layer_steps = float((ns * spec.n_layers).sum())
@@ -183,6 +184,9 @@ def main(argv=None):
     ap.add_argument("--fp64", action="store_true", help="time the FP64 fixed-step lane layouts instead")
     ap.add_argument("--n", type=int, nargs="+", default=[1, 64, 1024, 16384], help="--fp64 batch sizes")
     ap.add_argument("--lanes", type=int, nargs="+", default=[0, 1, 4], help="--fp64 lanes per layer")
+    ap.add_argument("--vsd-shape", type=float, nargs=4, default=[128, 1024, 5.0, 50.0],
+                    metavar=("FREQS", "FIELDS", "T_MIN_NS", "T_MAX_NS"),
+                    help="spin-diode sweep: frequencies x fields, durations uniform in [T_MIN, T_MAX] ns")
     ap.add_argument("--time-lib", help=argparse.SUPPRESS)
     a = ap.parse_args(argv)
     if a.fp64:
@@ -192,14 +196,15 @@ def main(argv=None):
                 print(json.dumps(time_fp64(n, a.steps, a.reps, lanes)), flush=True)
         return
     if a.time_lib:
-        print(json.dumps(time_library(a.time_lib, a.n_h, a.n_draw, a.steps, a.reps, a.workload)), flush=True)
+        print(json.dumps(time_library(a.time_lib, a.n_h, a.n_draw, a.steps, a.reps, a.workload,
+                                      tuple(a.vsd_shape))), flush=True)
         return
     results = []
     for mb in a.minb:
         lib = build_variant(mb, a.layers)
         out = subprocess.run([sys.executable, "-m", "cmtj_gb300.tune", "--time-lib", lib, "--steps", str(a.steps),
                               "--n-h", str(a.n_h), "--n-draw", str(a.n_draw), "--reps", str(a.reps),
-                              "--workload", a.workload],
+                              "--workload", a.workload, "--vsd-shape", *[str(x) for x in a.vsd_shape]],
                              capture_output=True, text=True, cwd=os.path.dirname(B.PKG))
         if out.returncode:
             raise RuntimeError(out.stderr)
