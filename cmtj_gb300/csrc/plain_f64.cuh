@@ -1,7 +1,8 @@
-// FP64 plain-form device physics shared by the single-junction kernel
-// (plain_f64.cu) and the stack kernel (stack_f64.cu).  Every expression keeps
-// the reference's operand order; units that include this header are compiled
-// with --fmad=false so nothing is contracted into an FMA.
+// FP64 plain-form device physics shared by every FP64 kernel (single
+// junctions, stacks, groups; a thread or lanes per junction).  Every
+// expression keeps the reference's operand order; units that include this
+// header are compiled with --fmad=false so nothing is contracted into an
+// FMA.
 #pragma once
 #include "common.cuh"
 #include "philox.cuh"
@@ -321,9 +322,12 @@ static __device__ __forceinline__ V langevin(const cmtj_layer_t &L, const cmtj_c
 
 
 // One iteration of the runner chosen by getSolver (junction.hpp:1668-1815)
-// for the n layers of one junction.  single_layer: runSingleLayerSolver is
-// in force (a Stack whose last junction has one layer steps only layer 0 of
-// every junction).  Returns false on a NaN magnetisation (rk4_step throws).
+// for the n layers of one junction, on one thread (the stack and group
+// kernels for stacks and groups too wide for lanes; out of line, since they
+// run rarely and it shortens their build).  single_layer:
+// runSingleLayerSolver is in force (a Stack whose last junction has one
+// layer steps only layer 0 of every junction).  Returns false on a NaN
+// magnetisation (rk4_step throws).
 static __device__ __noinline__ bool junction_step(int n, const cmtj_layer_t *Ls, D3 *mag, D3 *work, Side *side, uint32_t i, double t,
                               const cmtj_sim_params_t &p, const double *tables, const cmtj_driver_t *cur,
                               bool single_layer) {
