@@ -150,3 +150,25 @@ def test_dormand_prince_layouts_give_identical_bits(gpu_lib, monkeypatch):
             assert np.array_equal(la[k], lb[k]), k
         assert (a.layers[0].mag.x, a.layers[0].mag.y, a.layers[0].mag.z) == \
                (b.layers[0].mag.x, b.layers[0].mag.y, b.layers[0].mag.z)
+
+
+@pytest.mark.gpu
+def test_layer_bound_below_a_junctions_layers_is_an_error(gpu_lib, monkeypatch):
+    """cmtj_sim_params_t.max_layers bounds every junction's layer count: a
+    3-layer junction launched with max_layers = 2 gets
+    CMTJ_STATUS_BAD_INPUT, which the host raises, and keeps its m."""
+    from cmtj_gb300 import _lower, engine
+    orig = _lower.make_params
+
+    def make_params(*a, **k):
+        p = orig(*a, **k)
+        p["max_layers"] = 2
+        return p
+
+    monkeypatch.setattr(_lower, "make_params", make_params)
+    j, _ = cases.tri_layer(cmtj_gb300)
+    assert j.layerNo == 3
+    m0 = [(l.mag.x, l.mag.y, l.mag.z) for l in j.layers]
+    with pytest.raises(RuntimeError, match="status 3"):
+        engine.run_junctions([j], engine.plan_run(1e-12, 1e-13, 1e-13), cmtj_gb300.SolverMode.RK4)
+    assert [(l.mag.x, l.mag.y, l.mag.z) for l in j.layers] == m0
