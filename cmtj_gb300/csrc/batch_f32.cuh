@@ -700,6 +700,9 @@ template <int L> __device__ __forceinline__ int log_channels(int mode) {
 #ifndef CMTJ_BATCH_MINB_PACKED
 #define CMTJ_BATCH_MINB_PACKED CMTJ_BATCH_MINB
 #endif
+#ifndef CMTJ_BATCH_MINB_STOCH
+#define CMTJ_BATCH_MINB_STOCH 4  // Euler-Heun / Heun variants (the p-bit sweep: 4 beat 5 and 6 by 6-7 %)
+#endif
 #ifndef CMTJ_BATCH_MINB_WIDE
 #define CMTJ_BATCH_MINB_WIDE 2  // packed 3- and 4-layer variants (best of 2/3/4/5 measured)
 #endif
@@ -714,7 +717,7 @@ template <int L, int SOLVER, int FEAT>
 __host__ __device__ constexpr int min_blocks() {
   return FEAT == CMTJ_FEAT_ALL ? 1
          : (packed_variant<L, SOLVER, FEAT>() ? (L == 2 ? CMTJ_BATCH_MINB_PACKED : CMTJ_BATCH_MINB_WIDE)
-                                               : CMTJ_BATCH_MINB);
+                                               : (SOLVER == CMTJ_RK4 ? CMTJ_BATCH_MINB : CMTJ_BATCH_MINB_STOCH));
 }
 
 template <int L, int SOLVER, int FEAT, int NW>

@@ -40,7 +40,7 @@ def build_variant(minb, layers=(2,)):
     out = os.path.join(B.BUILD, "tune_mb%d" % minb)
     os.makedirs(out, exist_ok=True)
     flags = ["-DCMTJ_BATCH_MINB=%d" % minb, "-DCMTJ_BATCH_MINB_PACKED=%d" % minb,
-             "-DCMTJ_BATCH_MINB_WIDE=%d" % minb]
+             "-DCMTJ_BATCH_MINB_WIDE=%d" % minb, "-DCMTJ_BATCH_MINB_STOCH=%d" % minb]
     tuned = {"batch_f32_l%d.cu" % L for L in layers}
     objs = []
     jobs = []
