@@ -41,17 +41,98 @@ __device__ __forceinline__ LaneGeo lane_geo(int G) {
   return g;
 }
 
+// A field-only layer: no dipole, IDMI, second-order anisotropy or
+// biquadratic IEC term (CMTJ_ZERO_*), no STT and no SOT.  With constant
+// drivers, everything rhs() reads for such a layer except m and the
+// neighbours is fixed for the whole run; FieldOnly holds it in registers.
+__device__ __forceinline__ bool field_only(const cmtj_layer_t &L) {
+  const uint32_t all = CMTJ_ZERO_DIPOLE | CMTJ_ZERO_IDMI | CMTJ_ZERO_K2 | CMTJ_ZERO_J2;
+  return (L.zero_terms & all) == all && !L.includeSTT && !L.includeSOT;
+}
+
+template <class V>
+struct FieldOnly {
+  V Hext, Hoe, Hdmi, Hres, anis;
+  double K, Jb, Jt, Ms, Mst, ms_mu0, damping, conv, gyro;
+  const double *demag;
+};
+
+// The constants of a field-only layer whose driver slots are all constant
+// (each slot reads constantValue, as slot_at does with a zero slot mask).
+template <class V>
+__device__ __forceinline__ FieldOnly<V> field_only_load(const cmtj_layer_t &L, const cmtj_constants_t &c) {
+  const DriverCtx dc = {nullptr, 0u, 0};
+  FieldOnly<V> f;
+  f.Hext = V::axial(L, CMTJ_SLOT_HEXT, 0.0, dc, 0u);
+  f.Hoe = V::axial(L, CMTJ_SLOT_HOE, 0.0, dc, 0u);
+  f.Hdmi = V::axial(L, CMTJ_SLOT_HDMI, 0.0, dc, 0u);
+  f.Hres = V::axial(L, CMTJ_SLOT_HRES, 0.0, dc, 0u);
+  f.anis = V::load(L.anis);
+  f.K = L.drv[CMTJ_SLOT_ANIS].constantValue;
+  f.Jb = L.drv[CMTJ_SLOT_IEC_BOTTOM].constantValue;
+  f.Jt = L.drv[CMTJ_SLOT_IEC_TOP].constantValue;
+  f.Ms = L.Ms;
+  f.Mst = L.Ms * L.thickness;
+  f.ms_mu0 = L.ms_over_mu0;
+  f.damping = L.damping;
+  f.conv = L.conv_term;
+  f.gyro = c.gyro;
+  f.demag = L.demag;
+  return f;
+}
+
+// rhs()'s IEC term of a field-only layer (the CMTJ_ZERO_J2 form), which
+// depends only on the neighbours, frozen for an RK4 step.
+template <class V>
+__device__ __forceinline__ V field_only_iec(const FieldOnly<V> &f, const V &bottom, const V &top) {
+  const bool zb = is_zero3(bottom), ztop = is_zero3(top);
+  if (!zb && !ztop) return (bottom * f.Jb) / f.Mst + (top * f.Jt) / f.Mst;
+  if (!zb) return (bottom * f.Jb) / f.Mst;
+  if (!ztop) return (top * f.Jt) / f.Mst;
+  return V::zero();
+}
+
+// rhs() (calculateHeff + solveLLG, junction.hpp:580-815) of a field-only
+// layer: the same operations in the same order, with the terms rhs()
+// leaves out for such a layer absent and the constant ones preloaded.
+template <class V>
+__device__ __forceinline__ V rhs_field_only(const FieldOnly<V> &f, const V &m, const V &Hiec,
+                                            typename NoDeduce<SideT<V>>::type *side) {
+  const V Hdemag = tensor_mul(m, f.demag, f.ms_mu0);
+  const V Hanis = f.anis * ((2 * f.K) * dot(f.anis, m) / f.Ms);
+  V H = f.Hext + Hanis;
+  H = H + Hiec;
+  H = H + f.Hoe + f.Hdmi - Hdemag;
+  H = H + f.Hres;
+  if (side) {
+    side->K = f.K;
+    side->K2 = 0.0;
+    side->Jb = f.Jb;
+    side->Jt = f.Jt;
+    side->Hext = f.Hext;
+    side->Hiec = Hiec;
+    side->Hanis = Hanis;
+    side->Hdemag = Hdemag;
+  }
+  const V prod = cross(m, H);
+  const V prod2 = cross(m, prod);
+  const V dmdt = prod + prod2 * f.damping;
+  return dmdt * -f.gyro * f.conv;
+}
+
 // One iteration of the fixed-step runner (RK4, Euler-Heun or Heun;
 // core/junction.hpp:1668-1815) for the lane's layer of a junction whose
 // n layers step (1 under runSingleLayerSolver).  cur overrides the current
-// driver (stacks), hres the reserved interaction field (groups).  Returns
-// the first layer whose m became NaN (RK4: the layers above it keep their
-// start-of-step m, as when rk4_step throws), or -1.
+// driver (stacks), hres the reserved interaction field (groups).  fo: RK4
+// only, the layer is field-only with constant drivers (FieldOnly).
+// Returns the first layer whose m became NaN (RK4: the layers above it
+// keep their start-of-step m, as when rk4_step throws), or -1.
 template <int SOLVER, class V>
 __device__ __forceinline__ int lane_step(const cmtj_layer_t &L, const cmtj_constants_t &c, V &mag,
                                          SideT<V> &side, bool step, const LaneGeo &g, int n, uint32_t i, double t,
                                          double dt, const double *tables, bool energies,
-                                         const cmtj_driver_t *cur, uint32_t dyn, const double *hres = nullptr) {
+                                         const cmtj_driver_t *cur, uint32_t dyn, const double *hres = nullptr,
+                                         const FieldOnly<V> *fo = nullptr) {
   // neighbours at the start of the step; zero beyond the stack's ends
   V below = shfl_vec(mag, g.below_src), above = shfl_vec(mag, g.above_src);
   if (g.l == 0) below = V::zero();
@@ -63,13 +144,23 @@ __device__ __forceinline__ int lane_step(const cmtj_layer_t &L, const cmtj_const
     bool nan = false;
     if (step) {
       V k = V::zero(), acc = V::zero();
+      if (fo) {
+        const V hiec = field_only_iec(*fo, below, above);
 #pragma unroll 1
-      for (int s = 0; s < 4; ++s) {
-        const double ts = s == 0 ? t : (s == 3 ? t + dt : t + 0.5 * dt);
-        const V mi = s == 0 ? mag : (s == 3 ? mag + k : mag + k * 0.5);
-        const DriverCtx dc = {tables, i, s == 0 ? 0 : (s == 3 ? 2 : 1)};
-        k = rhs(L, c, ts, mi, below, above, dc, (s == 3 && energies) ? &side : nullptr, cur, dyn, hres) * dt;
-        acc = s == 0 ? k : acc + (s == 3 ? k : k * 2.0);
+        for (int s = 0; s < 4; ++s) {
+          const V mi = s == 0 ? mag : (s == 3 ? mag + k : mag + k * 0.5);
+          k = rhs_field_only(*fo, mi, hiec, (s == 3 && energies) ? &side : nullptr) * dt;
+          acc = s == 0 ? k : acc + (s == 3 ? k : k * 2.0);
+        }
+      } else {
+#pragma unroll 1
+        for (int s = 0; s < 4; ++s) {
+          const double ts = s == 0 ? t : (s == 3 ? t + dt : t + 0.5 * dt);
+          const V mi = s == 0 ? mag : (s == 3 ? mag + k : mag + k * 0.5);
+          const DriverCtx dc = {tables, i, s == 0 ? 0 : (s == 3 ? 2 : 1)};
+          k = rhs(L, c, ts, mi, below, above, dc, (s == 3 && energies) ? &side : nullptr, cur, dyn, hres) * dt;
+          acc = s == 0 ? k : acc + (s == 3 ? k : k * 2.0);
+        }
       }
       next = normalized(mag + acc / 6.0);
       nan = x_is_nan(next);

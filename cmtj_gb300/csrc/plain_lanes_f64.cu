@@ -21,7 +21,9 @@
 // A block is one warp; blocks spread over the SMs.  Driver slots whose
 // driver is constant are read directly (slot mask per lane), and the four
 // RK4 stages run as a rolled loop so the field code is compiled once per
-// kernel.
+// kernel.  A warp whose layers are all field-only with constant drivers
+// (RK4) runs a variant without the per-term branches, with the layer
+// constants in registers and the IEC term formed once per step.
 //
 // This unit is compiled with --fmad=false like plain_f64.cu.
 #include "plain_lanes.cuh"
@@ -33,8 +35,9 @@ namespace {
 
 // The whole run of the warp's junctions.  DYN = false when no layer of the
 // warp has a time-dependent driver slot: every slot then reads its
-// constantValue, a loop invariant.
-template <int SOLVER, class V, bool DYN>
+// constantValue, a loop invariant.  FIELD (RK4, DYN = false): every layer of
+// the warp is field-only (FieldOnly), with its constants in registers.
+template <int SOLVER, class V, bool DYN, bool FIELD>
 __device__ __forceinline__ void run_lanes(const cmtj_junction_t *__restrict__ junctions, int32_t n_junctions,
                                           const cmtj_layer_t *__restrict__ params, cmtj_layer_t *layers,
                                           const double *__restrict__ tables, const cmtj_sim_params_t &p, int G,
@@ -70,6 +73,8 @@ __device__ __forceinline__ void run_lanes(const cmtj_junction_t *__restrict__ ju
     mag = V::load(layers[off + g.l].mag);
     if (DYN) dyn = dynamic_slots(L);
   }
+  FieldOnly<V> fo;
+  if (FIELD) fo = field_only_load<V>(L, c);
   double *out = have ? log + (size_t)j * p.n_log * p.log_width : nullptr;
   uint32_t row = 0;
 
@@ -77,7 +82,8 @@ __device__ __forceinline__ void run_lanes(const cmtj_junction_t *__restrict__ ju
     if (!__any_sync(kWarpAll, run)) break;
     const double t = (double)i * dt;
     const int first =
-        lane_step<SOLVER, V>(L, c, mag, side, mine && run, g, n, i, t, dt, tables, energies, nullptr, dyn);
+        lane_step<SOLVER, V>(L, c, mag, side, mine && run, g, n, i, t, dt, tables, energies, nullptr, dyn, nullptr,
+                             FIELD ? &fo : nullptr);
     if (first >= 0) {
       if (run) code = CMTJ_STATUS_NAN;
       run = false;
@@ -106,15 +112,22 @@ __global__ void __launch_bounds__(32)
   const int lane = threadIdx.x;
   const int l = (lane % span) / V::kLanes;
   const int j = blockIdx.x * (32 / span) + lane / span;
-  bool varying = false;
+  bool varying = false, general = false;
   if (j < n_junctions) {
     const int n = junctions[j].n_layers;
-    if (l < n && n <= G) varying = dynamic_slots(params[junctions[j].layer_offset + l]) != 0u;
+    if (l < n && n <= G) {
+      const cmtj_layer_t &L = params[junctions[j].layer_offset + l];
+      varying = dynamic_slots(L) != 0u;
+      general = !field_only(L);
+    }
   }
   if (__any_sync(kWarpAll, varying))
-    run_lanes<SOLVER, V, true>(junctions, n_junctions, params, layers, tables, p, G, log, status);
+    run_lanes<SOLVER, V, true, false>(junctions, n_junctions, params, layers, tables, p, G, log, status);
+  else if (SOLVER == CMTJ_RK4 && !__any_sync(kWarpAll, general))
+    run_lanes<SOLVER, V, false, SOLVER == CMTJ_RK4>(junctions, n_junctions, params, layers, tables, p, G, log,
+                                                    status);
   else
-    run_lanes<SOLVER, V, false>(junctions, n_junctions, params, layers, tables, p, G, log, status);
+    run_lanes<SOLVER, V, false, false>(junctions, n_junctions, params, layers, tables, p, G, log, status);
 }
 
 }  // namespace

@@ -84,6 +84,55 @@ def test_fp64_plain_both_layouts_match_reference(gpu_lib, monkeypatch, name, lan
         assert np.max(np.abs(np.asarray(mags[lid]) - gm)) <= TOL_M
 
 
+def _rh_pair():
+    """The R(H) MTJ (field-only layers, constant drivers) and a copy with a
+    time-dependent Oersted driver."""
+    cm = cmtj_gb300
+    a = cases.mtj_rh_point(cm, hx=2e5, total=2e-10)[0]
+    b = cases.mtj_rh_point(cm, hx=2e5, total=2e-10)[0]
+    b.setLayerOerstedFieldDriver("all", cm.AxialDriver(cm.sineDriver(0, 1e3, 3e9, 0), cm.NullDriver(),
+                                                       cm.NullDriver()))
+    return a, b
+
+
+def test_rh_junction_is_field_only():
+    """The lowered R(H) MTJ selects the field-only RK4 variant (every
+    CMTJ_ZERO_* term absent, no STT or SOT, constant drivers); its copy with
+    a sine driver does not."""
+    from cmtj_gb300 import _abi, _lower
+    plan = _lower.plan_run(2e-10, 1e-13, 1e-12)
+    a, b = _rh_pair()
+    low = _lower.lower([a, b], plan, cmtj_gb300.SolverMode.RK4, False)
+    L = low.layers
+    assert np.all(L["zero_terms"] == 15)
+    assert not np.any(L["includeSTT"]) and not np.any(L["includeSOT"])
+    dyn = L["drv"]["update"] != _abi.DRV_CONSTANT
+    assert not dyn[:2].any() and dyn[2:].any()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("lanes", [1, 4])
+def test_field_only_variant_gives_the_general_bits(gpu_lib, monkeypatch, lanes):
+    """Alone, the R(H) MTJ runs the field-only RK4 variant; in one warp with
+    a junction that has a time-dependent driver it runs the general one.
+    Both give the same bits in every log column (with the energy log too)
+    and in the final m."""
+    from cmtj_gb300 import engine
+    _force_lanes(monkeypatch, lanes)
+    plan = engine.plan_run(2e-10, 1e-13, 1e-12)
+    for energies in (False, True):
+        solo, _ = _rh_pair()
+        mixed, other = _rh_pair()
+        engine.run_junctions([solo], plan, cmtj_gb300.SolverMode.RK4, calculate_energies=energies)
+        engine.run_junctions([mixed, other], plan, cmtj_gb300.SolverMode.RK4, calculate_energies=energies)
+        la, lb = solo.getLogArrays(), mixed.getLogArrays()
+        assert set(la) == set(lb)
+        for k in la:
+            assert np.array_equal(la[k], lb[k]), (energies, k)
+        for x, y in zip(solo.layers, mixed.layers):
+            assert (x.mag.x, x.mag.y, x.mag.z) == (y.mag.x, y.mag.y, y.mag.z)
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("solver", ["RK4", "EulerHeun", "Heun"])
 def test_fp64_plain_layouts_give_identical_bits(gpu_lib, monkeypatch, solver):
