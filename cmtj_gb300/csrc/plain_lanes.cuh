@@ -146,7 +146,7 @@ __device__ __forceinline__ int lane_step(const cmtj_layer_t &L, const cmtj_const
       V k = V::zero(), acc = V::zero();
       if (fo) {
         const V hiec = field_only_iec(*fo, below, above);
-#pragma unroll 1
+#pragma unroll
         for (int s = 0; s < 4; ++s) {
           const V mi = s == 0 ? mag : (s == 3 ? mag + k : mag + k * 0.5);
           k = rhs_field_only(*fo, mi, hiec, (s == 3 && energies) ? &side : nullptr) * dt;
