@@ -42,13 +42,20 @@ __device__ __forceinline__ LaneGeo lane_geo(int G) {
 }
 
 // A field-only layer: no dipole, IDMI, second-order anisotropy or
-// biquadratic IEC term (CMTJ_ZERO_*), no STT and no SOT.  With constant
-// drivers, everything rhs() reads for such a layer except m and the
-// neighbours is fixed for the whole run; FieldOnly holds it in registers.
+// biquadratic IEC term (CMTJ_ZERO_*), no STT and no SOT.  rhs() of such a
+// layer reads only m, the neighbours and the slots HEXT, HOE, HDMI, HRES,
+// ANIS, IEC_TOP and IEC_BOTTOM.  With those constant, everything but m and
+// the neighbours is fixed for the whole run, and FieldOnly holds it in
+// registers; the field and anisotropy slots may also be time-dependent
+// (field_only_dyn), the IEC slots may not (the IEC term is formed once per
+// step).
 __device__ __forceinline__ bool field_only(const cmtj_layer_t &L) {
   const uint32_t all = CMTJ_ZERO_DIPOLE | CMTJ_ZERO_IDMI | CMTJ_ZERO_K2 | CMTJ_ZERO_J2;
   return (L.zero_terms & all) == all && !L.includeSTT && !L.includeSOT;
 }
+// The driver slots whose dynamic_slots() bit keeps a field-only layer off
+// the field-only loop.
+constexpr uint32_t kFieldOnlyFixedSlots = (1u << CMTJ_SLOT_IEC_TOP) | (1u << CMTJ_SLOT_IEC_BOTTOM);
 
 template <class V>
 struct FieldOnly {
@@ -95,21 +102,29 @@ __device__ __forceinline__ V field_only_iec(const FieldOnly<V> &f, const V &bott
 // rhs() (calculateHeff + solveLLG, junction.hpp:580-815) of a field-only
 // layer: the same operations in the same order, with the terms rhs()
 // leaves out for such a layer absent and the constant ones preloaded.
-template <class V>
-__device__ __forceinline__ V rhs_field_only(const FieldOnly<V> &f, const V &m, const V &Hiec,
+// DYN: the field and anisotropy slots are read through slot_at() at the
+// stage time (dyn: dynamic_slots(L)), as rhs() reads them.
+template <class V, bool DYN>
+__device__ __forceinline__ V rhs_field_only(const FieldOnly<V> &f, const cmtj_layer_t &L, double time,
+                                            const DriverCtx &dc, uint32_t dyn, const V &m, const V &Hiec,
                                             typename NoDeduce<SideT<V>>::type *side) {
+  const V Hext = DYN ? V::axial(L, CMTJ_SLOT_HEXT, time, dc, dyn) : f.Hext;
+  const V Hoe = DYN ? V::axial(L, CMTJ_SLOT_HOE, time, dc, dyn) : f.Hoe;
+  const V Hdmi = DYN ? V::axial(L, CMTJ_SLOT_HDMI, time, dc, dyn) : f.Hdmi;
+  const V Hres = DYN ? V::axial(L, CMTJ_SLOT_HRES, time, dc, dyn) : f.Hres;
+  const double K = DYN ? slot_at(L, CMTJ_SLOT_ANIS, time, dc, dyn) : f.K;
   const V Hdemag = tensor_mul(m, f.demag, f.ms_mu0);
-  const V Hanis = f.anis * ((2 * f.K) * dot(f.anis, m) / f.Ms);
-  V H = f.Hext + Hanis;
+  const V Hanis = f.anis * ((2 * K) * dot(f.anis, m) / f.Ms);
+  V H = Hext + Hanis;
   H = H + Hiec;
-  H = H + f.Hoe + f.Hdmi - Hdemag;
-  H = H + f.Hres;
+  H = H + Hoe + Hdmi - Hdemag;
+  H = H + Hres;
   if (side) {
-    side->K = f.K;
+    side->K = K;
     side->K2 = 0.0;
     side->Jb = f.Jb;
     side->Jt = f.Jt;
-    side->Hext = f.Hext;
+    side->Hext = Hext;
     side->Hiec = Hiec;
     side->Hanis = Hanis;
     side->Hdemag = Hdemag;
@@ -124,10 +139,11 @@ __device__ __forceinline__ V rhs_field_only(const FieldOnly<V> &f, const V &m, c
 // core/junction.hpp:1668-1815) for the lane's layer of a junction whose
 // n layers step (1 under runSingleLayerSolver).  cur overrides the current
 // driver (stacks), hres the reserved interaction field (groups).  fo: RK4
-// only, the layer is field-only with constant drivers (FieldOnly).
+// only, the layer is field-only (FieldOnly), with constant drivers or, under
+// FDYN, time-dependent field and anisotropy drivers.
 // Returns the first layer whose m became NaN (RK4: the layers above it
 // keep their start-of-step m, as when rk4_step throws), or -1.
-template <int SOLVER, class V>
+template <int SOLVER, class V, bool FDYN = false>
 __device__ __forceinline__ int lane_step(const cmtj_layer_t &L, const cmtj_constants_t &c, V &mag,
                                          SideT<V> &side, bool step, const LaneGeo &g, int n, uint32_t i, double t,
                                          double dt, const double *tables, bool energies,
@@ -148,8 +164,10 @@ __device__ __forceinline__ int lane_step(const cmtj_layer_t &L, const cmtj_const
         const V hiec = field_only_iec(*fo, below, above);
 #pragma unroll
         for (int s = 0; s < 4; ++s) {
+          const double ts = s == 0 ? t : (s == 3 ? t + dt : t + 0.5 * dt);
           const V mi = s == 0 ? mag : (s == 3 ? mag + k : mag + k * 0.5);
-          k = rhs_field_only(*fo, mi, hiec, (s == 3 && energies) ? &side : nullptr) * dt;
+          const DriverCtx dc = {tables, i, s == 0 ? 0 : (s == 3 ? 2 : 1)};
+          k = rhs_field_only<V, FDYN>(*fo, L, ts, dc, dyn, mi, hiec, (s == 3 && energies) ? &side : nullptr) * dt;
           acc = s == 0 ? k : acc + (s == 3 ? k : k * 2.0);
         }
       } else {

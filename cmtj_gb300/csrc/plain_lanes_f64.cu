@@ -21,9 +21,10 @@
 // A block is one warp; blocks spread over the SMs.  Driver slots whose
 // driver is constant are read directly (slot mask per lane), and the four
 // RK4 stages run as a rolled loop so the field code is compiled once per
-// kernel.  A warp whose layers are all field-only with constant drivers
-// (RK4) runs a variant without the per-term branches, with the layer
-// constants in registers and the IEC term formed once per step.
+// kernel.  A warp whose layers are all field-only (RK4) runs a variant
+// without the per-term branches, with the layer constants in registers and
+// the IEC term formed once per step; its field and anisotropy drivers may
+// be time-dependent.
 //
 // This unit is compiled with --fmad=false like plain_f64.cu.
 #include "plain_lanes.cuh"
@@ -35,8 +36,9 @@ namespace {
 
 // The whole run of the warp's junctions.  DYN = false when no layer of the
 // warp has a time-dependent driver slot: every slot then reads its
-// constantValue, a loop invariant.  FIELD (RK4, DYN = false): every layer of
-// the warp is field-only (FieldOnly), with its constants in registers.
+// constantValue, a loop invariant.  FIELD (RK4): every layer of the warp is
+// field-only (FieldOnly), with its constants in registers; with DYN, its
+// field and anisotropy drivers may be time-dependent.
 template <int SOLVER, class V, bool DYN, bool FIELD>
 __device__ __forceinline__ void run_lanes(const cmtj_junction_t *__restrict__ junctions, int32_t n_junctions,
                                           const cmtj_layer_t *__restrict__ params, cmtj_layer_t *layers,
@@ -82,8 +84,8 @@ __device__ __forceinline__ void run_lanes(const cmtj_junction_t *__restrict__ ju
     if (!__any_sync(kWarpAll, run)) break;
     const double t = (double)i * dt;
     const int first =
-        lane_step<SOLVER, V>(L, c, mag, side, mine && run, g, n, i, t, dt, tables, energies, nullptr, dyn, nullptr,
-                             FIELD ? &fo : nullptr);
+        lane_step<SOLVER, V, DYN && FIELD>(L, c, mag, side, mine && run, g, n, i, t, dt, tables, energies, nullptr,
+                                           dyn, nullptr, FIELD ? &fo : nullptr);
     if (first >= 0) {
       if (run) code = CMTJ_STATUS_NAN;
       run = false;
@@ -117,15 +119,23 @@ __global__ void __launch_bounds__(32)
     const int n = junctions[j].n_layers;
     if (l < n && n <= G) {
       const cmtj_layer_t &L = params[junctions[j].layer_offset + l];
-      varying = dynamic_slots(L) != 0u;
-      general = !field_only(L);
+      const uint32_t dyn = dynamic_slots(L);
+      varying = dyn != 0u;
+      general = !field_only(L) || (dyn & kFieldOnlyFixedSlots) != 0u;
     }
   }
-  if (__any_sync(kWarpAll, varying))
+  const bool dyn = __any_sync(kWarpAll, varying);
+  if constexpr (SOLVER == CMTJ_RK4) {
+    if (!__any_sync(kWarpAll, general)) {
+      if (dyn)
+        run_lanes<SOLVER, V, true, true>(junctions, n_junctions, params, layers, tables, p, G, log, status);
+      else
+        run_lanes<SOLVER, V, false, true>(junctions, n_junctions, params, layers, tables, p, G, log, status);
+      return;
+    }
+  }
+  if (dyn)
     run_lanes<SOLVER, V, true, false>(junctions, n_junctions, params, layers, tables, p, G, log, status);
-  else if (SOLVER == CMTJ_RK4 && !__any_sync(kWarpAll, general))
-    run_lanes<SOLVER, V, false, SOLVER == CMTJ_RK4>(junctions, n_junctions, params, layers, tables, p, G, log,
-                                                    status);
   else
     run_lanes<SOLVER, V, false, false>(junctions, n_junctions, params, layers, tables, p, G, log, status);
 }

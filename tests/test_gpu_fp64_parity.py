@@ -84,45 +84,54 @@ def test_fp64_plain_both_layouts_match_reference(gpu_lib, monkeypatch, name, lan
         assert np.max(np.abs(np.asarray(mags[lid]) - gm)) <= TOL_M
 
 
-def _rh_pair():
-    """The R(H) MTJ (field-only layers, constant drivers) and a copy with a
-    time-dependent Oersted driver."""
+def _sine(cm, amplitude):
+    return cm.sineDriver(0, amplitude, 3e9, 0)
+
+
+def _rh_junction(oersted=False, iec_sine=False):
+    """The R(H) MTJ (field-only layers, constant drivers); oersted adds a
+    time-dependent Oersted field (still field-only), iec_sine a
+    time-dependent IEC coupling (which sends its warp down the general
+    loop)."""
     cm = cmtj_gb300
-    a = cases.mtj_rh_point(cm, hx=2e5, total=2e-10)[0]
-    b = cases.mtj_rh_point(cm, hx=2e5, total=2e-10)[0]
-    b.setLayerOerstedFieldDriver("all", cm.AxialDriver(cm.sineDriver(0, 1e3, 3e9, 0), cm.NullDriver(),
-                                                       cm.NullDriver()))
-    return a, b
+    j = cases.mtj_rh_point(cm, hx=2e5, total=2e-10)[0]
+    if oersted:
+        j.setLayerOerstedFieldDriver("all", cm.AxialDriver(_sine(cm, 1e3), cm.NullDriver(), cm.NullDriver()))
+    if iec_sine:
+        j.setIECDriver("free", "ref", cm.ScalarDriver.getSineDriver(-5e-5, 1e-5, 3e9, 0))
+    return j
 
 
-def test_rh_junction_is_field_only():
-    """The lowered R(H) MTJ selects the field-only RK4 variant (every
-    CMTJ_ZERO_* term absent, no STT or SOT, constant drivers); its copy with
-    a sine driver does not."""
+def test_field_only_selection():
+    """The lowered R(H) MTJ is field-only (every CMTJ_ZERO_* term absent, no
+    STT or SOT); a time-dependent Oersted driver keeps it so, a
+    time-dependent IEC driver does not (its IEC slots are dynamic)."""
     from cmtj_gb300 import _abi, _lower
     plan = _lower.plan_run(2e-10, 1e-13, 1e-12)
-    a, b = _rh_pair()
-    low = _lower.lower([a, b], plan, cmtj_gb300.SolverMode.RK4, False)
-    L = low.layers
+    js = [_rh_junction(), _rh_junction(oersted=True), _rh_junction(iec_sine=True)]
+    L = _lower.lower(js, plan, cmtj_gb300.SolverMode.RK4, False).layers
     assert np.all(L["zero_terms"] == 15)
     assert not np.any(L["includeSTT"]) and not np.any(L["includeSOT"])
     dyn = L["drv"]["update"] != _abi.DRV_CONSTANT
-    assert not dyn[:2].any() and dyn[2:].any()
+    assert not dyn[:2].any()
+    assert dyn[2:4, _abi.SLOT_HOE].all() and not dyn[2:4, _abi.SLOT_IEC_TOP].any()
+    assert dyn[4:6, _abi.SLOT_IEC_TOP].any() or dyn[4:6, _abi.SLOT_IEC_BOTTOM].any()
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("oersted", [False, True], ids=["constant", "oersted_sine"])
 @pytest.mark.parametrize("lanes", [1, 4])
-def test_field_only_variant_gives_the_general_bits(gpu_lib, monkeypatch, lanes):
-    """Alone, the R(H) MTJ runs the field-only RK4 variant; in one warp with
-    a junction that has a time-dependent driver it runs the general one.
-    Both give the same bits in every log column (with the energy log too)
-    and in the final m."""
+def test_field_only_variant_gives_the_general_bits(gpu_lib, monkeypatch, lanes, oersted):
+    """Alone, the R(H) MTJ runs the field-only RK4 loop (constant drivers, or
+    a time-dependent Oersted field); in one warp with a junction whose IEC
+    driver is time-dependent it runs the general loop.  Both give the same
+    bits in every log column (with the energy log too) and in the final m."""
     from cmtj_gb300 import engine
     _force_lanes(monkeypatch, lanes)
     plan = engine.plan_run(2e-10, 1e-13, 1e-12)
     for energies in (False, True):
-        solo, _ = _rh_pair()
-        mixed, other = _rh_pair()
+        solo = _rh_junction(oersted)
+        mixed, other = _rh_junction(oersted), _rh_junction(iec_sine=True)
         engine.run_junctions([solo], plan, cmtj_gb300.SolverMode.RK4, calculate_energies=energies)
         engine.run_junctions([mixed, other], plan, cmtj_gb300.SolverMode.RK4, calculate_energies=energies)
         la, lb = solo.getLogArrays(), mixed.getLogArrays()
