@@ -46,9 +46,9 @@ __device__ __forceinline__ LaneGeo lane_geo(int G) {
 // layer reads only m, the neighbours and the slots HEXT, HOE, HDMI, HRES,
 // ANIS, IEC_TOP and IEC_BOTTOM.  With those constant, everything but m and
 // the neighbours is fixed for the whole run, and FieldOnly holds it in
-// registers; the field and anisotropy slots may also be time-dependent
-// (field_only_dyn), the IEC slots may not (the IEC term is formed once per
-// step).
+// registers.  The field and anisotropy slots may also be time-dependent
+// (rhs_field_only with DYN reads them at each stage time); the IEC slots
+// may not, because the IEC term is formed once per step.
 __device__ __forceinline__ bool field_only(const cmtj_layer_t &L) {
   const uint32_t all = CMTJ_ZERO_DIPOLE | CMTJ_ZERO_IDMI | CMTJ_ZERO_K2 | CMTJ_ZERO_J2;
   return (L.zero_terms & all) == all && !L.includeSTT && !L.includeSOT;
