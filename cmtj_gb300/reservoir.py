@@ -137,20 +137,26 @@ class GroupInteraction:
         mu0 = _mu0()
         tops = [j.getLayer(self.topId) for j in self.junctionList]
         pos = [_v(c) for c in self.coordinateMatrix]
+        # the scale depends only on the source junction k
+        if kind == INTERACTION_DIPOLE:
+            scale = [(L2.Ms / mu0) * (L2.thickness * L2.cellSurface) for L2 in tops]
+        else:
+            scale = [(L2.Ms * (L2.thickness * L2.cellSurface)) / mu0 for L2 in tops]
+        idx, rows = [], []
         for i in range(n):
             for k in range(n):
                 if i == k:
                     continue
-                rec = pairs[i * n + k]
-                L2 = tops[k]
-                V = L2.thickness * L2.cellSurface
+                idx.append(i * n + k)
                 if kind == INTERACTION_DIPOLE:
                     rij, r3, r5 = _dipole_geometry(pos[i], pos[k])
-                    rec["g"][:5] = (rij[0], rij[1], rij[2], r3, r5)
-                    rec["scale"] = (L2.Ms / mu0) * V
+                    rows.append((rij[0], rij[1], rij[2], r3, r5))
                 else:
-                    rec["g"] = _dipole_tensor(pos[i], pos[k])
-                    rec["scale"] = (L2.Ms * V) / mu0
+                    rows.append(_dipole_tensor(pos[i], pos[k]))
+        if idx:
+            width = 5 if kind == INTERACTION_DIPOLE else 9
+            pairs["g"][idx, :width] = np.array(rows, dtype=np.float64)
+            pairs["scale"][idx] = np.array(scale, dtype=np.float64)[np.array(idx) % n]
         return pairs
 
     def runSimulation(self, totalTime, timeStep=1e-13, writeFrequency=1e-11):
