@@ -65,6 +65,44 @@ def test_group_api_checks():
         cm.reservoir.computeDipoleInteraction(p1, cm.CVector(1e-12, 0, 0), j1.getLayer("free"), j2.getLayer("free"))
 
 
+def test_group_pair_table():
+    """The device pair table of a group: for every ordered pair (i, k != i)
+    the fixed geometry of reservoir.hpp:82-90 (dipole) or the tensor of
+    37-57 (Nomura) and the source junction's Ms V / mu0 factor; zero rows on
+    the diagonal; too-close points raise when the table is formed."""
+    from cmtj_gb300 import reservoir
+    z = cm.CVector(0, 0, 0)
+
+    def junction(ms, t):
+        l = cm.Layer("free", mag=cm.CVector(0, 0, 1), anis=cm.CVector(0, 0, 1), Ms=ms, thickness=t,
+                     cellSurface=1e-16, demagTensor=[z, z, z])
+        return cm.Junction([l])
+
+    pos = [cm.CVector(0, 0, 0), cm.CVector(60e-9, 0, 0), cm.CVector(0, 45e-9, 5e-9)]
+    js = [junction(1.0 + 0.1 * k, (1 + k) * 1e-9) for k in range(3)]
+    g = reservoir.GroupInteraction(pos, js)
+    mu0 = reservoir._mu0()
+    P = [reservoir._v(p) for p in pos]
+    dip = g._pairs(reservoir.INTERACTION_DIPOLE)
+    nom = g._pairs(reservoir.INTERACTION_NOUMRA)
+    for i in range(3):
+        for k in range(3):
+            a, b = dip[3 * i + k], nom[3 * i + k]
+            if i == k:
+                assert not a["g"].any() and a["scale"] == 0 and not b["g"].any() and b["scale"] == 0
+                continue
+            ms, t = 1.0 + 0.1 * k, (1 + k) * 1e-9
+            rij, r3, r5 = reservoir._dipole_geometry(P[i], P[k])
+            assert list(a["g"][:5]) == [rij[0], rij[1], rij[2], r3, r5] and not a["g"][5:].any()
+            assert a["scale"] == (ms / mu0) * (t * 1e-16)
+            assert list(b["g"]) == reservoir._dipole_tensor(P[i], P[k])
+            assert b["scale"] == (ms * (t * 1e-16)) / mu0
+    close = reservoir.GroupInteraction([cm.CVector(0, 0, 0), cm.CVector(1e-12, 0, 0)],
+                                       [junction(1.0, 1e-9), junction(1.0, 1e-9)])
+    with pytest.raises(RuntimeError, match="too close"):
+        close._pairs(reservoir.INTERACTION_DIPOLE)
+
+
 def test_group_interaction_functions_match_reference_formula():
     """The host forms of the two dipole fields against their formulas
     written with numpy (reservoir.hpp:77-97 and 37-57, 99-122)."""
