@@ -312,19 +312,26 @@ def decode_log(junction, rows, calculate_energies):
 def apply_results(junctions, lowered, log, status, plan):
     """Write final magnetisations back, append logs, raise on NaN."""
     nan = False
+    # whole columns as Python lists: one conversion instead of a record
+    # lookup per layer (the values are the same doubles)
+    offsets = lowered.junctions["layer_offset"].tolist()
+    codes = np.asarray(status).tolist()
+    mags = lowered.layers["mag"].tolist()
+    if plan.adaptive:
+        prev_ratio = lowered.layers["adaptive"]["prev_error_ratio"].tolist()
+        integral = lowered.layers["adaptive"]["integral_error"].tolist()
+    energies = bool(lowered.params["calculate_energies"][0])
     for k, j in enumerate(junctions):
-        off = int(lowered.junctions[k]["layer_offset"])
-        code, rows = int(status[2 * k]), int(status[2 * k + 1])
+        off = offsets[k]
+        code, rows = codes[2 * k], codes[2 * k + 1]
         for i, l in enumerate(j.layers):
-            rec = lowered.layers[off + i]
-            m = rec["mag"]
-            l.mag.x, l.mag.y, l.mag.z = float(m[0]), float(m[1]), float(m[2])
+            l.mag.x, l.mag.y, l.mag.z = mags[off + i]
             l.noise_step += plan.total_iterations
             if plan.adaptive:
-                l.adaptiveParams.prev_error_ratio = float(rec["adaptive"]["prev_error_ratio"])
-                l.adaptiveParams.integral_error = float(rec["adaptive"]["integral_error"])
+                l.adaptiveParams.prev_error_ratio = prev_ratio[off + i]
+                l.adaptiveParams.integral_error = integral[off + i]
         if rows:
-            j._append_log(decode_log(j, log[k, :rows], bool(lowered.params["calculate_energies"][0])), rows)
+            j._append_log(decode_log(j, log[k, :rows], energies), rows)
         if code == _abi.STATUS_NAN:
             nan = True
         elif code == _abi.STATUS_DP_STALL:
