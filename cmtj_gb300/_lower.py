@@ -9,7 +9,11 @@ from . import _abi
 from . import constants as _constants
 from .core import MR_CLASSIC, MR_NONE, MR_STRIP, SolverMode, UpdateType, _AXIAL_SLOTS, _SCALAR_SLOTS
 
-_SCALAR_INDEX = {name: i for i, name in enumerate(_SCALAR_SLOTS)}
+# driver slot order of cmtj_layer_t.drv: the scalar slots in _SCALAR_SLOTS
+# order, then three per axial slot in _AXIAL_SLOTS order
+if [i for i, _ in enumerate(_SCALAR_SLOTS)] + [b + k for b in _AXIAL_SLOTS.values() for k in range(3)] != \
+        list(range(_abi.NUM_SLOTS)):
+    raise ImportError("driver slot tables do not match cmtj_layer_t.drv")
 
 # stages each solver evaluates drivers at: 0 -> t, 1 -> t + dt/2, 2 -> t + dt
 _SOLVER_STAGES = {
@@ -107,12 +111,16 @@ class TableBuilder:
 
 def _driver_record(d, tables):
     """One cmtj_driver_t as a tuple in DRIVER_DTYPE field order."""
-    if d.update == UpdateType.custom:
+    u = d.update
+    if u is _CUSTOM:
         if tables is None:
             raise RuntimeError("custom drivers need a run plan")
         return (_abi.DRV_TABLE, 0, tables.add(d), 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0)
-    return (int(d.update), 0, 0, d.constantValue, d.amplitude, d.frequency, d.phase, d.period, d.cycle,
+    return (int(u), 0, 0, d.constantValue, d.amplitude, d.frequency, d.phase, d.period, d.cycle,
             d.timeStart, d.timeStop, d.edgeTime, d.steadyTime)
+
+
+_CUSTOM = UpdateType.custom
 
 
 def _tensor9(rows):
@@ -151,15 +159,19 @@ def lower_layers(layers, larr, tables=None):
     for field in _ADAPTIVE_FIELDS:
         ap[field] = [getattr(l.adaptiveParams, field) for l in layers]
     ap["use_pid_control"] = [int(bool(l.adaptiveParams.use_pid_control)) for l in layers]
+    # slot order: the scalar slots in _SCALAR_SLOTS order, then three per
+    # axial slot in _AXIAL_SLOTS order (checked at import)
     slots = []
+    add = slots.append
+    rec = _driver_record
+    axial_names = tuple(_AXIAL_SLOTS)
     for l in layers:
-        row = [None] * _abi.NUM_SLOTS
-        for name, idx in _SCALAR_INDEX.items():
-            row[idx] = _driver_record(l.scalar[name], tables)
-        for name, base in _AXIAL_SLOTS.items():
-            for k in range(3):
-                row[base + k] = _driver_record(l.axial[name].drivers[k], tables)
-        slots.extend(row)
+        sc, ax = l.scalar, l.axial
+        for name in _SCALAR_SLOTS:
+            add(rec(sc[name], tables))
+        for name in axial_names:
+            for d in ax[name].drivers:
+                add(rec(d, tables))
     if layers:
         larr["drv"] = np.array(slots, dtype=_abi.DRIVER_DTYPE).reshape(len(layers), _abi.NUM_SLOTS)
     derive_layers(larr)
