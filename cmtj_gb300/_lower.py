@@ -7,7 +7,8 @@ import numpy as np
 
 from . import _abi
 from . import constants as _constants
-from .core import MR_CLASSIC, MR_NONE, MR_STRIP, SolverMode, UpdateType, _AXIAL_SLOTS, _SCALAR_SLOTS
+from .core import (MR_CLASSIC, MR_NONE, MR_STRIP, SolverMode, UpdateType, _AXIAL_SLOTS, _SCALAR_SLOTS,
+                   _UNSET_DRIVER)
 
 # driver slot order of cmtj_layer_t.drv: the scalar slots in _SCALAR_SLOTS
 # order, then three per axial slot in _AXIAL_SLOTS order
@@ -121,6 +122,7 @@ def _driver_record(d, tables):
 
 
 _CUSTOM = UpdateType.custom
+_UNSET_RECORD = np.array(_driver_record(_UNSET_DRIVER, None), dtype=_abi.DRIVER_DTYPE)
 
 
 def _tensor9(rows):
@@ -159,22 +161,41 @@ def lower_layers(layers, larr, tables=None):
     for field in _ADAPTIVE_FIELDS:
         ap[field] = [getattr(l.adaptiveParams, field) for l in layers]
     ap["use_pid_control"] = [int(bool(l.adaptiveParams.use_pid_control)) for l in layers]
-    # slot order: the scalar slots in _SCALAR_SLOTS order, then three per
-    # axial slot in _AXIAL_SLOTS order (checked at import)
-    slots = []
-    add = slots.append
-    rec = _driver_record
+    if layers:
+        larr["drv"] = _driver_slots(layers, tables)
+    derive_layers(larr)
+
+
+def _driver_slots(layers, tables):
+    """The [layer][slot] cmtj_driver_t records.  Slot order: the scalar
+    slots in _SCALAR_SLOTS order, then three per axial slot in _AXIAL_SLOTS
+    order (checked at import).  Slots a layer was never given a driver for
+    hold the shared unset driver and start as its record; only the others
+    are converted, in layer and slot order (the order custom drivers are
+    tabulated in)."""
+    drv = np.empty(len(layers) * _abi.NUM_SLOTS, dtype=_abi.DRIVER_DTYPE)
+    drv[:] = _UNSET_RECORD
+    idx, recs = [], []
+    unset, rec = _UNSET_DRIVER, _driver_record
     axial_names = tuple(_AXIAL_SLOTS)
+    s = 0
     for l in layers:
         sc, ax = l.scalar, l.axial
         for name in _SCALAR_SLOTS:
-            add(rec(sc[name], tables))
+            d = sc[name]
+            if d is not unset:
+                idx.append(s)
+                recs.append(rec(d, tables))
+            s += 1
         for name in axial_names:
             for d in ax[name].drivers:
-                add(rec(d, tables))
-    if layers:
-        larr["drv"] = np.array(slots, dtype=_abi.DRIVER_DTYPE).reshape(len(layers), _abi.NUM_SLOTS)
-    derive_layers(larr)
+                if d is not unset:
+                    idx.append(s)
+                    recs.append(rec(d, tables))
+                s += 1
+    if idx:
+        drv[idx] = np.array(recs, dtype=_abi.DRIVER_DTYPE)
+    return drv.reshape(len(layers), _abi.NUM_SLOTS)
 
 
 def _const_zero(drv, slot):

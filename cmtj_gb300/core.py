@@ -254,6 +254,8 @@ class ScalarDriver:
         return ScalarDriver(UpdateType.custom, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, callback)
 
     def copy(self):
+        if self is _UNSET_DRIVER:
+            return self
         d = ScalarDriver.__new__(ScalarDriver)
         for k in ScalarDriver.__slots__:
             setattr(d, k, getattr(self, k))
@@ -348,6 +350,13 @@ def _call_custom(callback, t):
         raise RuntimeError("Error in Python callback") from e
 
 
+# The driver of every Layer slot that has not been given one.  One shared
+# object: a Layer replaces a slot's driver with a copy of the one it is
+# given and never changes a driver in place, so this one stays the default
+# ScalarDriver() and lowering recognises it by identity.
+_UNSET_DRIVER = ScalarDriver()
+
+
 class NullDriver(ScalarDriver):
     """drivers.hpp:356-360: always zero."""
 
@@ -413,6 +422,13 @@ class AxialDriver:
     def copy(self):
         a = AxialDriver.__new__(AxialDriver)
         a.drivers = [d.copy() for d in self.drivers]
+        return a
+
+    @staticmethod
+    def _unset():
+        """The axial driver of a Layer slot that has not been given one."""
+        a = AxialDriver.__new__(AxialDriver)
+        a.drivers = [_UNSET_DRIVER, _UNSET_DRIVER, _UNSET_DRIVER]
         return a
 
 
@@ -527,8 +543,8 @@ class Layer:
         self.secondaryReferenceLayer = CVector()
         self.dipoleTop = [CVector(), CVector(), CVector()]
         self.dipoleBottom = [CVector(), CVector(), CVector()]
-        self.scalar = {k: ScalarDriver() for k in _SCALAR_SLOTS}
-        self.axial = {k: AxialDriver() for k in _AXIAL_SLOTS}
+        self.scalar = {k: _UNSET_DRIVER for k in _SCALAR_SLOTS}
+        self.axial = {k: AxialDriver._unset() for k in _AXIAL_SLOTS}
         self.alphaNoiseScale = 0.0
         self.adaptiveParams = AdaptiveIntegrationParams()
         # Thermal noise stream: copies of a Layer share it, like the

@@ -271,3 +271,39 @@ def test_layer_records_mark_identically_zero_terms():
         assert r["conv_term"] == 1 / (1 + d * d)
         assert r["stoch_conv"] == -c["gyro"] / (1. + d * d)
         assert r["ms_over_mu0"] == float(r["Ms"]) / c["mu0"]
+
+
+def test_unset_driver_slots_lower_like_default_drivers():
+    """Slots a layer was never given a driver for lower to the record of a
+    default ScalarDriver(), the same as slots given one explicitly; giving
+    one layer a driver, or changing the given driver in place afterwards,
+    leaves every other slot and layer as it was."""
+    from cmtj_gb300 import _abi, _lower
+    z = cmtj.CVector(0, 0, 0)
+
+    def layer(i):
+        return cmtj.Layer("L%d" % i, mag=cmtj.CVector(0, 0, 1), anis=cmtj.CVector(0, 0, 1), Ms=1.0, thickness=1e-9,
+                        cellSurface=1e-16, demagTensor=[z, z, z])
+
+    plan = _lower.plan_run(1e-12, 1e-13, 1e-13)
+    unset, given = layer(0), layer(1)
+    for name in ("anis", "current", "temperature", "iec_top", "fl"):
+        given.scalar[name] = cmtj.ScalarDriver().copy()
+    for name in ("hext", "hoe", "idmi_top"):
+        given.axial[name] = cmtj.AxialDriver(cmtj.ScalarDriver(), cmtj.ScalarDriver(), cmtj.ScalarDriver())
+    a = _lower.lower([cmtj.Junction([unset])], plan, cmtj.SolverMode.RK4, False).layers["drv"]
+    b = _lower.lower([cmtj.Junction([given])], plan, cmtj.SolverMode.RK4, False).layers["drv"]
+    assert a.tobytes() == b.tobytes()
+    # a driver given to one layer is a copy: changing it later changes nothing
+    d = cmtj.ScalarDriver.getSineDriver(1.0, 2.0, 3e9, 0.0)
+    l2, l3 = layer(2), layer(3)
+    l2.setAnisotropyDriver(d)
+    d *= 5
+    d.phaseShift(1.0)
+    low = _lower.lower([cmtj.Junction([l2]), cmtj.Junction([l3])], plan, cmtj.SolverMode.RK4, False).layers["drv"]
+    anis = low[0, _abi.SLOT_ANIS]
+    assert (int(anis["update"]), float(anis["constantValue"]), float(anis["amplitude"]), float(anis["phase"])) == \
+        (int(cmtj.UpdateType.sine), 1.0, 2.0, 0.0)
+    assert low[1].tobytes() == a[0].tobytes()
+    ref = cmtj.ScalarDriver()
+    assert (ref.constantValue, ref.amplitude, ref.frequency) == (0.0, 0.0, -1.0)
