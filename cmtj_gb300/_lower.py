@@ -1,6 +1,7 @@
 """Lowering of host-side Junction descriptions into the packed structs of
 include/cmtj_gpu.h, and decoding of the solver's log rows back into the
 reference's log dictionary (junction.hpp:1580-1636)."""
+import operator
 from dataclasses import dataclass
 
 import numpy as np
@@ -134,9 +135,12 @@ _LAYER_SCALARS = (("Ms", "Ms"), ("thickness", "thickness"), ("cellSurface", "cel
                   ("dampingLikeTorque", "dampingLikeTorque"), ("slonczewski", "SlonczewskiSpacerLayerParameter"),
                   ("beta", "beta"), ("kappa", "kappa"), ("spinPolarisation", "spinPolarisation"),
                   ("noise_step", "noise_step"))
+_LAYER_FLOATS = tuple(fa for fa in _LAYER_SCALARS if fa[0] != "noise_step")
+_LAYER_FLOAT_VALUES = operator.attrgetter(*(attr for _, attr in _LAYER_FLOATS))
 _LAYER_FLAGS = ("includeSTT", "includeSOT", "dynamicSOT", "alternativeSTT", "temperatureSet")
 _ADAPTIVE_FIELDS = ("abs_tol", "rel_tol", "max_factor", "min_factor", "safety_factor", "ki", "kp", "kd",
                     "prev_error_ratio", "integral_error")
+_ADAPTIVE_VALUES = operator.attrgetter(*_ADAPTIVE_FIELDS)
 
 
 def lower_layers(layers, larr, tables=None):
@@ -150,17 +154,23 @@ def lower_layers(layers, larr, tables=None):
     larr["demag"] = [_tensor9(l.demagTensor) for l in layers]
     larr["dipole_top"] = [_tensor9(l.dipoleTop) for l in layers]
     larr["dipole_bottom"] = [_tensor9(l.dipoleBottom) for l in layers]
-    for field, attr in _LAYER_SCALARS:
-        larr[field] = [getattr(l, attr) for l in layers]
+    n = len(layers)
+    # the FP64 scalars of all layers as one [n][k] array, then column by column
+    vals = np.array([_LAYER_FLOAT_VALUES(l) for l in layers], dtype=np.float64).reshape(n, len(_LAYER_FLOATS))
+    for c, (field, _) in enumerate(_LAYER_FLOATS):
+        larr[field] = vals[:, c]
+    larr["noise_step"] = [l.noise_step for l in layers]
     larr["referenceType"] = [int(l.referenceType) for l in layers]
     for field in _LAYER_FLAGS:
         larr[field] = [int(getattr(l, field)) for l in layers]
     larr["seed_lo"] = [l.noise_seed & 0xFFFFFFFF for l in layers]
     larr["seed_hi"] = [(l.noise_seed >> 32) & 0xFFFFFFFF for l in layers]
     ap = larr["adaptive"]
-    for field in _ADAPTIVE_FIELDS:
-        ap[field] = [getattr(l.adaptiveParams, field) for l in layers]
-    ap["use_pid_control"] = [int(bool(l.adaptiveParams.use_pid_control)) for l in layers]
+    aps = [l.adaptiveParams for l in layers]
+    vals = np.array([_ADAPTIVE_VALUES(a) for a in aps], dtype=np.float64).reshape(n, len(_ADAPTIVE_FIELDS))
+    for c, field in enumerate(_ADAPTIVE_FIELDS):
+        ap[field] = vals[:, c]
+    ap["use_pid_control"] = [int(bool(a.use_pid_control)) for a in aps]
     if layers:
         larr["drv"] = _driver_slots(layers, tables)
     derive_layers(larr)
