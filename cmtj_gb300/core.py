@@ -254,8 +254,6 @@ class ScalarDriver:
         return ScalarDriver(UpdateType.custom, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, callback)
 
     def copy(self):
-        if self is _UNSET_DRIVER:
-            return self
         d = ScalarDriver.__new__(ScalarDriver)
         for k in ScalarDriver.__slots__:
             setattr(d, k, getattr(self, k))
@@ -351,10 +349,16 @@ def _call_custom(callback, t):
 
 
 # The driver of every Layer slot that has not been given one.  One shared
-# object: a Layer replaces a slot's driver with a copy of the one it is
-# given and never changes a driver in place, so this one stays the default
-# ScalarDriver() and lowering recognises it by identity.
+# object, never handed out: a Layer replaces a slot's driver with a copy of
+# the one it is given and never changes a driver in place, and a Layer copy
+# keeps this object in its unset slots (_keep_unset), so it stays the
+# default ScalarDriver() and lowering recognises it by identity.
 _UNSET_DRIVER = ScalarDriver()
+
+
+def _keep_unset(d):
+    """A layer copy's driver for a slot holding d."""
+    return d if d is _UNSET_DRIVER else d.copy()
 
 
 class NullDriver(ScalarDriver):
@@ -422,6 +426,12 @@ class AxialDriver:
     def copy(self):
         a = AxialDriver.__new__(AxialDriver)
         a.drivers = [d.copy() for d in self.drivers]
+        return a
+
+    def _layer_copy(self):
+        """copy() for a Layer copy: unset slots keep the shared unset driver."""
+        a = AxialDriver.__new__(AxialDriver)
+        a.drivers = [_keep_unset(d) for d in self.drivers]
         return a
 
     @staticmethod
@@ -580,9 +590,9 @@ class Layer:
         l = Layer.__new__(Layer)
         for k, v in self.__dict__.items():
             if k in ("scalar",):
-                l.scalar = {s: d.copy() for s, d in v.items()}
+                l.scalar = {s: _keep_unset(d) for s, d in v.items()}
             elif k in ("axial",):
-                l.axial = {s: d.copy() for s, d in v.items()}
+                l.axial = {s: d._layer_copy() for s, d in v.items()}
             else:
                 setattr(l, k, copy.deepcopy(v, memo))
         return l

@@ -307,3 +307,35 @@ def test_unset_driver_slots_lower_like_default_drivers():
     assert low[1].tobytes() == a[0].tobytes()
     ref = cmtj.ScalarDriver()
     assert (ref.constantValue, ref.amplitude, ref.frequency) == (0.0, 0.0, -1.0)
+
+
+def test_shared_unset_driver_is_never_changed():
+    """Every layer slot without a driver of its own holds one shared unset
+    driver; the API paths that set, combine, copy and lower drivers leave it
+    equal to a fresh ScalarDriver()."""
+    from cmtj_gb300 import _lower, core
+    fields = core.ScalarDriver.__slots__
+
+    def snapshot(d):
+        return tuple(getattr(d, k) for k in fields)
+
+    fresh = snapshot(core.ScalarDriver())
+    z = cmtj.CVector(0, 0, 0)
+    ls = [cmtj.Layer("L%d" % i, mag=cmtj.CVector(0, 0, 1), anis=cmtj.CVector(0, 0, 1), Ms=1.0, thickness=1e-9,
+                     cellSurface=1e-16, demagTensor=[z, z, z]) for i in range(2)]
+    j = cmtj.Junction(ls, 100, 200)
+    j.setLayerAnisotropyDriver("all", cmtj.constantDriver(1e5))
+    j.setLayerExternalFieldDriver("all", cmtj.AxialDriver(cmtj.sineDriver(0, 1e3, 1e9, 0), cmtj.NullDriver(),
+                                                          cmtj.NullDriver()))
+    j.setIECDriver("L0", "L1", cmtj.constantDriver(1e-4))
+    for l in j.layers:
+        for d in list(l.scalar.values()) + [d for a in l.axial.values() for d in a.drivers]:
+            c = d.copy()
+            c *= 3
+            c += 1
+            c.phaseShift(0.5)
+    j2 = j.layers[0].copy()
+    j2.axial["hoe"].applyMask([1, 0, 1])
+    _lower.lower([j, cmtj.Junction([j2])], _lower.plan_run(1e-12, 1e-13, 1e-13), cmtj.SolverMode.RK4, True)
+    assert snapshot(core._UNSET_DRIVER) == fresh
+    assert j.layers[0].scalar["anis2"] is core._UNSET_DRIVER
