@@ -513,6 +513,21 @@ def main():
         torch.distributed.destroy_process_group()
 
 
+def build_peak_probe():
+    """Compile bench_peak.cu (the FP32 FMA throughput probe that gives the
+    roofline its denominator) into _build/libbench_peak.so."""
+    from cmtj_gb300 import build as cbuild
+    src = os.path.join(ROOT, "bench_peak.cu")
+    out_dir = os.path.join(ROOT, "_build")
+    lib = os.path.join(out_dir, "libbench_peak.so")
+    os.makedirs(out_dir, exist_ok=True)
+    if not os.path.exists(lib) or os.path.getmtime(src) > os.path.getmtime(lib):
+        subprocess.check_call([cbuild._nvcc(), *cbuild.ARCH, "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-shared",
+                               src, "-o", lib + ".tmp"])
+        os.replace(lib + ".tmp", lib)
+    return lib
+
+
 def measure_rest(run, low, spec, n_steps, kern_ms, fft_ms, lib):
     """Roofline, FP64 plain comparisons, FP32-vs-FP64 accuracy, CPU baseline."""
     import torch
@@ -524,9 +539,8 @@ def measure_rest(run, low, spec, n_steps, kern_ms, fft_ms, lib):
     n = spec.n
     kavg = float(np.mean(kern_ms)) / 1e3
     achieved = fpls * n * n_steps * 2 / kavg / 1e12
-    from cmtj_gb300 import build as cbuild
     import ctypes
-    probe = ctypes.CDLL(cbuild.build_probe())
+    probe = ctypes.CDLL(build_peak_probe())
     peaks = {}
     for name in ("cmtj_probe_fp32_peak", "cmtj_probe_fp32x2_peak"):
         fn = getattr(probe, name)

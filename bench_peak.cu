@@ -1,4 +1,5 @@
-// Measurement probe (libcmtj_probe.so, used by bench.py only): FP32 FMA
+// Measurement probe of bench.py (built into _build/libbench_peak.so by
+// bench.build_peak_probe, never part of libcmtj_gpu.so): FP32 FMA
 // throughput of this GPU, the denominator of the FP32 roofline.  Each
 // thread runs 8 independent FMA chains so the pipe, not latency, bounds it.
 // Two forms: scalar FFMA, and the packed two-lane __ffma2_rn (sm_100+).

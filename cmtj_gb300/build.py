@@ -36,9 +36,6 @@ UNITS = {
     "batch_f32_l4.cu": [],
     "reduce.cu": [],
 }
-# measurement-only probe library (FP32 FMA throughput), not the product
-PROBE_UNITS = {"probe_peak.cu": []}
-PROBE_LIB = os.path.join(BUILD, "libcmtj_probe.so")
 
 
 def _nvcc():
@@ -95,11 +92,6 @@ def build(verbose=False, extra_flags=(), units=None, lib=None):
     return lib
 
 
-def build_probe(verbose=False):
-    return build(verbose=verbose, units=PROBE_UNITS, lib=PROBE_LIB)
-
-
 if __name__ == "__main__":
     extra = sys.argv[1:]
     print(build(verbose=True, extra_flags=extra))
-    print(build_probe(verbose=True))

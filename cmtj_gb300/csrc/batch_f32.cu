@@ -1,5 +1,7 @@
 // Host side of the FP32 batched form: variant choice, persistent grid size,
 // ticket reset and launch.
+#include <cuda.h>
+
 #include <mutex>
 
 #include "batch_variants.cuh"
@@ -67,6 +69,14 @@ extern "C" int cmtj_batch_run_f32(const cmtj_f32_junction_t *d_junctions, const 
                      p->log_tile * channels);
       return CMTJ_ERR_LIMIT;
     }
+    // A chunk that ends inside a log tile flushes a partial tile, and the
+    // next chunk's bulk stores would start off a 16-byte boundary.
+    const uint64_t tile_steps = (uint64_t)p->log_every * p->log_tile;
+    if (p->chunk_steps != 0xffffffffu && (uint64_t)p->chunk_steps % tile_steps != 0) {
+      cmtj_set_error("cmtj_batch_run_f32: chunk_steps %u is not a multiple of log_every * log_tile = %llu",
+                     p->chunk_steps, (unsigned long long)tile_steps);
+      return CMTJ_ERR_ARG;
+    }
   }
   const int need_nw = (features >> 16) & 0xff;
   const CmtjBatchVariant *v = pick(n_layers, p->solver, features & 0xffff, need_nw);
@@ -124,11 +134,43 @@ static __device__ __align__(256) uint32_t g_noalloc_tickets[CMTJ_NOALLOC_TICKET_
 namespace {
 constexpr int kMaxDevices = 64;
 std::mutex g_noalloc_mutex;
-uint32_t *g_noalloc_ptr[kMaxDevices] = {nullptr};
+struct NoallocAddress {
+  unsigned long long ctx_id;  // context the address was resolved in (0: unknown)
+  uint32_t *ptr;
+};
+NoallocAddress g_noalloc_addr[kMaxDevices] = {};
 
-// Device address of g_noalloc_tickets on the current device, resolved once
-// per device with that device current.  In host code the array's name is
-// only a host-side stand-in for the symbol, never a device address.
+// Unique id of the calling thread's current context, through the driver
+// entry points the runtime hands out (no link against libcuda, no
+// allocation).  0 when the driver does not offer them.
+unsigned long long current_context_id() {
+  typedef CUresult (*GetCurrentFn)(CUcontext *);
+  typedef CUresult (*GetIdFn)(CUcontext, unsigned long long *);
+  static GetCurrentFn get_current = nullptr;
+  static GetIdFn get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *f = nullptr, *g = nullptr;
+    cudaDriverEntryPointQueryResult q1 = cudaDriverEntryPointSymbolNotFound, q2 = q1;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q1) == cudaSuccess &&
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &g, 12000, cudaEnableDefault, &q2) == cudaSuccess &&
+        q1 == cudaDriverEntryPointSuccess && q2 == cudaDriverEntryPointSuccess) {
+      get_current = reinterpret_cast<GetCurrentFn>(f);
+      get_id = reinterpret_cast<GetIdFn>(g);
+    }
+  });
+  if (!get_current || !get_id) return 0;
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (get_current(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
+
+// Device address of g_noalloc_tickets on the current device, resolved with
+// that device current the first time it is used in a context, and again
+// whenever the device's context changes (after cudaDeviceReset the module
+// is loaded anew and the old address is gone).  In host code the array's
+// name is only a host-side stand-in for the symbol, never a device address.
 int noalloc_tickets(uint32_t **out) {
   int dev = 0;
   CMTJ_CUDA_TRY(cudaGetDevice(&dev));
@@ -136,17 +178,23 @@ int noalloc_tickets(uint32_t **out) {
     cmtj_set_error("cmtj_batch_run_f32_noalloc: device ordinal %d beyond %d", dev, kMaxDevices);
     return CMTJ_ERR_LIMIT;
   }
+  // Before the runtime has made a context current this reads 0, and the
+  // symbol lookup below creates the primary context; the id is read again
+  // after it.  Without the driver entry points every call resolves anew.
+  const unsigned long long ctx = current_context_id();
   std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-  if (!g_noalloc_ptr[dev]) {
+  NoallocAddress &a = g_noalloc_addr[dev];
+  if (!a.ptr || ctx == 0 || a.ctx_id != ctx) {
     void *ptr = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_tickets);
     if (e != cudaSuccess || !ptr) {
       cmtj_set_error("cmtj_batch_run_f32_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
       return CMTJ_ERR_CUDA;
     }
-    g_noalloc_ptr[dev] = static_cast<uint32_t *>(ptr);
+    a.ptr = static_cast<uint32_t *>(ptr);
+    a.ctx_id = current_context_id();
   }
-  *out = g_noalloc_ptr[dev];
+  *out = a.ptr;
   return CMTJ_OK;
 }
 }  // namespace

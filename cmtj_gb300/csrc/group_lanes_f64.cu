@@ -26,9 +26,10 @@ template <int SOLVER, class V>
 __global__ void __launch_bounds__(kGroupLaneThreads)
     k_group_lanes(const cmtj_group_t *__restrict__ groups, const cmtj_pair_t *__restrict__ pairs,
                   const cmtj_junction_t *__restrict__ junctions, const int32_t *__restrict__ top,
-                  const cmtj_layer_t *__restrict__ params, cmtj_layer_t *layers, const double *__restrict__ tables,
+                  const cmtj_layer_t *params, cmtj_layer_t *layers, const double *__restrict__ tables,
                   cmtj_sim_params_t p, int G, double *__restrict__ log, uint32_t *__restrict__ status) {
-  // `params` and `layers` address the same records: every field but mag and
+  // `params` and `layers` address the same records, so neither is
+  // __restrict__: every field but mag and
   // the HRES drivers is read through `params`; mag is read and written and
   // the HRES drivers are written through `layers` only.
   __shared__ double s_m[kMaxGroup][3], s_h[kMaxGroup][3];

@@ -41,7 +41,7 @@ namespace {
 // field and anisotropy drivers may be time-dependent.
 template <int SOLVER, class V, bool DYN, bool FIELD>
 __device__ __forceinline__ void run_lanes(const cmtj_junction_t *__restrict__ junctions, int32_t n_junctions,
-                                          const cmtj_layer_t *__restrict__ params, cmtj_layer_t *layers,
+                                          const cmtj_layer_t *params, cmtj_layer_t *layers,
                                           const double *__restrict__ tables, const cmtj_sim_params_t &p, int G,
                                           double *__restrict__ log, uint32_t *__restrict__ status) {
   const LaneGeo g = lane_geo<V>(G);
@@ -106,10 +106,11 @@ __device__ __forceinline__ void run_lanes(const cmtj_junction_t *__restrict__ ju
 template <int SOLVER, class V>
 __global__ void __launch_bounds__(32)
     k_plain_lanes(const cmtj_junction_t *__restrict__ junctions, int32_t n_junctions,
-                  const cmtj_layer_t *__restrict__ params, cmtj_layer_t *layers, const double *__restrict__ tables,
+                  const cmtj_layer_t *params, cmtj_layer_t *layers, const double *__restrict__ tables,
                   cmtj_sim_params_t p, int G, double *__restrict__ log, uint32_t *__restrict__ status) {
-  // `params` and `layers` address the same records: every field but mag is
-  // read through `params`, mag is read and written through `layers` only.
+  // `params` and `layers` address the same records, so neither is
+  // __restrict__: every field but mag is read through `params`, mag is read
+  // and written through `layers` only.
   const int span = G * V::kLanes;
   const int lane = threadIdx.x;
   const int l = (lane % span) / V::kLanes;

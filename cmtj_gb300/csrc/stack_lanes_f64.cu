@@ -24,11 +24,12 @@ template <int SOLVER, class V>
 __global__ void __launch_bounds__(kStackLaneThreads)
     k_stack_lanes(const cmtj_stack_t *__restrict__ stacks, const double *__restrict__ couplings,
                   const cmtj_junction_t *__restrict__ junctions, const int32_t *__restrict__ top_bottom,
-                  const cmtj_layer_t *__restrict__ params, cmtj_layer_t *layers, const double *__restrict__ tables,
+                  const cmtj_layer_t *params, cmtj_layer_t *layers, const double *__restrict__ tables,
                   cmtj_sim_params_t p, int G, double *__restrict__ log, double *__restrict__ stack_log,
                   int32_t stack_width, uint32_t *__restrict__ status) {
-  // `params` and `layers` address the same records: every field but mag is
-  // read through `params`, mag is read and written through `layers` only.
+  // `params` and `layers` address the same records, so neither is
+  // __restrict__: every field but mag is read through `params`, mag is read
+  // and written through `layers` only.
   __shared__ double s_m[kMaxStack][3], s_p[kMaxStack][3], s_q[kMaxStack][3];
   __shared__ double s_c[kMaxStack], s_R[kMaxStack], s_I[kMaxStack], s_eff[kMaxStack];
   __shared__ double s_total;

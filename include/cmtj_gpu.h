@@ -463,7 +463,11 @@ enum cmtj_log_mode {
 
 typedef struct cmtj_f32_params {
   double dt;              /* time step (s)                                     */
-  uint32_t chunk_steps;   /* max iterations per junction in this launch        */
+  uint32_t chunk_steps;   /* max iterations per junction in this launch
+                           * (0xffffffff: run to the end).  With a log, a
+                           * multiple of log_every * log_tile, so that every
+                           * chunk ends on a whole log tile (else
+                           * CMTJ_ERR_ARG)                                    */
   int32_t solver;         /* CMTJ_RK4, CMTJ_EULER_HEUN or CMTJ_HEUN            */
   int32_t log_mode, log_axis;
   uint32_t log_every;     /* 0: no log                                         */
@@ -524,7 +528,10 @@ int cmtj_batch_variant_f32(int32_t n_layers, int32_t solver, int32_t features);
  * CMTJ_ERR_LIMIT.  The caller still passes every input and output buffer.
  * The first call on a device resolves the array's device address
  * (cudaGetSymbolAddress) with that device current, so make it before any
- * stream capture.  Each call zeroes its slot on `stream` before launching;
+ * stream capture.  The address is cached per device together with the id of
+ * the context it was resolved in, and resolved again when that context
+ * changes (after cudaDeviceReset): the first call after such a reset is a
+ * set-up call too.  Each call zeroes its slot on `stream` before launching;
  * calls that overlap on the GPU and use the same slot race on its ticket. */
 #define CMTJ_NOALLOC_TICKET_SLOTS 64
 int cmtj_batch_run_f32_noalloc(const cmtj_f32_junction_t *d_junctions, const cmtj_f32_layer_t *d_layers,

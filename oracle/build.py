@@ -3,7 +3,7 @@
 Compiles oracle/cmtj_oracle.cpp into oracle/_build/libcmtj_oracle.so with
 -ffp-contract=off so that a*b+c is never fused (the reference's x86-64
 build has no FMA; on aarch64 GCC would otherwise contract), and, when the
-reference sources are present, runs oracle/build_ref.sh to build the real
+reference checkout is named by $CMTJ_REF, runs oracle/build_ref.sh to build the real
 reference extension into oracle/_ref/.
 """
 import os
@@ -37,8 +37,10 @@ def build_oracle(verbose=False):
 
 
 def build_reference(verbose=False):
-    ref = os.environ.get("CMTJ_REF", "/root/reference")
-    if not os.path.isfile(os.path.join(ref, "python", "cmtj.cpp")):
+    """Build oracle/_ref from the reference checkout named by $CMTJ_REF;
+    None when it is unset or holds no python/cmtj.cpp."""
+    ref = os.environ.get("CMTJ_REF")
+    if not ref or not os.path.isfile(os.path.join(ref, "python", "cmtj.cpp")):
         return None
     subprocess.check_call(["bash", os.path.join(HERE, "build_ref.sh")],
                           stdout=None if verbose else subprocess.DEVNULL)

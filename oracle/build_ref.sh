@@ -3,7 +3,7 @@
 # into oracle/_ref/.  The product never loads this: it is the checker that
 # pins the C++ restatement in oracle/ and generates tests/golden/ fixtures.
 #
-# Reads:   $CMTJ_REF (default /root/reference): python/cmtj.cpp + core/*.hpp
+# Reads:   $CMTJ_REF (required: the reference checkout): python/cmtj.cpp + core/*.hpp
 # Writes:  oracle/_ref/_cmtj<ext-suffix>, oracle/_ref/cmtj/__init__.py (shim)
 #
 # Flags follow setup.py:51-88 on Linux (C++17, -fvisibility=hidden,
@@ -13,10 +13,10 @@
 # project-written stand-in header under oracle/stubs/ satisfies noise.hpp.
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
-REF="${CMTJ_REF:-/root/reference}"
+REF="${CMTJ_REF:-}"
 OUT="$HERE/_ref"
-if [ ! -f "$REF/python/cmtj.cpp" ]; then
-  echo "reference sources not found at $REF; skipping _cmtj build" >&2
+if [ -z "$REF" ] || [ ! -f "$REF/python/cmtj.cpp" ]; then
+  echo "reference sources not found (set CMTJ_REF to the reference checkout); skipping _cmtj build" >&2
   exit 0
 fi
 mkdir -p "$OUT"

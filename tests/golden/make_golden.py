@@ -6,7 +6,7 @@ and stores the full-precision logs and final magnetisations as
 <case>.npz.  Needs the reference sources, so it runs in the development
 container only; the fixtures are committed and travel with the tests.
 
-    python tests/golden/make_golden.py [case ...]
+    CMTJ_REF=<reference checkout> python tests/golden/make_golden.py [case ...]
 """
 import os
 import sys
@@ -23,7 +23,7 @@ def reference_module():
     from oracle.build import build_reference
     ref = build_reference()
     if ref is None:
-        raise SystemExit("reference sources not available; cannot regenerate fixtures")
+        raise SystemExit("reference sources not available (set CMTJ_REF); cannot regenerate fixtures")
     sys.path.insert(0, ref)
     import cmtj  # the shim package of oracle/_ref
     import cmtj.stack  # noqa: F401

@@ -2,7 +2,7 @@
 run with the reference extension built from its sources (oracle/_ref).
 Output: tests/golden/groups.npz (key "<case>__<junction>__<log key>").
 
-    python tests/golden/make_groups.py
+    CMTJ_REF=<reference checkout> python tests/golden/make_groups.py
 """
 import os
 import sys

@@ -3,7 +3,7 @@
 from its sources (oracle/_ref) on small sweeps.  Output:
 tests/golden/procedures.npz.
 
-    python tests/golden/make_procedures.py
+    CMTJ_REF=<reference checkout> python tests/golden/make_procedures.py
 """
 import os
 import sys

@@ -7,7 +7,12 @@ reference sources) on the p-bit case of tests/thermal_cases.py: n runs per
 current density, Euler-Heun, T = 300 K, and records how many ended with
 m_z < 0.  Output: tests/golden/pbit_switching.npz.
 
-    python tests/golden/make_thermal.py [runs_per_current]
+With --sweep it runs the p-bit sweep at its full parameters instead
+(thermal_cases.pbit_sweep_junction: Ku 2.5e5 J/m^3, 17 of the sweep's 64
+current densities over [0, 5e11] A/m^2, each run's duration drawn from
+U[5, 20] ns) and writes tests/golden/pbit_sweep.npz.
+
+    CMTJ_REF=<reference checkout> python tests/golden/make_thermal.py [--sweep] [runs_per_current]
 """
 import multiprocessing as mp
 import os
@@ -35,12 +40,51 @@ def _worker(args):
     return switched
 
 
-def main(argv):
+def _sweep_worker(args):
+    ref_path, j_density, n, seed = args
+    sys.path.insert(0, ref_path)
+    import cmtj
+    import thermal_cases
+    switched = 0
+    for d in thermal_cases.sweep_durations(n, seed):
+        junc, run = thermal_cases.pbit_sweep_junction(cmtj, j_density, d)
+        junc.runSimulation(**run)
+        if junc.getLayerMagnetisation("free").z < 0:
+            switched += 1
+    return switched
+
+
+def main_sweep(argv):
     from oracle.build import build_reference
     import thermal_cases
     ref = build_reference()
     if ref is None:
-        raise SystemExit("reference sources not available")
+        raise SystemExit("reference sources not available (set CMTJ_REF)")
+    n = int(argv[0]) if argv else 1024
+    currents = thermal_cases.SWEEP_CURRENTS
+    chunks = 16
+    tasks = [(ref, float(j), n // chunks, 7000 + 100 * q + c)
+             for q, j in enumerate(currents) for c in range(chunks)]
+    with mp.get_context("spawn").Pool(os.cpu_count()) as pool:
+        res = pool.map(_sweep_worker, tasks, chunksize=1)
+    counts = np.array(res).reshape(len(currents), chunks).sum(axis=1)
+    runs = (n // chunks) * chunks
+    np.savez_compressed(os.path.join(HERE, "pbit_sweep.npz"), currents=np.asarray(currents),
+                        switched=counts, runs=np.full(len(currents), runs),
+                        t_min=thermal_cases.SWEEP_T_MIN, t_max=thermal_cases.SWEEP_T_MAX,
+                        Ku=thermal_cases.SWEEP_KU)
+    for j, c in zip(currents, counts):
+        print("j=%.3g  P=%.3f" % (j, c / runs))
+
+
+def main(argv):
+    if argv and argv[0] == "--sweep":
+        return main_sweep(argv[1:])
+    from oracle.build import build_reference
+    import thermal_cases
+    ref = build_reference()
+    if ref is None:
+        raise SystemExit("reference sources not available (set CMTJ_REF)")
     n = int(argv[0]) if argv else 512
     currents = thermal_cases.PBIT_CURRENTS
     chunks = 8

@@ -54,3 +54,23 @@ def test_feature_constants_mirror_header():
     for name in ("FULL_DEMAG", "DIPOLE", "IDMI", "K2", "STT", "SOT", "WAVES", "SCALAR_WAVES", "IEC2", "OFFAXIS",
                  "ALL"):
         assert defs["CMTJ_FEAT_" + name] == getattr(batch, "FEAT_" + name), name
+
+
+def test_f32_batch_rejects_chunk_inside_a_log_tile(lib):
+    """A chunk that ends inside a log tile would leave the next chunk's bulk
+    log stores off a 16-byte boundary: the entry point refuses it before it
+    touches the device (no GPU needed)."""
+    import ctypes
+    import numpy as np
+    from cmtj_gb300 import _abi, batch
+    p = np.zeros(1, dtype=batch.F32_PARAMS_DTYPE)
+    p["solver"] = 0  # RK4
+    p["log_mode"] = batch.LOG_M
+    p["log_every"] = 10
+    p["log_tile"] = 4
+    dummy = ctypes.c_void_p(16)
+    for chunk in (41, 60, 4):  # none a multiple of 10 * 4 steps
+        p["chunk_steps"] = chunk
+        rc = lib.cmtj_batch_run_f32(dummy, dummy, dummy, dummy, 1, 1, 0, p.ctypes.data, dummy, dummy, 0, None)
+        assert rc == _abi.CMTJ_ERR_ARG, chunk
+        assert "not a multiple of log_every * log_tile = 40" in _abi.last_error(lib)

@@ -110,3 +110,79 @@ def test_fp32_and_fp64_forms_share_the_noise_stream(gpu_lib):
         cmtj_gb300, 8e10, 32, 31337)[0]])
     assert np.max(np.abs(m64 - m0)) > 1e-2  # the noise moved m
     assert np.max(np.abs(m32 - m64)) <= 1e-4, np.max(np.abs(m32 - m64))
+
+
+@pytest.mark.gpu
+def test_fp32_batch_full_pbit_sweep_matches_reference(gpu_lib):
+    """The whole stochastic p-bit sweep in the FP32 batched form: 64 current
+    densities over [0, 5e11] A/m^2 x 16,384 single-layer STT junctions
+    (1,048,576), Ku 2.5e5 J/m^3, Euler-Heun at 300 K, each junction's
+    duration drawn from U[5, 20] ns.  At the 17 currents the reference ran
+    (2048 runs each, tests/golden/pbit_sweep.npz), P(m_z < 0 at the end) is
+    within the 3-sigma binomial bound; |m| stays 1 to FP32 rounding."""
+    from cmtj_gb300 import sweeps
+    from test_thermal import load_sweep_ref
+    dt = 1e-13
+    spec, n_steps, jd = sweeps.pbit_config(dt=dt)
+    run = batch.BatchRun(batch.lower(spec, dt, n_steps), dt, cmtj_gb300.SolverMode.EulerHeun)
+    run.launch()
+    st = run.state()
+    assert np.all(st["status"] == 0) and np.all(st["step"] == n_steps)
+    m = st["m"][:, 0, :].astype(np.float64)
+    assert np.max(np.abs(np.linalg.norm(m, axis=1) - 1)) <= 1e-6
+    cur, sw, runs = load_sweep_ref()
+    for q, c in enumerate(cur):
+        sel = jd == c
+        n = int(sel.sum())
+        assert n == 16384, c
+        k = int(np.sum(m[sel, 2] < 0))
+        ok, d, b = binomial_ok(k, n, int(sw[q]), int(runs[q]))
+        assert ok, (c, k / n, sw[q] / runs[q], d, b)
+
+
+def _run_f64_rows(js, plan, solver, every_rows):
+    """The FP64 plain form on `js`, returning only log rows every_rows[k] of
+    junction k (gathered on the device)."""
+    from cmtj_gb300 import _abi
+    t = engine.torch()
+    lib = engine.require_gpu()
+    low = engine.lower(js, plan, solver, False)
+    n, p = len(js), low.params
+    n_log, width = int(p["n_log"][0]), low.log_width
+    d_j, d_l = engine.to_device(low.junctions), engine.to_device(low.layers)
+    d_tab = engine.to_device(low.tables) if low.tables is not None else None
+    d_log = t.empty((n, n_log, width), dtype=t.float64, device="cuda")
+    d_status = t.zeros(2 * n, dtype=t.int32, device="cuda")
+    _abi.check(lib.cmtj_run_simulation_f64(engine.ptr(d_j), n, engine.ptr(d_l), engine.ptr(d_tab), p.ctypes.data,
+                                           engine.ptr(d_log), engine.ptr(d_status), engine.stream_ptr()), lib)
+    idx = t.from_numpy(np.asarray(every_rows, dtype=np.int64)).cuda()
+    rows = d_log[t.arange(n, device="cuda"), idx].cpu().numpy()
+    return rows, d_status.cpu().numpy().view(np.uint32)
+
+
+@pytest.mark.gpu
+def test_fp64_plain_full_pbit_sweep_matches_reference(gpu_lib):
+    """The FP64 plain form on the same 17 currents of the full p-bit sweep,
+    512 runs each with their own U[5, 20] ns durations, in one launch of
+    the longest duration logged every 100 steps: a run of n steps is read
+    from the last log row at or before its end (the state after
+    100 * floor((n - 1) / 100) + 1 steps, at most 10 ps early).  P(m_z < 0)
+    is within the 3-sigma binomial bound of the reference's counts."""
+    from test_thermal import load_sweep_ref
+    cur, sw, runs = load_sweep_ref()
+    dt, every, n = 1e-13, 100, 512
+    js, last = [], []
+    for q, c in enumerate(cur):
+        for k, d in enumerate(thermal_cases.sweep_durations(n, 900 + q)):
+            j, _ = thermal_cases.pbit_sweep_junction(cmtj_gb300, float(c), d)
+            j.layers[0].noise_seed = 40_000_000 + 100_000 * q + k
+            js.append(j)
+            last.append((int(d / dt) - 1) // every)
+    plan = engine.plan_run(thermal_cases.SWEEP_T_MAX, dt, every * dt)
+    rows, status = _run_f64_rows(js, plan, cmtj_gb300.SolverMode.EulerHeun, last)
+    assert np.all(status[0::2] == 0)
+    mz = rows[:, 2]
+    for q, c in enumerate(cur):
+        k = int(np.sum(mz[q * n:(q + 1) * n] < 0))
+        ok, d, b = binomial_ok(k, n, int(sw[q]), int(runs[q]))
+        assert ok, (c, k / n, sw[q] / runs[q], d, b)

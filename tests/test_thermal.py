@@ -15,6 +15,13 @@ def load_ref():
     return g["currents"], g["switched"], g["runs"]
 
 
+def load_sweep_ref():
+    """Reference switching counts of the full p-bit sweep (Ku 2.5e5, 17 of
+    its 64 currents, durations U[5, 20] ns): tests/golden/pbit_sweep.npz."""
+    g = np.load("%s/golden/pbit_sweep.npz" % thermal_cases.__file__.rsplit("/", 1)[0])
+    return g["currents"], g["switched"], g["runs"]
+
+
 def binomial_ok(k1, n1, k2, n2):
     p1, p2 = k1 / n1, k2 / n2
     p = (k1 + k2) / (n1 + n2)
@@ -75,3 +82,39 @@ def check_density(mz, Ku, V, bins=10, sigmas=4.0):
     corr = 8.0
     z = (h - expect) / np.sqrt(corr * np.maximum(expect, 1.0))
     assert np.max(np.abs(z)) < sigmas, (np.round(z, 2), h, np.round(expect))
+
+
+def test_sweep_fixture_matches_its_generator():
+    """The full-sweep fixture holds the 17 currents of thermal_cases (every
+    4th of the sweep's 64 plus the last), 2048 runs each, and its switching
+    probability rises with the current from the thermal floor."""
+    cur, sw, runs = load_sweep_ref()
+    assert np.array_equal(cur, np.asarray(thermal_cases.SWEEP_CURRENTS))
+    assert np.all(runs == 2048)
+    p = sw / runs
+    assert 0.1 < p[0] < 0.3 and p[-1] > 0.7 and p[5] > p[1]
+
+
+def test_oracle_full_sweep_statistics_match_reference():
+    """The oracle (Philox noise) on three currents of the full p-bit sweep,
+    512 runs each with their own U[5, 20] ns durations, within the 3-sigma
+    binomial bound of the reference's counts."""
+    from concurrent.futures import ThreadPoolExecutor
+    cur, sw, runs = load_sweep_ref()
+    oracle_harness.oracle_lib()
+    n = 512
+    for q in (0, 2, 16):
+        jd = float(cur[q])
+        durs = thermal_cases.sweep_durations(n, 500 + q)
+
+        def one(k):
+            j, run = thermal_cases.pbit_sweep_junction(cmtj_gb300, jd, durs[k])
+            j.layers[0].noise_seed = 3_000_000 + 10_000 * q + k
+            r = dict(run)
+            oracle_harness.run_oracle([j], r.pop("totalTime"), **r)
+            return j.getLayerMagnetisation("free").z < 0
+
+        with ThreadPoolExecutor(8) as ex:
+            k = sum(ex.map(one, range(n)))
+        ok, d, b = binomial_ok(k, n, int(sw[q]), int(runs[q]))
+        assert ok, (jd, k / n, sw[q] / runs[q], d, b)

@@ -55,10 +55,10 @@ def test_noalloc_matches_allocating_entry_point(gpu_lib):
     ref_log = run.d_log.cpu().numpy().copy()
     assert np.all(ref_state["status"] == 0) and np.all(ref_state["step"] == 2000)
 
-    for call in range(2):  # two calls in a row share (and re-zero) the static ticket
+    for call in range(2):  # two calls in a row on the same slot: the second re-zeroes the used ticket
         run.d_s.copy_(zero_state)
         run.d_log.zero_()
-        _run_noalloc(run, lib, slot=call)
+        _run_noalloc(run, lib, slot=3)
         torch.cuda.synchronize()
         st = run.state()
         log = run.d_log.cpu().numpy()

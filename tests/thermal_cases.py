@@ -36,3 +36,29 @@ def boltzmann_mz_density(mz, Ku, V, T, kB=1.380649e-23):
     x = np.linspace(-1, 1, 20001)
     Z = np.trapezoid(np.exp(d * x * x), x)
     return np.exp(d * np.asarray(mz) ** 2) / Z
+
+
+# The p-bit sweep at its full parameters (1,048,576 junctions in the bench:
+# 64 current densities over [0, 5e11] A/m^2 x 16,384): Ku 2.5e5 J/m^3, a
+# barrier of about 5 kT at 300 K, the same STT layer as above, a 1 ns
+# current step, and a duration drawn per run from U[5, 20] ns.  The
+# reference fixture uses every 4th current of the 64 plus the last one.
+SWEEP_KU = 2.5e5
+SWEEP_T_MIN, SWEEP_T_MAX = 5e-9, 20e-9
+SWEEP_ALL_CURRENTS = [float(x) for x in __import__("numpy").linspace(0, 5e11, 64)]
+SWEEP_CURRENTS = SWEEP_ALL_CURRENTS[0:64:4] + [SWEEP_ALL_CURRENTS[63]]
+
+
+def sweep_durations(n, seed):
+    """Per-run durations U[5, 20] ns (seeded)."""
+    import numpy as np
+    return np.random.default_rng(seed).uniform(SWEEP_T_MIN, SWEEP_T_MAX, size=n)
+
+
+def pbit_sweep_junction(cm, j_density, duration):
+    """One junction of the full p-bit sweep and its run arguments (logging
+    once per ns: the observable is the final m_z)."""
+    j, run = pbit_junction(cm, j_density, Ku=SWEEP_KU)
+    run = dict(run)
+    run.update(totalTime=float(duration), writeFrequency=1e-9)
+    return j, run
