@@ -12,6 +12,7 @@ import os
 import numpy as np
 
 MAX_LAYERS = 8
+ALPHA_MAX_LEN = 8388608  # CMTJ_ALPHA_MAX_LEN: samples per alpha-noise buffer
 MAX_LAYERS_F32 = 4
 NUM_SLOTS = 30
 ENERGY_COLS = 29
@@ -56,7 +57,13 @@ LAYER_DTYPE = np.dtype(
      ("seed_lo", "<u4"), ("seed_hi", "<u4"), ("noise_step", "<u8"),
      ("drv", DRIVER_DTYPE, NUM_SLOTS), ("adaptive", ADAPTIVE_DTYPE),
      ("conv_term", "<f8"), ("stoch_conv", "<f8"), ("ms_over_mu0", "<f8"), ("zero_terms", "<u4"),
-     ("reserved2", "<u4")], align=True)
+     ("reserved2", "<u4"), ("alpha_buf", "<u8"), ("alpha_scale", "<f8"), ("alpha_len", "<u4"),
+     ("alpha_axis", "<i4")], align=True)
+
+# cmtj_alpha_noise_t: one buffer row of BufferedAlphaNoise::fillBuffer.
+ALPHA_NOISE_DTYPE = np.dtype(
+    [("alpha", "<f8"), ("std", "<f8"), ("seed_lo", "<u4"), ("seed_hi", "<u4"), ("counter", "<u8"),
+     ("component", "<i4"), ("reserved", "<i4")], align=True)
 
 ZERO_DIPOLE, ZERO_IDMI, ZERO_K2, ZERO_J2 = 1, 2, 4, 8
 
@@ -116,6 +123,8 @@ PROTOTYPES = {
     "cmtj_spectrum_f32": (ctypes.c_int, [_P, ctypes.c_int64, _I32, _I32, _I32, _I32, _I32, _P, _P]),
     "cmtj_run_stack_f64": (ctypes.c_int, [_P, _I32, _P, _P, _P, _P, _P, _P, _P, _P, _I32, _I32, _P, _P]),
     "cmtj_run_group_f64": (ctypes.c_int, [_P, _I32, _P, _P, _P, _P, _P, _P, _P, _I32, _P, _P]),
+    "cmtj_alpha_noise_scratch_bytes": (ctypes.c_size_t, [ctypes.c_uint32]),
+    "cmtj_alpha_noise_f32": (ctypes.c_int, [_P, _I32, ctypes.c_uint32, _P, _P, _P, ctypes.c_size_t, _P]),
 }
 
 _lib = None
@@ -155,6 +164,7 @@ def check_layout(lib):
     sizes["cmtj_stack_t"] = STACK_DTYPE.itemsize
     sizes["cmtj_group_t"] = GROUP_DTYPE.itemsize
     sizes["cmtj_pair_t"] = PAIR_DTYPE.itemsize
+    sizes["cmtj_alpha_noise_t"] = ALPHA_NOISE_DTYPE.itemsize
     n = len(sizes)
     buf = (ctypes.c_int32 * n)()
     lib.cmtj_struct_sizes(ctypes.cast(buf, _P), n)

@@ -256,8 +256,8 @@ def validate(junctions, solver, max_layers=_abi.MAX_LAYERS):
             raise ValueError("the GPU solver supports at most %d layers per junction, got %d" %
                              (max_layers, j.layerNo))
         for l in j.layers:
-            if l.alphaNoiseScale != 0:
-                raise RuntimeError("buffered 1/f alpha noise (core/noise.hpp) is not supported by the GPU solver")
+            if l.alphaNoiseScale != 0 and solver not in (SolverMode.EulerHeun, SolverMode.Heun):
+                raise RuntimeError("buffered alpha noise runs under Euler-Heun or Heun (getSolver forces them)")
             if l.Ms * l.thickness == 0:
                 raise RuntimeError("Failed to divide vector by zero!")
             if l.temperatureSet and solver in (SolverMode.EulerHeun, SolverMode.Heun) and l.cellVolume == 0.0:
@@ -271,6 +271,35 @@ class Lowered:
     tables: np.ndarray
     params: np.ndarray
     log_width: int
+    # buffered alpha noise of this run: cmtj_alpha_noise_t rows (x, y, z of
+    # each noisy layer in turn) and the layer index each triple belongs to;
+    # the runner fills the buffers and sets layers[q]["alpha_buf"]
+    alpha_specs: np.ndarray = None
+    alpha_layers: np.ndarray = None
+
+
+def alpha_noise_rows(layers, larr, plan):
+    """cmtj_alpha_noise_t rows of the layers with a non-zero alpha-noise
+    scale (createBufferedAlphaNoise(totalIterations) per layer and run,
+    junction.hpp:1912-1916): three rows (normals 0, 1, 2 of the layer's
+    alpha-noise stream at counter noise_step + m) per noisy layer; fills
+    the layers' alpha_scale, alpha_axis and alpha_len."""
+    from .noise import specs_array
+    rows, which = [], []
+    for q, l in enumerate(layers):
+        if l.alphaNoiseScale == 0:
+            continue
+        which.append(q)
+        rows += [(l.alphaNoise, l.alphaNoiseStd, l.noise_seed, l.noise_step, c) for c in range(3)]
+        larr[q]["alpha_scale"] = l.alphaNoiseScale
+        larr[q]["alpha_axis"] = int(l.alphaNoiseAxis)
+        larr[q]["alpha_len"] = plan.total_iterations
+    if not which:
+        return None, None
+    if plan.total_iterations > _abi.ALPHA_MAX_LEN:
+        raise ValueError("alpha noise: %d iterations exceed the %d samples of a buffer" %
+                         (plan.total_iterations, _abi.ALPHA_MAX_LEN))
+    return specs_array(rows), np.asarray(which, dtype=np.int64)
 
 
 def lower(junctions, plan, solver, calculate_energies):
@@ -285,11 +314,27 @@ def lower(junctions, plan, solver, calculate_energies):
     for k, j in enumerate(junctions):
         lower_junction(j, jarr[k], off)
         off += j.layerNo
-    lower_layers([l for j in junctions for l in j.layers], larr, tables)
+    all_layers = [l for j in junctions for l in j.layers]
+    lower_layers(all_layers, larr, tables)
+    alpha_specs, alpha_layers = (alpha_noise_rows(all_layers, larr, plan) if plan.total_iterations
+                                 else (None, None))
     max_layers = max(j.layerNo for j in junctions)
     width = _abi.log_width(max_layers, calculate_energies)
     params = make_params(plan, solver, calculate_energies, width, max_layers)
-    return Lowered(jarr, larr, tables.array(), params, width)
+    return Lowered(jarr, larr, tables.array(), params, width, alpha_specs, alpha_layers)
+
+
+def with_alpha_buffers(lowered, base_address):
+    """The layer records with alpha_buf pointing into a buffer array at
+    base_address ([rows][alpha_len] float32, rows in alpha_specs order)."""
+    larr = lowered.layers
+    if lowered.alpha_specs is None:
+        return larr
+    larr = larr.copy()
+    n = int(larr[lowered.alpha_layers[0]]["alpha_len"])
+    for a, q in enumerate(lowered.alpha_layers.tolist()):
+        larr[q]["alpha_buf"] = base_address + 4 * 3 * a * n
+    return larr
 
 
 def make_params(plan, solver, calculate_energies, width, max_layers=0):

@@ -295,7 +295,8 @@ class BatchSpec:
         self.wave_drivers[k] = []
         for l, ly in enumerate(j.layers):
             if ly.alphaNoiseScale != 0:
-                raise RuntimeError("buffered 1/f alpha noise is not supported by the GPU solver")
+                raise RuntimeError("the FP32 batched form has no buffered alpha noise; the FP64 plain form "
+                                   "(Junction.runSimulation) runs it")
             self.m0[k, l] = ly.mag.tolist()
             self.anis[k, l] = ly.anis.tolist()
             self.Ms[k, l], self.thickness[k, l] = ly.Ms, ly.thickness

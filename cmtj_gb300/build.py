@@ -35,6 +35,7 @@ UNITS = {
     "batch_f32_l3.cu": [],
     "batch_f32_l4.cu": [],
     "reduce.cu": [],
+    "alpha_noise.cu": [],
 }
 
 

@@ -555,7 +555,12 @@ class Layer:
         self.dipoleBottom = [CVector(), CVector(), CVector()]
         self.scalar = {k: _UNSET_DRIVER for k in _SCALAR_SLOTS}
         self.axial = {k: AxialDriver._unset() for k in _AXIAL_SLOTS}
+        # BufferedNoiseParameters defaults (junction.hpp:203-209)
+        self.alphaNoise = 1.0
+        self.alphaNoiseStd = 0.0
         self.alphaNoiseScale = 0.0
+        self.alphaNoiseAxis = Axis.all
+        self._alpha_source = None
         self.adaptiveParams = AdaptiveIntegrationParams()
         # Thermal noise stream: copies of a Layer share it, like the
         # reference's copied std::mt19937 state.
@@ -730,21 +735,36 @@ class Layer:
     def setAdaptiveParams(self, params):
         self.adaptiveParams = params
 
-    # 1/f and buffered alpha noise (core/noise.hpp) are outside the GPU
-    # solver.  setOneFNoise has no effect on the reference's solvers either;
-    # a non-zero alpha-noise scale is rejected at runSimulation.
+    # 1/f noise (OneFNoise, core/noise.hpp:72-135): the reference's solvers
+    # never tick it (getStochasticOneFNoise has no caller), so setting it
+    # changes no run, here as there.
     def setOneFNoise(self, sources, bias, scale):
         pass
 
+    # Buffered 1/f^alpha noise (setAlphaNoise / createBufferedAlphaNoise /
+    # getOneFVector, junction.hpp:406-424, 1130-1136): with a non-zero
+    # scale, runSimulation forces Euler-Heun (unless Heun) and every run
+    # gets fresh buffers of its iteration count, filled on the GPU
+    # (cmtj_gb300.noise) from this layer's Philox key on the alpha-noise
+    # stream, at counter noise_step.
     def setAlphaNoise(self, alpha, std, scale, axis=Axis.all):
         if alpha < 0 or alpha > 2:
             raise RuntimeError("alpha must be between 0 and 2")
+        self.alphaNoise = float(alpha)
+        self.alphaNoiseStd = float(std)
         self.alphaNoiseScale = float(scale)
+        self.alphaNoiseAxis = Axis(int(axis))
 
     def createBufferedAlphaNoise(self, bufferSize):
-        pass
+        from .noise import VectorAlphaNoise
+        self._alpha_source = VectorAlphaNoise(bufferSize, self.alphaNoise, self.alphaNoiseStd,
+                                              self.alphaNoiseScale, self.alphaNoiseAxis)
 
     def getOneFVector(self):
+        if self.alphaNoiseScale != 0:
+            if self._alpha_source is None:
+                raise RuntimeError("getOneFVector: createBufferedAlphaNoise(bufferSize) has not been called")
+            return self._alpha_source.tickVector()
         return CVector()
 
 

@@ -24,18 +24,18 @@ int cmtj_log_width(int n_layers, int calculate_energies) {
 }
 
 int cmtj_struct_sizes(int32_t *sizes, int32_t n) {
-  const int32_t all[13] = {(int32_t)sizeof(cmtj_driver_t),       (int32_t)sizeof(cmtj_layer_t),
+  const int32_t all[14] = {(int32_t)sizeof(cmtj_driver_t),       (int32_t)sizeof(cmtj_layer_t),
                            (int32_t)sizeof(cmtj_junction_t),     (int32_t)sizeof(cmtj_constants_t),
                            (int32_t)sizeof(cmtj_sim_params_t),   (int32_t)sizeof(cmtj_wave_t),
                            (int32_t)sizeof(cmtj_f32_layer_t),    (int32_t)sizeof(cmtj_f32_junction_t),
                            (int32_t)sizeof(cmtj_f32_state_t),    (int32_t)sizeof(cmtj_f32_params_t),
                            (int32_t)sizeof(cmtj_stack_t),        (int32_t)sizeof(cmtj_group_t),
-                           (int32_t)sizeof(cmtj_pair_t)};
+                           (int32_t)sizeof(cmtj_pair_t),         (int32_t)sizeof(cmtj_alpha_noise_t)};
   if (!sizes || n < 0) {
     cmtj_set_error("cmtj_struct_sizes: null output");
     return CMTJ_ERR_ARG;
   }
-  for (int i = 0; i < n && i < 13; ++i) sizes[i] = all[i];
+  for (int i = 0; i < n && i < 14; ++i) sizes[i] = all[i];
   return CMTJ_OK;
 }
 

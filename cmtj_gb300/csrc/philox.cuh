@@ -34,10 +34,13 @@ __device__ __forceinline__ uint4 cmtj_thermal_words(uint32_t seed_lo, uint32_t s
                             seed_lo, seed_hi);
 }
 
-// FP64 draws (plain form).
-__device__ __forceinline__ void cmtj_gaussian3_f64(uint32_t seed_lo, uint32_t seed_hi, uint64_t step,
-                                                   double &g0, double &g1, double &g2) {
-  const uint4 w = cmtj_thermal_words(seed_lo, seed_hi, step);
+// The white draws of a layer's buffered 1/f^alpha noise: the same key and
+// transform as the thermal draws, with counter {i_lo, i_hi, 0xA1F4, 0} for
+// draw i, an independent stream.
+#define CMTJ_ALPHA_TAG 0xA1F4u
+
+// FP64 Box-Muller of one Philox block (plain form).
+__device__ __forceinline__ void cmtj_gaussian3_of_words(uint4 w, double &g0, double &g1, double &g2) {
   const double s = 2.3283064365386963e-10;  // 2^-32
   const double u0 = ((double)w.x + 0.5) * s, u1 = ((double)w.y + 0.5) * s;
   const double u2 = ((double)w.z + 0.5) * s, u3 = ((double)w.w + 0.5) * s;
@@ -46,6 +49,20 @@ __device__ __forceinline__ void cmtj_gaussian3_f64(uint32_t seed_lo, uint32_t se
   g0 = r0 * cos(a0);
   g1 = r0 * sin(a0);
   g2 = r1 * cos(a1);
+}
+
+// FP64 thermal draws (plain form).
+__device__ __forceinline__ void cmtj_gaussian3_f64(uint32_t seed_lo, uint32_t seed_hi, uint64_t step,
+                                                   double &g0, double &g1, double &g2) {
+  cmtj_gaussian3_of_words(cmtj_thermal_words(seed_lo, seed_hi, step), g0, g1, g2);
+}
+
+// FP64 white draws of the buffered alpha noise.
+__device__ __forceinline__ void cmtj_alpha_gaussian3_f64(uint32_t seed_lo, uint32_t seed_hi, uint64_t i,
+                                                         double &g0, double &g1, double &g2) {
+  cmtj_gaussian3_of_words(
+      cmtj_philox4x32_10(make_uint4((uint32_t)i, (uint32_t)(i >> 32), CMTJ_ALPHA_TAG, 0u), seed_lo, seed_hi), g0, g1,
+      g2);
 }
 
 // FP32 draws (batched form): the same words, transformed in single

@@ -307,17 +307,41 @@ static __device__ __forceinline__ V stoch_torque(const cmtj_layer_t &L, const cm
   return (th + th2 * L.damping) * convTerm;
 }
 
-// getStochasticLangevinVector (junction.hpp:1111-1128).
+// getOneFVector (junction.hpp:1130-1136): the layer's buffered 1/f^alpha
+// sample of iteration i, VectorAlphaNoise::tickVector (noise.hpp:280-290):
+// the float samples of the active axis (all three, normalised, for
+// Axis::all) times the scale.  Iterations beyond the buffer read zero.
+template <class V>
+static __device__ __forceinline__ V alpha_sample(const cmtj_layer_t &L, uint32_t i) {
+  if (i >= L.alpha_len) return V::zero();
+  const float *b = L.alpha_buf + i;
+  const size_t n = L.alpha_len;
+  const int ax = L.alpha_axis;
+  const double x = (ax == 0 || ax == 3) ? (double)b[0] : 0.0;
+  const double y = (ax == 1 || ax == 3) ? (double)b[n] : 0.0;
+  const double z = (ax == 2 || ax == 3) ? (double)b[2 * n] : 0.0;
+  V v = V::make(x, y, z);
+  if (ax == 3) v = normalized(v);
+  return v * L.alpha_scale;
+}
+
+// getStochasticLangevinVector (junction.hpp:1111-1128), plus the buffered
+// alpha noise where the layer has one: dW of the Euler-Heun and Heun
+// runners (junction.hpp:1726-1727, 1792-1793).
 template <class V = D3>
 static __device__ __forceinline__ V langevin(const cmtj_layer_t &L, const cmtj_constants_t &c, double time,
                                        uint32_t i, const DriverCtx &dc, uint32_t dyn = 0xffffffffu) {
-  if (!L.temperatureSet) return V::zero();
-  const double temp = slot_at(L, CMTJ_SLOT_TEMPERATURE, time, dc, dyn);
-  const double mainFactor = (2 * L.damping * c.kB * temp) / (L.Ms * L.cellVolume * c.gyro);
-  const double sigma = sqrt(mainFactor);
-  double g0, g1, g2;
-  cmtj_gaussian3_f64(L.seed_lo, L.seed_hi, L.noise_step + i, g0, g1, g2);
-  return V::make(g0, g1, g2) * sigma;
+  V dW = V::zero();
+  if (L.temperatureSet) {
+    const double temp = slot_at(L, CMTJ_SLOT_TEMPERATURE, time, dc, dyn);
+    const double mainFactor = (2 * L.damping * c.kB * temp) / (L.Ms * L.cellVolume * c.gyro);
+    const double sigma = sqrt(mainFactor);
+    double g0, g1, g2;
+    cmtj_gaussian3_f64(L.seed_lo, L.seed_hi, L.noise_step + i, g0, g1, g2);
+    dW = V::make(g0, g1, g2) * sigma;
+  }
+  if (L.alpha_buf) dW = dW + alpha_sample<V>(L, i);
+  return dW;
 }
 
 

@@ -46,6 +46,20 @@ def stream_ptr(stream=None):
     return ctypes.c_void_p(s.cuda_stream)
 
 
+def device_layers(lowered, stream=None):
+    """Upload the layer records of a lowered run.  Layers with buffered
+    alpha noise first get this run's buffers, filled on the GPU
+    (cmtj_alpha_noise_f32) and referenced from their records.  Returns
+    (layers tensor, buffers tensor or None); keep both until the run ends."""
+    if lowered.alpha_specs is None:
+        return to_device(lowered.layers), None
+    from .noise import device_buffers
+    n = int(lowered.layers[lowered.alpha_layers[0]]["alpha_len"])
+    bufs = device_buffers(lowered.alpha_specs, n, stream=stream)
+    from ._lower import with_alpha_buffers
+    return to_device(with_alpha_buffers(lowered, bufs.data_ptr())), bufs
+
+
 def run_lowered_f64(lowered, stream=None):
     """Run a lowered batch on the FP64 plain form; returns host arrays
     (log [n][n_log][width], status [n*2], updated layers)."""
@@ -56,7 +70,7 @@ def run_lowered_f64(lowered, stream=None):
     n_log = int(p["n_log"][0])
     width = lowered.log_width
     d_j = to_device(lowered.junctions)
-    d_l = to_device(lowered.layers)
+    d_l, alpha = device_layers(lowered, stream)
     d_tab = to_device(lowered.tables) if lowered.tables is not None else None
     d_log = t.empty((n, max(n_log, 1), width), dtype=t.float64, device="cuda")
     d_status = t.zeros(2 * n, dtype=t.int32, device="cuda")
@@ -66,6 +80,7 @@ def run_lowered_f64(lowered, stream=None):
     log = d_log.cpu().numpy()
     status = d_status.cpu().numpy().view(np.uint32)
     layers = d_l.cpu().numpy().view(_abi.LAYER_DTYPE).copy()
+    del alpha
     return log, status, layers
 
 

@@ -222,7 +222,8 @@ def run_groups(groups, totalTime, timeStep=1e-13, writeFrequency=1e-11):
     t = engine.torch()
     n = len(junctions)
     d_g, d_p = engine.to_device(grec), engine.to_device(pairs)
-    d_j, d_l = engine.to_device(low.junctions), engine.to_device(low.layers)
+    d_j = engine.to_device(low.junctions)
+    d_l, alpha = engine.device_layers(low)  # alpha: this run's noise buffers, kept until it ends
     d_tab = engine.to_device(low.tables) if low.tables is not None else None
     d_top = engine.to_device(tops)
     d_log = t.empty((n, max(plan.n_log, 1), low.log_width), dtype=t.float64, device="cuda")

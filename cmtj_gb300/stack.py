@@ -227,7 +227,8 @@ def run_stacks(stacks, totalTime, timeStep=1e-13, writeFrequency=1e-11):
     t = engine.torch()
     n = len(junctions)
     n_log = plan.n_log
-    d_j, d_l = engine.to_device(low.junctions), engine.to_device(low.layers)
+    d_j = engine.to_device(low.junctions)
+    d_l, alpha = engine.device_layers(low)  # alpha: this run's noise buffers, kept until it ends
     d_tab = engine.to_device(low.tables) if low.tables is not None else None
     d_s = engine.to_device(srec)
     d_c = engine.to_device(np.asarray(couplings, dtype=np.float64))

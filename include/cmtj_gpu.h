@@ -143,6 +143,18 @@ typedef struct cmtj_layer {
    * skips them. */
   double conv_term, stoch_conv, ms_over_mu0;
   uint32_t zero_terms, reserved2;
+  /* Buffered 1/f^alpha noise of this run (setAlphaNoise, getOneFVector,
+   * junction.hpp:406-424, 1130-1136): null for none, else the samples of
+   * iterations 0 .. alpha_len-1 in three rows (x, y, z) of alpha_len floats
+   * each, as cmtj_alpha_noise_f32 writes them.  alpha_axis is the Axis:
+   * 0, 1, 2 use that component alone; 3 (all) uses the normalised sample
+   * vector (VectorAlphaNoise::tickVector, noise.hpp:280-290).  The
+   * Euler-Heun and Heun runners add alpha_scale times it to the layer's
+   * thermal dW at iteration i (junction.hpp:1727, 1793). */
+  const float *alpha_buf;
+  double alpha_scale;
+  uint32_t alpha_len;
+  int32_t alpha_axis;
 } cmtj_layer_t;
 
 #define CMTJ_ZERO_DIPOLE 1u  /* both dipole tensors are zero                 */
@@ -538,6 +550,41 @@ int cmtj_batch_run_f32_noalloc(const cmtj_f32_junction_t *d_junctions, const cmt
                                cmtj_f32_state_t *d_state, const int32_t *d_order, int32_t n, int32_t n_layers,
                                int32_t features, const cmtj_f32_params_t *p, float *d_log, int32_t ticket_slot,
                                int32_t grid_blocks, void *stream);
+
+/* ---------------------------------------------------------------------- */
+/* Buffered 1/f^alpha noise (core/noise.hpp:138-241).                      */
+/* ---------------------------------------------------------------------- */
+/* One buffer row of BufferedAlphaNoise::fillBuffer: n white draws of
+ * standard deviation `std` coloured by the 1/f^alpha filter.  The white
+ * draw m is normal `component` (0, 1 or 2) of the Philox4x32-10 block with
+ * key (seed_lo, seed_hi) and counter {counter + m, 0xA1F4, 0}, the thermal
+ * stream's Box-Muller transform on an independent counter tag. */
+typedef struct cmtj_alpha_noise {
+  double alpha;           /* exponent in [0, 2] (outside: NaN samples)      */
+  double std;             /* standard deviation of the white draws          */
+  uint32_t seed_lo, seed_hi;
+  uint64_t counter;
+  int32_t component;
+  int32_t reserved;
+} cmtj_alpha_noise_t;     /* 40 bytes */
+
+#define CMTJ_ALPHA_MAX_LEN 8388608u  /* samples per buffer (2^23)          */
+
+/* Scratch bytes per buffer row for buffers of n samples (0 when n is 0 or
+ * above CMTJ_ALPHA_MAX_LEN): three complex float rows of the power-of-two
+ * FFT size M >= 2n - 1 and 64 bytes. */
+size_t cmtj_alpha_noise_scratch_bytes(uint32_t n);
+
+/* BufferedAlphaNoise::fillBuffer (noise.hpp:186-225) for n_buffers rows:
+ * d_out[r*n .. r*n+n) = the reference's buffer of d_specs[r] (a device
+ * array).  d_white, when not null, holds the white draws [n_buffers][n]
+ * instead of the Philox ones.  The caller's 16-byte aligned d_scratch of
+ * scratch_bytes holds k >= 1 rows' scratch; rows are processed k at a time.
+ * Samples follow the reference's algorithm exactly (weights by its float
+ * recurrence, the halved bins 0 and n-1 and the dropped upper half),
+ * computed as one FFT convolution plus the two top bins in FP64. */
+int cmtj_alpha_noise_f32(const cmtj_alpha_noise_t *d_specs, int32_t n_buffers, uint32_t n, const float *d_white,
+                         float *d_out, void *d_scratch, size_t scratch_bytes, void *stream);
 
 /* ---------------------------------------------------------------------- */
 /* On-device reductions.                                                   */

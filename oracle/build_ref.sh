@@ -4,7 +4,8 @@
 # pins the C++ restatement in oracle/ and generates tests/golden/ fixtures.
 #
 # Reads:   $CMTJ_REF (required: the reference checkout): python/cmtj.cpp + core/*.hpp
-# Writes:  oracle/_ref/_cmtj<ext-suffix>, oracle/_ref/cmtj/__init__.py (shim)
+# Writes:  oracle/_ref/_cmtj<ext-suffix>, oracle/_ref/libalpha_ref.so,
+#          oracle/_ref/cmtj/__init__.py (shim)
 #
 # Flags follow setup.py:51-88 on Linux (C++17, -fvisibility=hidden,
 # -Wno-unused-variable) at -O3, plus -ffp-contract=off so that no compiler
@@ -29,6 +30,13 @@ if [ ! -f "$TARGET" ] || [ "$REF/core/junction.hpp" -nt "$TARGET" ]; then
       -I"$REF" -I"$REF/core" -I"$HERE/stubs/third_party" \
       $PYBIND_INC "$REF/python/cmtj.cpp" -o "$TARGET.tmp"
   mv "$TARGET.tmp" "$TARGET"
+fi
+# The reference's BufferedAlphaNoise behind a C entry point (alpha_ref.cpp).
+ALPHA="$OUT/libalpha_ref.so"
+if [ ! -f "$ALPHA" ] || [ "$REF/core/noise.hpp" -nt "$ALPHA" ] || [ "$HERE/alpha_ref.cpp" -nt "$ALPHA" ]; then
+  g++ -O2 -shared -fPIC -std=c++17 -ffp-contract=off -I"$REF/core" -I"$HERE/stubs/third_party" \
+      "$HERE/alpha_ref.cpp" -o "$ALPHA.tmp"
+  mv "$ALPHA.tmp" "$ALPHA"
 fi
 # A shim package named `cmtj` whose submodules (cmtj.utils, cmtj.stack, ...)
 # resolve from the reference tree, so no reference file is copied here.

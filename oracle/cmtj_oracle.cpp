@@ -14,7 +14,8 @@
 //   core/junction.hpp:716-831          solveLLG (LLG + STT + SOT), stochasticTorque
 //   core/junction.hpp:866-1002         Layer::dormand_prince_step
 //   core/junction.hpp:1017-1041        Layer::rk4_step
-//   core/junction.hpp:1111-1128        thermal field standard deviation
+//   core/junction.hpp:1111-1136        thermal field standard deviation, getOneFVector
+//   core/noise.hpp:160-225, 280-290    BufferedAlphaNoise::fillBuffer, VectorAlphaNoise::tickVector
 //   core/junction.hpp:1580-1636        logLayerParams
 //   core/junction.hpp:1668-1815        runners (single/multi layer, Euler-Heun, Heun)
 //   core/junction.hpp:1835-1867        strip / classic magnetoresistance
@@ -38,6 +39,7 @@
 #include <vector>
 #include <algorithm>
 #include <atomic>
+#include <complex>
 
 #include "../include/cmtj_gpu.h"
 
@@ -153,12 +155,14 @@ inline U4 philox4x32_10(U4 c, uint32_t k0, uint32_t k1) {
   return c;
 }
 // Three N(0,1) draws of one layer at one step: Box-Muller on the four
-// 32-bit words, u = (w + 0.5) / 2^32 in (0, 1).
-inline void gaussian3(uint32_t seed_lo, uint32_t seed_hi, uint64_t step, double g[3]) {
+// 32-bit words, u = (w + 0.5) / 2^32 in (0, 1).  The counter's third word
+// tags the stream: 0x7E4D the thermal field, 0xA1F4 the white draws of the
+// buffered alpha noise.
+inline void gaussian3_tag(uint32_t tag, uint32_t seed_lo, uint32_t seed_hi, uint64_t step, double g[3]) {
   U4 c;
   c.v[0] = (uint32_t)step;
   c.v[1] = (uint32_t)(step >> 32);
-  c.v[2] = 0x7E4Du;  // thermal-field stream tag
+  c.v[2] = tag;
   c.v[3] = 0u;
   const U4 w = philox4x32_10(c, seed_lo, seed_hi);
   const double s = 2.3283064365386963e-10;  // 2^-32
@@ -169,6 +173,101 @@ inline void gaussian3(uint32_t seed_lo, uint32_t seed_hi, uint64_t step, double 
   g[0] = r0 * cos(a0);
   g[1] = r0 * sin(a0);
   g[2] = r1 * cos(a1);
+}
+inline void gaussian3(uint32_t seed_lo, uint32_t seed_hi, uint64_t step, double g[3]) {
+  gaussian3_tag(0x7E4Du, seed_lo, seed_hi, step, g);
+}
+
+// ------------------------------------------------------ buffered alpha noise
+// Iterative radix-2 complex FFT in FP64 (size a power of two); sign -1
+// forward, +1 inverse (unnormalised).
+inline void fft_pow2(std::vector<std::complex<double>> &a, int sign) {
+  const size_t n = a.size();
+  for (size_t i = 1, j = 0; i < n; ++i) {
+    size_t bit = n >> 1;
+    for (; j & bit; bit >>= 1) j ^= bit;
+    j ^= bit;
+    if (i < j) std::swap(a[i], a[j]);
+  }
+  for (size_t len = 2; len <= n; len <<= 1) {
+    const double ang = sign * 2.0 * M_PI / (double)len;
+    for (size_t i = 0; i < n; i += len) {
+      for (size_t k = 0; k < len / 2; ++k) {
+        const std::complex<double> w(std::cos(ang * (double)k), std::sin(ang * (double)k));
+        const std::complex<double> u = a[i + k], v = a[i + k + len / 2] * w;
+        a[i + k] = u + v;
+        a[i + k + len / 2] = u - v;
+      }
+    }
+  }
+}
+
+// BufferedAlphaNoise::fillBuffer (noise.hpp:186-225) of one buffer of n
+// samples.  White draws: `white` when given, else std times normal
+// `component` of the alpha-noise Philox stream at counter + m (the
+// reference: std::normal_distribution<float>(0, std) on mt19937).  Filter
+// weights: the reference's float recurrence (171-176).  The reference
+// multiplies the 2n-point spectra of the zero-padded white and weight rows
+// in bins [0, n), halves bins 0 and n-1, drops bins [n, 2n), and keeps
+// Re(inverse)[m] / n.  With C = H W the 2n-point spectrum of the linear
+// convolution c = h * w, that is c[m] - (C_n (-1)^m + Re(C_{n-1}
+// e^{i pi (n-1) m / n})) / 2n for n >= 2 (bins 0 and n-1 distinct) and C_0 / 4
+// for n = 1 (the one bin halved twice).  c comes from a power-of-two FFT
+// convolution, the two bins from direct sums, all in FP64.
+inline void alpha_fill(const cmtj_alpha_noise_t &sp, uint32_t n, const float *white, float *out) {
+  std::vector<float> w(n), h(n);
+  for (uint32_t m = 0; m < n; ++m) {
+    if (white) {
+      w[m] = white[m];
+    } else {
+      double g[3];
+      gaussian3_tag(0xA1F4u, sp.seed_lo, sp.seed_hi, sp.counter + m, g);
+      const int c = sp.component < 0 ? 0 : (sp.component > 2 ? 2 : sp.component);
+      w[m] = (float)(sp.std * g[c]);
+    }
+  }
+  float v = (sp.alpha >= 0.0 && sp.alpha <= 2.0) ? 1.0f : NAN;
+  h[0] = v;
+  for (uint32_t i = 1; i < n; ++i) {
+    const float weight = (float)(0.5 * sp.alpha + (double)(float)(i - 1)) / (float)i;
+    v = v * weight;
+    h[i] = v;
+  }
+  size_t M = 2;
+  while (M < 2 * (size_t)n - 1) M <<= 1;
+  std::vector<std::complex<double>> A(M), B(M);
+  for (uint32_t m = 0; m < n; ++m) {
+    A[m] = w[m];
+    B[m] = h[m];
+  }
+  fft_pow2(A, -1);
+  fft_pow2(B, -1);
+  for (size_t k = 0; k < M; ++k) A[k] *= B[k];
+  fft_pow2(A, +1);
+  if (n == 1) {
+    out[0] = (float)(0.25 * A[0].real() / (double)M);
+    return;
+  }
+  // the 2n-point bins n and n-1 of h and w
+  double hN = 0, wN = 0;
+  std::complex<double> h1(0, 0), w1(0, 0);
+  for (uint32_t j = 0; j < n; ++j) {
+    const double sg = (j & 1u) ? -1.0 : 1.0;
+    hN += h[j] * sg;
+    wN += w[j] * sg;
+    const uint64_t q = ((uint64_t)j * (uint64_t)(n - 1)) % (2ull * n);
+    const std::complex<double> e(std::cos(M_PI * (double)q / (double)n), -std::sin(M_PI * (double)q / (double)n));
+    h1 += (double)h[j] * e;
+    w1 += (double)w[j] * e;
+  }
+  const double cN = hN * wN;
+  const std::complex<double> c1 = h1 * w1;
+  for (uint32_t m = 0; m < n; ++m) {
+    const uint64_t q = ((uint64_t)m * (uint64_t)(n - 1)) % (2ull * n);
+    const std::complex<double> e(std::cos(M_PI * (double)q / (double)n), std::sin(M_PI * (double)q / (double)n));
+    const double corr = (cN * ((m & 1u) ? -1.0 : 1.0) + (c1 * e).real()) / (2.0 * (double)n);
+    out[m] = (float)(A[m].real() / (double)M - corr);
+  }
 }
 
 // ---------------------------------------------------------------- physics
@@ -306,16 +405,35 @@ template <typename T> V3<T> stoch_torque(const cmtj_layer_t &L, const cmtj_const
   return (th + th2 * T(L.damping)) * convTerm;
 }
 
-// getStochasticLangevinVector (junction.hpp:1111-1128).
+// getOneFVector (junction.hpp:1130-1136) through VectorAlphaNoise::
+// tickVector (noise.hpp:280-290): the float samples of iteration `step`
+// (all three normalised for Axis::all, else the one axis) times the scale.
+template <typename T> V3<T> alpha_sample(const cmtj_layer_t &L, uint64_t step) {
+  if (!L.alpha_buf || step >= L.alpha_len) return V3<T>();
+  const float *b = L.alpha_buf + step;
+  const size_t n = L.alpha_len;
+  const int ax = L.alpha_axis;
+  V3<T> v((ax == 0 || ax == 3) ? (double)b[0] : 0.0, (ax == 1 || ax == 3) ? (double)b[n] : 0.0,
+          (ax == 2 || ax == 3) ? (double)b[2 * n] : 0.0);
+  if (ax == 3) v = normalized(v);
+  return v * T(L.alpha_scale);
+}
+
+// getStochasticLangevinVector (junction.hpp:1111-1128) plus getOneFVector:
+// the dW of the Euler-Heun and Heun runners (1726-1727, 1792-1793).
 template <typename T> V3<T> langevin(const cmtj_layer_t &L, const cmtj_constants_t &c, const T &time,
                                      uint64_t step, const Tables<T> &tb) {
-  if (!L.temperatureSet) return V3<T>();
-  const T temp = driver_value<T>(L.drv[CMTJ_SLOT_TEMPERATURE], time, tb);
-  const T mainFactor = (2 * T(L.damping) * T(c.kB) * temp) / (T(L.Ms) * T(L.cellVolume) * T(c.gyro));
-  const T sigma = sqrt(mainFactor);
-  double g[3];
-  gaussian3(L.seed_lo, L.seed_hi, L.noise_step + step, g);
-  return V3<T>(g[0], g[1], g[2]) * sigma;
+  V3<T> dW;
+  if (L.temperatureSet) {
+    const T temp = driver_value<T>(L.drv[CMTJ_SLOT_TEMPERATURE], time, tb);
+    const T mainFactor = (2 * T(L.damping) * T(c.kB) * temp) / (T(L.Ms) * T(L.cellVolume) * T(c.gyro));
+    const T sigma = sqrt(mainFactor);
+    double g[3];
+    gaussian3(L.seed_lo, L.seed_hi, L.noise_step + step, g);
+    dW = V3<T>(g[0], g[1], g[2]) * sigma;
+  }
+  if (L.alpha_buf) dW = dW + alpha_sample<T>(L, step);
+  return dW;
 }
 
 // --------------------------------------------------------------- junction
@@ -788,6 +906,26 @@ int oracle_count_flops(const cmtj_junction_t *junction, cmtj_layer_t *layers, co
 // Three Gaussian draws of the thermal stream, exposed for the noise tests.
 void oracle_gaussian3(uint32_t seed_lo, uint32_t seed_hi, uint64_t step, double *g) {
   oracle::gaussian3(seed_lo, seed_hi, step, g);
+}
+
+// BufferedAlphaNoise::fillBuffer for n_buffers rows of n samples (the
+// restatement of cmtj_alpha_noise_f32): out[r*n ..] from specs[r], white
+// draws from white[r*n ..] when white is not null.  Rows run on n_threads
+// host threads.
+int oracle_alpha_noise(const cmtj_alpha_noise_t *specs, int32_t n_buffers, uint32_t n, const float *white,
+                       float *out, int32_t n_threads) {
+  if (n_buffers < 0 || n == 0 || !specs || !out) return CMTJ_ERR_ARG;
+  std::atomic<int> next(0);
+  auto work = [&]() {
+    for (int r = next++; r < n_buffers; r = next++)
+      oracle::alpha_fill(specs[r], n, white ? white + (size_t)r * n : nullptr, out + (size_t)r * n);
+  };
+  const int t = std::max(1, std::min<int>(n_threads, n_buffers));
+  std::vector<std::thread> pool;
+  for (int k = 1; k < t; ++k) pool.emplace_back(work);
+  work();
+  for (auto &th : pool) th.join();
+  return CMTJ_OK;
 }
 
 }  // extern "C"

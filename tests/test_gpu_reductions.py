@@ -28,7 +28,7 @@ DT = 1e-13
 # trajectories the FP32 bound applies to) and whose mixing covariance
 # <I R> - <I><R> is well above the tolerance (checked below).
 VSD_ROWS = [82121, 119468, 1678, 95069,        # 1 layer, classic R
-            109839, 124315, 89931, 105362,     # 2 layers, classic R
+            109839, 124315, 91883, 105362,     # 2 layers, classic R
             40864, 92767, 19241, 10835,        # 3 layers, series Rx
             100206, 100563, 81789, 121478]     # 4 layers, series Rx
 
@@ -64,12 +64,21 @@ def _vsd_fp64(spec, n_steps):
         return list(ex.map(one, range(spec.n)))
 
 
-def _vsd_tolerance(scale, r_mean):
-    """Error bound of an FP32 <I(t) x(t)> against FP64: the trajectory
-    (max|dm| <= 1e-5 on these rows moves R by at most 2 |dm| per unit of MR
-    scale) plus the FP32 sine of the drive phase, whose error multiplies the
-    whole of R."""
-    return 2e-5 * scale + 2e-7 * r_mean
+def _vsd_tolerance(scale, r_mean, r_coef=1e-8):
+    """Tolerance of an FP32 <I(t) R(t)> against FP64: 2e-6 of the MR scale
+    (the trajectory's error, averaged against the oscillating drive) plus
+    r_coef of the mean R (the FP32 sine of the drive phase and the FP32
+    filter weights multiply the whole of R).  Measured on these rows: at
+    most 2.3e-8 of the scale and 4e-9 of R for the plain mean, 7e-8 of R
+    for the filtered one."""
+    return 2e-6 * scale + r_coef * r_mean
+
+
+def _mean_r_tolerance(scale, r_mean):
+    """Error bound of the FP32 time-averaged R: the FP32 trajectory bound
+    max|dm| <= 1e-4 (reached in the transient from the literal start) moves
+    R by at most 2e-4 per unit of MR scale, plus FP32 rounding of R."""
+    return 2e-4 * scale + 2e-7 * r_mean
 
 
 @pytest.mark.gpu
@@ -95,17 +104,18 @@ def test_vsd_mixing_voltage_matches_fp64(gpu_lib):
         cov64, cov32 = v64 - i64 * r64, v32[k] - i64 * r32[k]
         dm = float(np.max(np.abs(st["m"][k, :L].astype(np.float64) - m64)))
         tol = _vsd_tolerance(scale, abs(r64))
-        report.append((VSD_ROWS[k], L, dm, v64, v32[k] - v64, r32[k] - r64, cov64, cov32 - cov64, tol))
-    print("\nrow L max|dm| v64 dv dR cov64 dcov tol")
+        tol_r = _mean_r_tolerance(scale, abs(r64))
+        report.append((VSD_ROWS[k], L, dm, v64, v32[k] - v64, r32[k] - r64, tol_r, cov64, cov32 - cov64, tol))
+    print("\nrow L max|dm| v64 dv dR tolR cov64 dcov tol")
     for r in report:
-        print("%d %d %.2e %.5g %.2e %.2e %.4e %.2e %.2e" % r)
-    for row, L, dm, v64, dv, dr, cov64, dcov, tol in report:
+        print("%d %d %.2e %.5g %.2e %.2e %.2e %.4e %.2e %.2e" % r)
+    for row, L, dm, v64, dv, dr, tol_r, cov64, dcov, tol in report:
         assert dm <= 1e-4, (row, dm)
         assert abs(cov64) > 10 * tol, (row, cov64, tol)
         assert abs(dv) <= tol, (row, L, dv, tol)
-        assert abs(dr) <= tol, (row, L, dr, tol)
+        assert abs(dr) <= tol_r, (row, L, dr, tol_r)
         assert abs(dcov) <= tol, (row, L, dcov, tol)
-        assert abs(dcov) <= 0.1 * abs(cov64), (row, L, dcov, cov64)
+        assert abs(dcov) <= 0.01 * abs(cov64), (row, L, dcov, cov64)
 
 
 def compute_sd_f64(R, I, dt):
@@ -135,7 +145,7 @@ def test_vsd_filtered_voltage_matches_compute_sd(gpu_lib):
     worst = []
     for k, (R, I, scale, _) in enumerate(ref):
         v64 = compute_sd_f64(R, I, DT)
-        tol = _vsd_tolerance(scale, float(np.mean(np.abs(R))))
+        tol = _vsd_tolerance(scale, float(np.mean(np.abs(R))), r_coef=1e-7)
         print("%d %d %.5g %.2e %.2e" % (VSD_ROWS[k], int(spec.n_layers[k]), v64, v32[k] - v64, tol))
         worst.append((abs(v32[k] - v64) / tol, VSD_ROWS[k], v64, v32[k]))
     assert max(worst)[0] <= 1.0, max(worst)
@@ -176,11 +186,13 @@ def test_pimm_spectrum_matches_numpy_and_fp64(gpu_lib):
         x64 = w[0] * lg["L0_mx"] + w[1] * lg["L1_mx"]
         fft64 = np.abs(np.fft.fft(x64[-nfft:]))[1:nfft // 2]
         # end to end (FP32 trajectory, log and FFT against the FP64
-        # trajectory's spectrum): within 1e-4 of the ringing's spectral peak
+        # trajectory's spectrum), relative to the ringing's spectral peak;
+        # at the field grid's ends m is saturated along the pulse and does
+        # not ring (peak 0): there only the FFT rounding remains
         peak = float(np.max(fft64))
         err = float(np.max(np.abs(gpu[k] - fft64)))
-        print("row %d: max|d spectrum| / peak = %.2e" % (k, err / peak))
-        assert err <= 1e-2 * peak, (k, err, peak)
+        print("row %d: peak %.3e  max|d spectrum| %.2e  fft_tol %.2e" % (k, peak, err, fft_tol))
+        assert err <= 1e-3 * peak + fft_tol, (k, err, peak, fft_tol)
 
 
 @pytest.mark.gpu
