@@ -267,6 +267,14 @@ def pimm_procedure_case(cm):
     return js, kw
 
 
+def rh_logs(junctions):
+    """m of both layers [n, rows, 6] and R [n, rows] from the R(H) logs."""
+    lg = [j.getLogArrays() for j in junctions]
+    m = np.stack([np.stack([g[k] for k in ("free_mx", "free_my", "free_mz", "ref_mx", "ref_my", "ref_mz")], 1)
+                  for g in lg])
+    return m, np.stack([g["R_free_ref"] for g in lg])
+
+
 def final_m(junctions):
     return np.array([[(l.mag.x, l.mag.y, l.mag.z) for l in j.layers] for j in junctions])
 
@@ -301,7 +309,8 @@ def cpu_baseline(budget_s=15.0):
     oracle_harness.run_oracle(js, 1e-8, DT, DT, threads=cores)
     rh_el = time.perf_counter() - t0
     rh = {"seconds": rh_el, "cores": cores, "layer_steps_per_s": 64 * 100_000 * 2 / rh_el,
-          "mean_R_last_2ns": [float(np.mean(j.getLogArrays()["R_free_ref"][-20_000:])) for j in js]}
+          "mean_R_last_2ns": [float(np.mean(j.getLogArrays()["R_free_ref"][-20_000:])) for j in js],
+          "logs": rh_logs(js)}
     # Dormand-Prince and a dipole-coupled group, the same runs as the GPU legs
     ocm = oracle_harness.oracle_module()
     js = dp_junctions(ocm)
@@ -629,15 +638,22 @@ def measure_rest(run, low, spec, n_steps, kern_ms, fft_ms, lib):
                          "sample": "2 solo launches x 2000 steps; one launch of %d junctions x %d steps"
                                    % (len(rows), n_steps)}
     out["accuracy"] = {"max_abs_dm_final_vs_fp64": dm_final, "max_abs_dmix_logged_vs_fp64": dmix,
-                       "tolerance": 1e-4, "sample_junctions": 256, "pass": max(dm_final, dmix) <= 1e-4}
+                       "tolerance": 1e-4, "sample_junctions": 256, "pass": max(dm_final, dmix) <= 1e-4,
+                       "start": "relaxed equilibrium (the timed workload)",
+                       "literal_start": literal_start_accuracy(rows, n_steps)}
     out["serving"] = serving_leg(fp64_batch)
     out["other_workloads"] = other_workloads()
     out["cpu_baseline"] = cpu_baseline()
     rh_cpu = out["cpu_baseline"].pop("rh_config0")
     rh_gpu = out["other_workloads"]["rh_config0_fp64"]
-    rh_gpu["cpu_oracle"] = {k: v for k, v in rh_cpu.items() if k != "mean_R_last_2ns"}
     rh_gpu["max_abs_dR_mean_vs_cpu_ohm"] = float(np.max(np.abs(np.array(rh_gpu.pop("mean_R_last_2ns")) -
                                                                np.array(rh_cpu["mean_R_last_2ns"]))))
+    (m64, r64), (mo, ro) = rh_gpu.pop("logs"), rh_cpu.pop("logs")
+    rh_gpu["vs_oracle_full_logs"] = {
+        "max_abs_dm": float(np.max(np.abs(m64 - mo))), "max_rel_dR": float(np.max(np.abs(r64 - ro) / np.abs(ro))),
+        "rows": int(m64.shape[0] * m64.shape[1]), "tolerance": "max|dm| <= 1e-9, R relative <= 1e-9",
+        "pass": bool(np.max(np.abs(m64 - mo)) <= 1e-9 and np.max(np.abs(r64 - ro) / np.abs(ro)) <= 1e-9)}
+    rh_gpu["cpu_oracle"] = {k: v for k, v in rh_cpu.items() if k != "mean_R_last_2ns"}
     for key, leg in (("dp", "dormand_prince_fmr_4096"), ("group", "groups_dipole_64x16")):
         cpu = out["cpu_baseline"].pop(key)
         gpu = out["other_workloads"][leg]
@@ -654,6 +670,161 @@ def measure_rest(run, low, spec, n_steps, kern_ms, fft_ms, lib):
     out["roofline"]["reference_flop_breakdown_add_mul_div_sqrt_trans"] = out["cpu_baseline"].pop(
         "reference_flop_breakdown")
     return out
+
+
+def literal_start_accuracy(rows, n_steps):
+    """The PIMM workload's sample rows from the literal start of the R(H)
+    MTJ (m along +z, no relaxation) instead of the relaxed equilibrium:
+    the FP32 batched form against the FP64 plain form, and the FP64 plain
+    form against itself with m0 nudged by 1e-7 along x (its conditioning:
+    how far a 1e-7 change of the start moves FP64 itself)."""
+    import cmtj_gb300 as cm
+    from cmtj_gb300 import batch, engine, sweeps
+    spec, _ = sweeps.pimm_config(n_h=N_H, n_draw=N_DRAW, seed=1, dt=DT, total=TOTAL)
+    sub = spec.take(rows)
+    run = batch.BatchRun(batch.lower(sub, DT, n_steps), DT, batch.SolverMode.RK4, batch.LOG_MIX, LOG_EVERY,
+                         log_axis=0)
+    run.launch()
+    m32 = run.state()["m"][:, :2, :].astype(np.float64)
+    plan = engine.plan_run(n_steps * DT, DT, DT * LOG_EVERY)
+    js = spec_to_junctions_rows(spec, rows)
+    engine.run_junctions(js, plan, cm.SolverMode.RK4)
+    m64 = final_m(js)
+    nudged = spec_to_junctions_rows(spec, rows)
+    for j in nudged:
+        for layer in j.layers:
+            layer.mag = cm.CVector(layer.mag.x + 1e-7, layer.mag.y, layer.mag.z)
+    engine.run_junctions(nudged, plan, cm.SolverMode.RK4)
+    d32 = np.max(np.abs(m32 - m64), axis=(1, 2))
+    cond = np.max(np.abs(final_m(nudged) - m64), axis=(1, 2))
+    well = cond <= 3e-5
+    return {"sample_junctions": len(rows), "max_abs_dm_final_fp32_vs_fp64": float(np.max(d32)),
+            "median_abs_dm_final_fp32_vs_fp64": float(np.median(d32)),
+            "fp64_nudge_1e-7_max_abs_dm": float(np.max(cond)),
+            "fp64_nudge_1e-7_median_abs_dm": float(np.median(cond)),
+            "well_conditioned_junctions": int(np.sum(well)),
+            "max_abs_dm_fp32_vs_fp64_well_conditioned": float(np.max(d32[well])) if np.any(well) else None,
+            "junctions_within_1e-4": int(np.sum(d32 <= 1e-4)),
+            "note": "well conditioned: FP64 moves <= 3e-5 under the 1e-7 nudge"}
+
+
+def fp64_rows_at(js, ends, every, solver):
+    """The FP64 plain form on `js` for the longest of `ends` iterations,
+    logged every `every` steps; for each junction the log row of the state
+    after every * floor((end - 1) / every) + 1 steps (gathered on the
+    device).  Returns (rows [n, width], status)."""
+    import torch
+    from cmtj_gb300 import _abi, engine
+    lib = engine.require_gpu()
+    plan = engine.plan_run(int(max(ends)) * DT, DT, every * DT)
+    low = engine.lower(js, plan, solver, False)
+    n, p = len(js), low.params
+    d_j = engine.to_device(low.junctions)
+    d_l, alpha = engine.device_layers(low)
+    d_tab = engine.to_device(low.tables) if low.tables is not None else None
+    d_log = torch.empty((n, int(p["n_log"][0]), low.log_width), dtype=torch.float64, device="cuda")
+    d_status = torch.zeros(2 * n, dtype=torch.int32, device="cuda")
+    _abi.check(lib.cmtj_run_simulation_f64(engine.ptr(d_j), n, engine.ptr(d_l), engine.ptr(d_tab), p.ctypes.data,
+                                           engine.ptr(d_log), engine.ptr(d_status), engine.stream_ptr()), lib)
+    idx = torch.from_numpy((np.asarray(ends, dtype=np.int64) - 1) // every).cuda()
+    out = d_log[torch.arange(n, device="cuda"), idx].cpu().numpy()
+    del alpha
+    return out, d_status.cpu().numpy().view(np.uint32)
+
+
+def pbit_accuracy(spec, n_steps, jd, mz32):
+    """The p-bit sweep's P(switch) against the reference's counts
+    (tests/golden/pbit_sweep.npz: 17 of the 64 currents, 2048 runs each,
+    3-sigma binomial bound), and 4 seeded junctions per current (256) on the
+    FP64 plain form under the same Philox noise words: how often the two
+    forms end on the same side."""
+    import cmtj_gb300 as cm
+    import thermal_cases
+    g = np.load(os.path.join(ROOT, "tests", "golden", "pbit_sweep.npz"))
+    cur, sw, runs = g["currents"], g["switched"], g["runs"]
+    rows = []
+    for q, c in enumerate(cur):
+        sel = jd == c
+        n = int(sel.sum())
+        k = int(np.sum(mz32[sel] < 0))
+        p1, p2 = k / n, sw[q] / runs[q]
+        p = (k + sw[q]) / (n + runs[q])
+        bound = 3 * np.sqrt(max(p * (1 - p), 1.0 / (n + runs[q])) * (1.0 / n + 1.0 / runs[q]))
+        rows.append((float(c), p1, float(p2), abs(p1 - p2), float(bound)))
+    within = sum(1 for r in rows if r[3] <= r[4])
+    # FP64 sample under the same noise
+    pick = np.concatenate([np.nonzero(jd == c)[0][:4] for c in np.unique(jd)])
+    js = []
+    for k in pick:
+        j, _ = thermal_cases.pbit_sweep_junction(cm, float(jd[k]), n_steps[k] * DT)
+        j.layers[0].noise_seed = int(spec.seed[k, 0])
+        js.append(j)
+    r64, st64 = fp64_rows_at(js, n_steps[pick], 100, cm.SolverMode.EulerHeun)
+    same = np.mean((r64[:, 2] < 0) == (mz32[pick] < 0))
+    return {"vs_reference": {"currents": len(rows), "within_3sigma": within,
+                             "max_abs_dP": float(max(r[3] for r in rows)),
+                             "per_current": [[round(r[0], 1), round(r[1], 4), round(r[2], 4), round(r[4], 4)]
+                                             for r in rows],
+                             "columns": "current A/m^2, P fp32 (16,384 runs), P reference (2048 runs), 3-sigma"},
+            "vs_fp64_same_noise": {"sample_junctions": int(len(pick)), "same_final_side": float(same),
+                                   "fp64_ok": bool(np.all(st64[0::2] == 0)),
+                                   "note": "FP64 read at the last 10 ps log row at or before each run's end"}}
+
+
+def vsd_accuracy(spec, n_steps, st, n_sample=64, seed=5):
+    """A seeded sample of the spin-diode sweep on the oracle (FP64, every
+    step logged, each row its own duration, all host cores): the on-device
+    <I R>, time-averaged R, mixing covariance <I R> - <I><R> and the
+    Butterworth-filtered voltage (compute_sd) against the same quantities of
+    the FP64 trajectory."""
+    from concurrent.futures import ThreadPoolExecutor
+    import cmtj_gb300 as cm
+    import oracle_harness
+    from cases import junctions_from_spec
+    from scipy.signal import butter, lfilter
+    rows = np.sort(np.random.default_rng(seed).choice(spec.n, n_sample, replace=False))
+    sub = spec.take(rows)
+    oracle_harness.oracle_lib()
+    b, a = butter(3, 10e6 / (0.5 / DT), btype="low", analog=False)
+
+    def one(q):
+        j = junctions_from_spec(sub, [q], lambda k: cm.AxialDriver(
+            cm.NullDriver(), cm.sineDriver(0, 500.0, float(sub.vsd_freq[k]), 0), cm.NullDriver()))[0]
+        ns = int(n_steps[rows[q]])
+        oracle_harness.run_oracle([j], ns * DT, DT, DT)
+        lg = j.getLogArrays()
+        L = int(sub.n_layers[q])
+        if sub.mr_mode[q] == 1:
+            R = lg["R"] if L == 1 else lg["R_L0_L1"]
+            scale = sub.Rap[q] - sub.Rp[q]
+        else:
+            R = sum(sub.strip[q, 0, l] + sub.strip[q, 2, l] * lg["L%d_mx" % l] ** 2 +
+                    sub.strip[q, 4, l] * lg["L%d_my" % l] ** 2 for l in range(L))
+            scale = sum(abs(sub.strip[q, 2, l]) + abs(sub.strip[q, 4, l]) for l in range(L))
+        I = np.sin(2 * np.pi * sub.vsd_freq[q] * lg["time"])
+        return (float(np.mean(I * R)), float(np.mean(R)), float(np.mean(I)),
+                float(np.mean(lfilter(b, a, -I * R))), float(scale))
+
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(os.cpu_count() or 1) as ex:
+        ref = list(ex.map(one, range(len(rows))))
+    el = time.perf_counter() - t0
+    ns = n_steps[rows].astype(np.float64)
+    v32 = (st["v_sum"][rows].astype(np.float64) + st["v_c"][rows]) / ns
+    r32 = (st["r_sum"][rows].astype(np.float64) + st["r_c"][rows]) / ns
+    sd32 = -(st["vw_sum"][rows].astype(np.float64) + st["vw_c"][rows]) / ns
+    v64, r64, i64, sd64, scale = (np.array(x) for x in zip(*ref))
+    cov64, cov32 = v64 - i64 * r64, v32 - i64 * r32
+    return {"sample_junctions": len(rows), "oracle_seconds": el,
+            "max_abs_dV_over_mr_scale": float(np.max(np.abs(v32 - v64) / scale)),
+            "max_abs_dR_mean_over_mr_scale": float(np.max(np.abs(r32 - r64) / scale)),
+            "max_abs_dcov_over_mr_scale": float(np.max(np.abs(cov32 - cov64) / scale)),
+            "median_rel_dcov": float(np.median(np.abs(cov32 - cov64) / np.maximum(np.abs(cov64), 1e-30))),
+            "max_abs_dV_filtered_over_mr_scale": float(np.max(np.abs(sd32 - sd64) / scale)),
+            "max_abs_dV_ohm": float(np.max(np.abs(v32 - v64))),
+            "median_abs_cov64_ohm": float(np.median(np.abs(cov64))),
+            "note": "V = <I R> per unit drive current; MR scale = Rap - Rp (classic) or sum |AMR_X| + |SMR_X| "
+                    "(series Rx)"}
 
 
 def _timed_run(run):
@@ -693,7 +864,8 @@ def other_workloads():
     norm = np.linalg.norm(st["m"][:, 0, :].astype(np.float64), axis=1)
     out["pbit_1M"] = {"layer_steps_per_s": float(n_steps.sum()) / el, "seconds": el, "junctions": spec.n,
                       "layer_steps": float(n_steps.sum()), "all_ok": bool(np.all(st["status"] == 0)),
-                      "p_switch_first_last": [p_sw[0], p_sw[-1]], "max_norm_drift": float(np.max(np.abs(norm - 1)))}
+                      "p_switch_first_last": [p_sw[0], p_sw[-1]], "max_norm_drift": float(np.max(np.abs(norm - 1))),
+                      "accuracy": pbit_accuracy(spec, n_steps, jd, mz)}
     del run, low, spec
     torch.cuda.empty_cache()
     # uneven spin-diode sweep with both voltage forms
@@ -707,7 +879,8 @@ def other_workloads():
     out["vsd_uneven_131k"] = {"layer_steps_per_s": ls / el, "seconds": el, "junctions": spec.n, "layer_steps": ls,
                               "all_ok": bool(np.all(st["status"] == 0)),
                               "variants": [[int(a), int(b), int(c)] for a, b, c in run.variants()],
-                              "reductions": "plain and Butterworth-weighted <I R>, every step"}
+                              "reductions": "plain and Butterworth-weighted <I R>, every step",
+                              "accuracy": vsd_accuracy(spec, n_steps, st)}
     del run, low, spec
     torch.cuda.empty_cache()
     # R(H) sweep of the 2-layer MTJ: 64 fields over +-800 kA/m along x, 1 ns
@@ -752,6 +925,7 @@ def other_workloads():
                               "layer_steps_per_s_kernel": k["layer_steps_per_s"], "all_ok": k["all_ok"],
                               "mean_R_last_2ns": [float(np.mean(j.getLogArrays()["R_free_ref"][-20_000:]))
                                                   for j in js],
+                              "logs": rh_logs(js),
                               "sample": "64 fields x 100,000 RK4 steps, log every step"}
     del js
     # Dormand-Prince: 4096 sine-driven free layers, 5 ns, adaptive steps
@@ -791,6 +965,40 @@ def other_workloads():
         leg["seconds_" + prec] = time.perf_counter() - t0
         leg["spectra_" + prec] = np.stack([r[0] for r in res])
     out["pimm_procedure_64x10"] = leg
+    # buffered 1/f^alpha noise: the generator alone (3072 buffers of
+    # 100,000 samples: one 10 ns run of 1024 noisy layers), and 1024 p-bit
+    # layers with thermal noise and alpha noise, 10 ns Euler-Heun on the
+    # FP64 plain form through Junction.runSimulation's path
+    from cmtj_gb300 import noise
+    import thermal_cases
+    specs = noise.specs_array([(1.0, 1.0, 77 + r // 3, 0, r % 3) for r in range(3072)])
+    noise.device_buffers(specs[:3], 100_000)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    bufs = noise.device_buffers(specs, 100_000)
+    b.record()
+    torch.cuda.synchronize()
+    gen_s = a.elapsed_time(b) / 1e3
+    del bufs
+    js = []
+    for k in range(1024):
+        j, _ = thermal_cases.pbit_sweep_junction(cm, 1e11, 1e-8)
+        j.layers[0].setAlphaNoise(1.0, 1.0, 0.05, cm.Axis.all)
+        j.layers[0].noise_seed = 5000 + k
+        js.append(j)
+    plan = engine.plan_run(1e-8, DT, 1e-9)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    engine.run_junctions(js, plan, cm.SolverMode.EulerHeun)
+    torch.cuda.synchronize()
+    el = time.perf_counter() - t0
+    out["alpha_noise_fp64_1024"] = {
+        "generator_s_3072x100k": gen_s, "generator_samples_per_s": 3072 * 100_000 / gen_s,
+        "run_seconds": el, "layer_steps_per_s": 1024 * plan.total_iterations / el,
+        "sample": "1024 p-bit layers (alpha 1, scale 0.05, axis all, plus 300 K), 10 ns Euler-Heun, FP64 plain "
+                  "form, buffers generated on the device per run"}
+    del js
     # 16-junction series stack, FP64 plain form
     js = [cases._stt_junction(cm, 1.0 + 0.02 * k, 1e3 + 50 * k, (0.1, 0.2, 1), (1, 0, 0)) for k in range(16)]
     s = cm.stack.SeriesStack(js)

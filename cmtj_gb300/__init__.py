@@ -27,7 +27,7 @@ __all__ = [
     "AdaptiveIntegrationParams", "AxialDriver", "Axis", "CVector", "Junction", "Layer", "NullDriver", "Reference",
     "ScalarDriver", "SolverMode", "UpdateType", "c_dot", "constantDriver", "gaussianImpulseDriver",
     "gaussianStepDriver", "posSineDriver", "pulseDriver", "sineDriver", "stepDriver", "trapezoidDriver",
-    "constants", "stack", "reservoir",
+    "constants", "stack", "reservoir", "noise",
     "xaxis", "yaxis", "zaxis", "all", "none", "fixed", "top", "bottom", "RK4", "Heun", "EulerHeun",
     "DormandPrince", "constant", "pulse", "sine", "step", "posine", "halfsine", "trapezoid", "gaussimpulse",
     "gaussstep", "custom",
@@ -36,8 +36,8 @@ __all__ = [
 
 def __getattr__(name):
     # submodules bound as attributes of the reference's module (cmtj.stack,
-    # cmtj.reservoir), imported on first use
-    if name in ("stack", "reservoir"):
+    # cmtj.reservoir, cmtj.noise), imported on first use
+    if name in ("stack", "reservoir", "noise"):
         import importlib
         return importlib.import_module(__name__ + "." + name)
     raise AttributeError(name)

@@ -1,6 +1,7 @@
 """The simulation-running tests of the reference suite (tests/test_basic.py,
 test_solvers.py, test_procedures.py and the fixtures of its conftest.py),
-written against the `cmtj` API and run on the GPU solver unchanged in
+imported as the reference's users import it (`import cmtj`, the alias
+package of cmtj_gb300) and run on the GPU solver unchanged in
 substance: the same junctions, solvers, calls and assertions.  The
 procedure sweeps are shortened (5 field points, 1 ns) so the file runs in
 seconds; the full-size numerical parity is pinned elsewhere."""
@@ -9,11 +10,11 @@ from math import pi
 import numpy as np
 import pytest
 
-import cmtj_gb300 as cmtj
-from cmtj_gb300 import AxialDriver, CVector, Junction, Layer, ScalarDriver, SolverMode
-from cmtj_gb300.utils import FieldScan
-from cmtj_gb300.utils.procedures import PIMM_procedure, ResistanceParameters, VSD_procedure
-from cmtj_gb300.utils.resistance import calculate_resistance_parallel, calculate_resistance_series
+import cmtj
+from cmtj import AxialDriver, CVector, Junction, Layer, ScalarDriver, SolverMode
+from cmtj.utils import FieldScan
+from cmtj.utils.procedures import PIMM_procedure, ResistanceParameters, VSD_procedure
+from cmtj.utils.resistance import calculate_resistance_parallel, calculate_resistance_series
 
 rp = ResistanceParameters(Rxx0=100, Rxy0=1, Rsmr=-0.46, Rahe=-2.7, Ramr=-0.24, l=30, w=20)
 demag = [CVector(0, 0, 0), CVector(0, 0, 0), CVector(0, 0, 1)]
