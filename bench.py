@@ -641,7 +641,7 @@ def measure_rest(run, low, spec, n_steps, kern_ms, fft_ms, lib):
                        "tolerance": 1e-4, "sample_junctions": 256, "pass": max(dm_final, dmix) <= 1e-4,
                        "start": "relaxed equilibrium (the timed workload)",
                        "literal_start": literal_start_accuracy(rows, n_steps)}
-    out["serving"] = serving_leg(fp64_batch)
+    out["serving"] = serving_leg()
     out["other_workloads"] = other_workloads()
     out["cpu_baseline"] = cpu_baseline()
     rh_cpu = out["cpu_baseline"].pop("rh_config0")
@@ -1015,41 +1015,138 @@ def other_workloads():
     return out
 
 
-def serving_leg(fp64_rate, n_requests=200, rate_hz=200.0):
-    """Serving trace: Poisson arrivals at 200 req/s of requests holding
-    64-16,384 solves (log-uniform) of three kinds -- PIMM-style 2-layer RK4,
-    thermal 1-layer p-bit Euler-Heun at 300 K, uneven 1-4-layer spin-diode
-    RK4 with on-device <I R> -- each solve 2-40 ns at dt = 1e-13, served by
-    continuous batching (cmtj_gb300.serving).  Latency = completion minus
-    arrival, wall clock."""
+def serving_leg(n_sat=200, sat_rate_hz=200.0, n_requests=1000, loads=(0.5, 0.8, 1.2)):
+    """Serving trace (cmtj_gb300.serving, continuous batching): Poisson
+    arrivals of requests holding 64-16,384 solves (log-uniform) of three
+    kinds -- PIMM-style 2-layer RK4, thermal 1-layer p-bit Euler-Heun at
+    300 K, uneven 1-4-layer spin-diode RK4 with on-device <I R> -- each
+    solve 2-40 ns at dt = 1e-13, 5 % of requests FP64 plain.
+
+    1. Capacity: 200 requests at 200 req/s (about 3x overload), shortest
+       job first and FIFO; the delivered layer-steps/s is the capacity.
+    2. Latency against load: 1000 requests at 0.5, 0.8 and 1.2 x that
+       capacity (arrival rate = load x capacity / mean request size).
+    3. FP64 plain alone, measured: 8 sampled FP32 requests of the 0.8 x run,
+       each run alone on the FP64 plain form (all its solves, one launch,
+       for 2000 steps, scaled to its longest solve), beside the same request
+       run alone on the FP32 form and its latency in the mix.
+    Latency = completion minus arrival, wall clock."""
     from cmtj_gb300 import serving
     f64_fraction = 0.05
+    out = {}
     fifo = serving.ServingEngine(hbm_budget_bytes=8 << 30, chunk_steps=4000, policy="fifo")
     t0 = time.perf_counter()
-    done_fifo = fifo.run(serving.make_trace(n_requests, rate_hz=rate_hz, seed=3, f64_fraction=f64_fraction))
+    done_fifo = fifo.run(serving.make_trace(n_sat, rate_hz=sat_rate_hz, seed=3, f64_fraction=f64_fraction))
     fifo_summary = serving.summary(done_fifo, time.perf_counter() - t0)
-    reqs = serving.make_trace(n_requests, rate_hz=rate_hz, seed=3, f64_fraction=f64_fraction)
     eng = serving.ServingEngine(hbm_budget_bytes=8 << 30, chunk_steps=4000, policy="sjf")
     t0 = time.perf_counter()
-    done = eng.run(reqs)
-    wall = time.perf_counter() - t0
-    out = serving.summary(done, wall)
-    out["policy"] = "sjf: smallest layer-steps first among arrived requests"
-    out["fifo"] = {k: fifo_summary[k] for k in ("p50_ms", "p99_ms", "layer_steps_per_s", "wall_s")}
-    lat64 = [r.latency for r in done if r.precision == "f64"]
-    if lat64:
-        out["fp64_requests"] = {"count": len(lat64), "p50_ms": float(np.percentile(lat64, 50) * 1e3),
-                                "p99_ms": float(np.percentile(lat64, 99) * 1e3),
-                                "each": "64 two-layer MTJs, 2 ns RK4 (20,000 steps), FP64 plain form"}
+    done = eng.run(serving.make_trace(n_sat, rate_hz=sat_rate_hz, seed=3, f64_fraction=f64_fraction))
+    sat = serving.summary(done, time.perf_counter() - t0)
     offered = sum(r.layer_steps for r in done)
-    out.update({"trace": "%d requests, Poisson %.0f req/s, 64-16384 solves, 2-40 ns, pimm/pbit/vsd mix, "
-                         "%.0f%% of requests FP64 plain" % (n_requests, rate_hz, 100 * f64_fraction),
-                "offered_layer_steps": offered,
-                "offered_over_span": offered / max(done[-1].arrival, 1e-9),
-                "ticks": eng.stats["ticks"], "host_s": eng.stats["host_s"],
-                "device_wait_s": eng.stats["device_wait_s"],
-                "fp64_plain_alone_estimate_s": offered / fp64_rate})
+    capacity = sat["layer_steps_per_s"]
+    out["saturated"] = dict(sat, policy="sjf: smallest layer-steps first among arrived requests",
+                            fifo={k: fifo_summary[k] for k in ("p50_ms", "p99_ms", "layer_steps_per_s", "wall_s")},
+                            offered_over_span=offered / max(done[-1].arrival, 1e-9),
+                            trace="%d requests, Poisson %.0f req/s" % (n_sat, sat_rate_hz),
+                            ticks=eng.stats["ticks"], host_s=eng.stats["host_s"])
+    probe = serving.make_trace(400, rate_hz=1.0, seed=11, f64_fraction=f64_fraction)
+    mean_ls = float(np.mean([serving._work_estimate(r) for r in probe]))
+    curve, mid = [], None
+    for q, load in enumerate(loads):
+        rate = load * capacity / mean_ls
+        reqs = serving.make_trace(n_requests, rate_hz=rate, seed=20 + q, f64_fraction=f64_fraction)
+        e = serving.ServingEngine(hbm_budget_bytes=8 << 30, chunk_steps=4000, policy="sjf")
+        t0 = time.perf_counter()
+        d = e.run(reqs)
+        wall = time.perf_counter() - t0
+        lat = np.array([r.latency for r in d]) * 1e3
+        ls = sum(r.layer_steps for r in d)
+        curve.append({"load": load, "rate_hz": rate, "requests": len(d),
+                      "offered_layer_steps_per_s": ls / max(d[-1].arrival, 1e-9),
+                      "delivered_layer_steps_per_s": ls / wall, "p50_ms": float(np.percentile(lat, 50)),
+                      "p90_ms": float(np.percentile(lat, 90)), "p99_ms": float(np.percentile(lat, 99)),
+                      "max_ms": float(np.max(lat)), "wall_s": wall})
+        if abs(load - 0.8) < 1e-9:
+            mid = d
+    out["latency_vs_load"] = {"capacity_layer_steps_per_s": capacity, "mean_request_layer_steps": mean_ls,
+                              "points": curve, "policy": "sjf"}
+    out["fp64_alone"] = fp64_alone_sample(mid if mid is not None else done)
     return out
+
+
+def request_junctions(req):
+    """Junction objects equal to the solves of an FP32 serving request."""
+    import cmtj_gb300 as cm
+    import thermal_cases
+    from cases import junctions_from_spec
+    sp = req.spec
+    if req.tag == "pimm":
+        return spec_to_junctions(sp)
+    if req.tag == "pbit":
+        out = []
+        for k in range(sp.n):
+            j, _ = thermal_cases.pbit_sweep_junction(cm, float(sp.wave_table["amp"][k, 0]), 1e-9)
+            j.layers[0].noise_seed = int(sp.seed[k, 0])
+            out.append(j)
+        return out
+    return junctions_from_spec(sp, range(sp.n), lambda k: cm.AxialDriver(
+        cm.NullDriver(), cm.sineDriver(0, float(sp.wave_table["amp"][k, 0]), float(sp.vsd_freq[k]), 0),
+        cm.NullDriver()))
+
+
+def fp64_alone_sample(done, n_sample=8, probe_steps=2000, seed=4):
+    """Eight FP32 requests of a served trace, each run alone: on the FP64
+    plain form (all its solves in one launch, logging what its result
+    needs -- R every step for the spin-diode kind, the final state
+    otherwise), timed over probe_steps and scaled to its longest solve; and
+    on the FP32 batched form through a fresh serving engine.  The smallest
+    sampled request also runs in full on the FP64 form, to check the
+    scaling."""
+    import torch
+    import cmtj_gb300 as cm
+    from cmtj_gb300 import engine, serving
+    rng = np.random.default_rng(seed)
+    f32 = [r for r in done if r.precision == "f32"]
+    pick = sorted(rng.choice(len(f32), min(n_sample, len(f32)), replace=False).tolist(),
+                  key=lambda i: f32[i].layer_steps)
+    rows = []
+    for q, i in enumerate(pick):
+        req = f32[i]
+        steps = np.broadcast_to(np.asarray(req.n_steps), (req.spec.n,))
+        mode = cm.SolverMode.EulerHeun if req.tag == "pbit" else cm.SolverMode.RK4
+        every = 1 if req.tag == "vsd" else probe_steps
+        js = request_junctions(req)
+        plan = engine.plan_run(probe_steps * DT, DT, every * DT)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        engine.run_junctions(js, plan, mode)
+        torch.cuda.synchronize()
+        t64 = (time.perf_counter() - t0) * float(steps.max()) / probe_steps
+        full = None
+        if q == 0 and req.tag != "vsd" and req.layer_steps <= 2e9:
+            js = request_junctions(req)
+            plan = engine.plan_run(float(steps.max()) * DT, DT, float(steps.max()) * DT)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            engine.run_junctions(js, plan, mode)
+            torch.cuda.synchronize()
+            full = time.perf_counter() - t0
+        alone = serving.Request(spec=req.spec, n_steps=req.n_steps, solver=req.solver, tag=req.tag,
+                                red_every=req.red_every, arrival=0.0)
+        e = serving.ServingEngine(hbm_budget_bytes=8 << 30, chunk_steps=4000, policy="sjf")
+        t0 = time.perf_counter()
+        e.run([alone])
+        t32 = time.perf_counter() - t0
+        rows.append({"kind": req.tag, "solves": int(req.spec.n), "layer_steps": float(req.layer_steps),
+                     "fp64_alone_s": t64, "fp64_alone_full_run_s": full, "fp32_alone_s": t32,
+                     "latency_in_mix_s": float(req.latency),
+                     "fp64_alone_over_latency_in_mix": t64 / float(req.latency)})
+    ratios = [r["fp64_alone_over_latency_in_mix"] for r in rows]
+    return {"requests": rows, "median_fp64_alone_over_latency_in_mix": float(np.median(ratios)),
+            "median_fp64_alone_over_fp32_alone": float(np.median([r["fp64_alone_s"] / r["fp32_alone_s"]
+                                                                  for r in rows])),
+            "method": "FP64 plain form, all solves of the request in one launch, %d steps timed and scaled to "
+                      "the longest solve (fp64_alone_full_run_s: the smallest request run in full)" % probe_steps}
 
 
 def spec_to_junctions_rows(spec, rows):

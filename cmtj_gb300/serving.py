@@ -224,8 +224,16 @@ class ServingEngine:
             pinned.append(h)
             return h.to("cuda", non_blocking=True)
 
+        alpha = None
+        larr = low.layers
+        if low.alpha_specs is not None:
+            # buffered alpha noise: this run's buffers, filled on the stream
+            from ._lower import with_alpha_buffers
+            from .noise import device_buffers
+            alpha = device_buffers(low.alpha_specs, int(larr[low.alpha_layers[0]]["alpha_len"]), stream=stream)
+            larr = with_alpha_buffers(low, alpha.data_ptr())
         with self.t.cuda.stream(stream):
-            d_j, d_l = up(low.junctions), up(low.layers)
+            d_j, d_l = up(low.junctions), up(larr)
             d_tab = up(low.tables) if low.tables is not None else None
             n = len(req.junctions)
             d_log = self.t.empty((n, max(plan.n_log, 1), low.log_width), dtype=self.t.float64, device="cuda")
@@ -242,7 +250,7 @@ class ServingEngine:
         req.n = n
         req.layer_steps = float(n * plan.total_iterations * np.mean([j.layerNo for j in req.junctions]))
         # the device and pinned buffers stay referenced until the event
-        self.active64.append((req, low, d_l, d_log, d_st, ev, plan, (d_j, d_tab, pinned)))
+        self.active64.append((req, low, d_l, d_log, d_st, ev, plan, (d_j, d_tab, pinned, alpha)))
         return True
 
     # ------------------------------------------------------------ ticks
