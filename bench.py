@@ -508,7 +508,10 @@ def main():
                                        % world) if world > 1 else "single",
                        "l2": "inputs and logs (5.2 GB) larger than L2", "all_ok": ok},
             "e2e": e2e, "clocks": clocks,
-            "gpu_launches": args.steps * 2}
+            "gpu_launches": args.steps * 2,
+            "autotune": {"enabled": os.environ.get("CMTJ_AUTOTUNE", "1") != "0",
+                         "partitions": [None if tu is None else {"key": tu[0], **tu[1]} for tu in run.tuning],
+                         "defaults": {"log_tile": 32, "bound": 5}}}
 
     if rank == 0 and not args.profile:
         extra = measure_rest(run, low, spec, n_steps, kern_ms, fft_only, lib)

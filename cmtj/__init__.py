@@ -22,7 +22,13 @@ _TARGET = _impl.__name__ + "."
 
 
 class _SubmoduleAlias(_abc.MetaPathFinder, _abc.Loader):
-    """Resolves cmtj.<sub> to the module cmtj_gb300.<sub>."""
+    """Resolves cmtj.<sub> to the module cmtj_gb300.<sub>.  The import
+    machinery stamps the alias spec on the module it loads; exec_module puts
+    the module's own spec back, so its relative imports and reloads keep
+    working under its real name."""
+
+    def __init__(self):
+        self._own_specs = {}
 
     def find_spec(self, fullname, path=None, target=None):
         if not fullname.startswith(_PREFIX):
@@ -32,10 +38,14 @@ class _SubmoduleAlias(_abc.MetaPathFinder, _abc.Loader):
         return _util.spec_from_loader(fullname, self, is_package=True)
 
     def create_module(self, spec):
-        return _importlib.import_module(_TARGET + spec.name[len(_PREFIX):])
+        module = _importlib.import_module(_TARGET + spec.name[len(_PREFIX):])
+        self._own_specs[spec.name] = module.__spec__
+        return module
 
     def exec_module(self, module):
-        pass
+        own = self._own_specs.pop(module.__spec__.name, None)
+        if own is not None:
+            module.__spec__ = own
 
 
 if not any(isinstance(f, _SubmoduleAlias) for f in _sys.meta_path):

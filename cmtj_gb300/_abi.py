@@ -119,6 +119,7 @@ PROTOTYPES = {
     "cmtj_run_simulation_f64": (ctypes.c_int, [_P, _I32, _P, _P, _P, _P, _P, _P]),
     "cmtj_batch_run_f32": (ctypes.c_int, [_P, _P, _P, _P, _I32, _I32, _I32, _P, _P, _P, _I32, _P]),
     "cmtj_batch_variant_f32": (ctypes.c_int, [_I32, _I32, _I32]),
+    "cmtj_batch_bounds_f32": (ctypes.c_int, [_I32, _I32, _I32, _P, _I32]),
     "cmtj_batch_run_f32_noalloc": (ctypes.c_int, [_P, _P, _P, _P, _I32, _I32, _I32, _P, _P, _I32, _I32, _P]),
     "cmtj_spectrum_f32": (ctypes.c_int, [_P, ctypes.c_int64, _I32, _I32, _I32, _I32, _I32, _P, _P]),
     "cmtj_run_stack_f64": (ctypes.c_int, [_P, _I32, _P, _P, _P, _P, _P, _P, _P, _P, _I32, _I32, _P, _P]),

@@ -604,11 +604,16 @@ class BatchRun:
                 raise ValueError("no FP32 kernel variant for layers=%d features=0x%x" % (nl, code))
             variant[keys == key] = v
         self.parts = []
+        self.part_rows = []
         for nl in range(1, 5):
             for v in sorted(set(variant[L == nl].tolist())):
                 idx = np.nonzero((L == nl) & (variant == v))[0]
                 idx = idx[np.argsort(-lowered.n_steps[idx], kind="stable")]
                 self.parts.append((nl, engine.to_device(idx.astype(np.int32)), int(idx.size), int(v)))
+                self.part_rows.append(idx)
+        # run-time launch choices per partition (cmtj_gb300.autotune):
+        # (key, {"bound", "tile", ...}); None: the fixed defaults
+        self.tuning = [None] * len(self.parts)
         self.params = np.zeros(1, dtype=F32_PARAMS_DTYPE)
         self.params["dt"] = self.dt
         self.params["solver"] = int(self.solver)
@@ -641,19 +646,20 @@ class BatchRun:
         logs stay 16-byte aligned.  Partitions (layer count x kernel
         variant) run concurrently, each on its own stream with its own work
         ticket, so a small partition's long junctions overlap the others
-        instead of adding their tail; `stream` waits for all of them."""
+        instead of adding their tail; `stream` waits for all of them.  Each
+        partition's log tile and resident-CTA bound come from the run-time
+        autotuner (cmtj_gb300.autotune), which times them once per kind of
+        partition; the choices change no result."""
         from . import engine
         t = engine.torch()
-        p = self.params
-        p["chunk_steps"] = 2 ** 32 - 1 if chunk_steps is None else int(chunk_steps)
-        if chunk_steps is not None and self.log_mode != LOG_NONE:
-            for nl, _, _, _ in self.parts:
-                tile = default_tile(log_channels(self.log_mode, nl))
-                if int(chunk_steps) % (self.log_every * tile):
-                    raise ValueError("chunk_steps must be a multiple of log_every * %d" % tile)
         if len(self.parts) > 80:
             raise ValueError("more than 80 partitions in one batch")
         main = stream if stream is not None else t.cuda.current_stream()
+        choices = [self._choice(q, chunk_steps, main) for q in range(len(self.parts))]
+        if chunk_steps is not None and self.log_mode != LOG_NONE:
+            for (nl, _, _, _), (tile, _) in zip(self.parts, choices):
+                if int(chunk_steps) % (self.log_every * tile):
+                    raise ValueError("chunk_steps must be a multiple of log_every * %d" % tile)
         multi = len(self.parts) > 1
         if multi and self._streams is None:
             self._streams = [t.cuda.Stream() for _ in range(min(len(self.parts), 8))]
@@ -661,24 +667,53 @@ class BatchRun:
         if multi:
             start.record(main)
         ends = []
-        for q, (nl, d_order, cnt, code) in enumerate(self.parts):
+        for q in range(len(self.parts)):
             s = self._streams[q % len(self._streams)] if multi else main
             if multi:
                 s.wait_event(start)
-            pq = p.copy()  # the library copies params at launch; one record per partition
-            pq["log_tile"] = default_tile(log_channels(self.log_mode, nl))
-            ticket = self.d_ticket[16 * q:]
-            rc = self.lib.cmtj_batch_run_f32(engine.ptr(self.d_j), engine.ptr(self.d_l), engine.ptr(self.d_s),
-                                             engine.ptr(d_order), cnt, nl, code, pq.ctypes.data,
-                                             engine.ptr(self.d_log), engine.ptr(ticket), grid_blocks,
-                                             engine.stream_ptr(s))
-            _abi.check(rc, self.lib)
+            tile, code = choices[q]
+            self._launch_part(q, chunk_steps, s, tile, code, grid_blocks)
             if multi:
                 e = t.cuda.Event()
                 e.record(s)
                 ends.append(e)
         for e in ends:
             main.wait_event(e)
+
+    def _choice(self, q, chunk_steps, stream):
+        """(log tile, variant code) of partition q: the autotuner's choice
+        (tuned now if this kind of partition is new), else the defaults."""
+        from . import autotune
+        nl, _, cnt, code = self.parts[q]
+        channels = log_channels(self.log_mode, nl)
+        tile, chosen = default_tile(channels), code
+        if not autotune.enabled() or cnt == 0:
+            return tile, chosen
+        key = autotune.f32_key(nl, self.solver, code, channels, self.d_w is not None, cnt)
+        c = autotune.lookup(key)
+        if c is None:
+            c = autotune.tune_f32_partition(self, q, stream, chunk_steps)
+            if c is None:
+                return tile, chosen
+            autotune.store(key, c)
+        if channels > 0 and (chunk_steps is None or int(chunk_steps) % (self.log_every * int(c["tile"])) == 0):
+            tile = int(c["tile"])
+        chosen = (code & 0xffffff) | (int(c["bound"]) << 24)
+        self.tuning[q] = (key, {"tile": tile, "bound": int(c["bound"])})
+        return tile, chosen
+
+    def _launch_part(self, q, chunk_steps, stream, tile, code, grid_blocks=0):
+        """One cmtj_batch_run_f32 launch of partition q on `stream`."""
+        from . import engine
+        nl, d_order, cnt, _ = self.parts[q]
+        pq = self.params.copy()  # the library copies params at launch; one record per partition
+        pq["chunk_steps"] = 2 ** 32 - 1 if chunk_steps is None else int(chunk_steps)
+        pq["log_tile"] = tile
+        ticket = self.d_ticket[16 * q:]
+        rc = self.lib.cmtj_batch_run_f32(engine.ptr(self.d_j), engine.ptr(self.d_l), engine.ptr(self.d_s),
+                                         engine.ptr(d_order), cnt, nl, code, pq.ctypes.data, engine.ptr(self.d_log),
+                                         engine.ptr(ticket), grid_blocks, engine.stream_ptr(stream))
+        _abi.check(rc, self.lib)
 
     def state(self):
         return self.d_s.cpu().numpy().view(F32_STATE_DTYPE)

@@ -18,27 +18,54 @@ int variants_for(int L, const CmtjBatchVariant **v) {
   }
 }
 
-// Smallest compiled variant whose feature set covers `features`
-// (waves beyond one need the four-wave variant).
-const CmtjBatchVariant *pick(int L, int solver, int features, int need_nw) {
+// Smallest compiled variant whose feature set covers `features` (waves
+// beyond one need the four-wave variant); of its instantiations, the one
+// with resident-CTA bound `mb` when mb > 0 and one exists, else the
+// default one.
+const CmtjBatchVariant *pick(int L, int solver, int features, int need_nw, int mb) {
   const CmtjBatchVariant *v = nullptr;
   const int n = variants_for(L, &v);
   const CmtjBatchVariant *best = nullptr;
   for (int k = 0; k < n; ++k) {
-    if (v[k].solver != solver) continue;
+    if (v[k].solver != solver || v[k].low) continue;
     if ((v[k].feat & features) != features) continue;
     if (v[k].nw < need_nw) continue;
     if (!best || __builtin_popcount(v[k].feat) < __builtin_popcount(best->feat)) best = &v[k];
   }
+  if (best && mb > 0 && best->mb != mb) {
+    for (int k = 0; k < n; ++k)
+      if (v[k].solver == best->solver && v[k].feat == best->feat && v[k].nw == best->nw && v[k].mb == mb)
+        return &v[k];
+  }
   return best;
 }
+
+inline int variant_code(const CmtjBatchVariant *v) { return v->feat | (v->nw << 16) | (v->mb << 24); }
 
 }  // namespace
 
 extern "C" int cmtj_batch_variant_f32(int32_t n_layers, int32_t solver, int32_t features) {
   const int need_nw = (features >> 16) & 0xff;
-  const CmtjBatchVariant *v = pick(n_layers, solver, features & 0xffff, need_nw > 0 ? need_nw : 0);
-  return v ? (v->feat | (v->nw << 16)) : CMTJ_ERR_ARG;
+  const CmtjBatchVariant *v =
+      pick(n_layers, solver, features & 0xffff, need_nw > 0 ? need_nw : 0, (features >> 24) & 0xf);
+  return v ? variant_code(v) : CMTJ_ERR_ARG;
+}
+
+extern "C" int cmtj_batch_bounds_f32(int32_t n_layers, int32_t solver, int32_t features, int32_t *bounds,
+                                     int32_t n) {
+  const CmtjBatchVariant *v = nullptr;
+  const int count = variants_for(n_layers, &v);
+  const CmtjBatchVariant *b = pick(n_layers, solver, features & 0xffff, (features >> 16) & 0xff, 0);
+  if (!b || !bounds || n < 1) {
+    cmtj_set_error("cmtj_batch_bounds_f32: no variant for n_layers=%d solver=%d features=0x%x", n_layers,
+                   solver, features);
+    return CMTJ_ERR_ARG;
+  }
+  int k = 0;
+  bounds[k++] = b->mb;
+  for (int q = 0; q < count && k < n; ++q)
+    if (v[q].low && v[q].solver == b->solver && v[q].feat == b->feat && v[q].nw == b->nw) bounds[k++] = v[q].mb;
+  return k;
 }
 
 extern "C" int cmtj_batch_run_f32(const cmtj_f32_junction_t *d_junctions, const cmtj_f32_layer_t *d_layers,
@@ -79,7 +106,7 @@ extern "C" int cmtj_batch_run_f32(const cmtj_f32_junction_t *d_junctions, const 
     }
   }
   const int need_nw = (features >> 16) & 0xff;
-  const CmtjBatchVariant *v = pick(n_layers, p->solver, features & 0xffff, need_nw);
+  const CmtjBatchVariant *v = pick(n_layers, p->solver, features & 0xffff, need_nw, (features >> 24) & 0xf);
   if (!v) {
     cmtj_set_error("cmtj_batch_run_f32: no kernel variant for n_layers=%d solver=%d features=0x%x", n_layers,
                    p->solver, features);

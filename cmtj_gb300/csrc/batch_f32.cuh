@@ -720,8 +720,18 @@ __host__ __device__ constexpr int min_blocks() {
                                                : (SOLVER == CMTJ_RK4 ? CMTJ_BATCH_MINB : CMTJ_BATCH_MINB_STOCH));
 }
 
-template <int L, int SOLVER, int FEAT, int NW>
-__global__ void __launch_bounds__(128, (min_blocks<L, SOLVER, FEAT>())) k_batch(Args A) {
+// The second, lower-occupancy instantiation of every specialised variant:
+// fewer resident CTAs per SM, so more registers per thread.  A batch too
+// small to fill the GPU gains from it; the run-time autotuner
+// (cmtj_gb300/autotune.py) picks between the two per partition.
+template <int L, int SOLVER, int FEAT>
+__host__ __device__ constexpr int low_min_blocks() {
+  return packed_variant<L, SOLVER, FEAT>() && L > 2 ? 1 : 2;
+}
+
+// MB > 0 overrides the variant's resident-CTA bound.
+template <int L, int SOLVER, int FEAT, int NW, int MB = 0>
+__global__ void __launch_bounds__(128, (MB > 0 ? MB : min_blocks<L, SOLVER, FEAT>())) k_batch(Args A) {
   using F = Feat<FEAT>;
   extern __shared__ __align__(16) float smem[];
   const int lane = threadIdx.x & 31;

@@ -60,6 +60,36 @@ def device_layers(lowered, stream=None):
     return to_device(with_alpha_buffers(lowered, bufs.data_ptr())), bufs
 
 
+# fixed-step batches below this many layer-steps run the library's own
+# lane pick: trial launches would cost more than they could save
+TUNE_F64_MIN_LAYER_STEPS = 2e7
+
+
+def tuned_f64_params(lowered, d_j, d_l, d_tab, stream=None):
+    """The launch parameters of a lowered FP64 batch, with the lane layout
+    (threads per junction) the run-time autotuner chose for this kind of
+    batch (cmtj_gb300.autotune; the layout changes no result)."""
+    from . import autotune
+    p = lowered.params
+    solver = int(p["solver"][0])
+    n = len(lowered.junctions)
+    work = float(n) * float(p["total_iterations"][0]) * float(lowered.junctions["n_layers"].mean() if n else 0)
+    if (not autotune.enabled() or solver == _abi.DORMAND_PRINCE or int(p["lanes_per_layer"][0]) != 0
+            or work < TUNE_F64_MIN_LAYER_STEPS):
+        return p
+    key = autotune.f64_key(int(p["max_layers"][0]), solver, n)
+    c = autotune.lookup(key)
+    if c is None:
+        t = torch()
+        c = autotune.tune_f64(lowered, d_j, d_l, d_tab, stream if stream is not None else t.cuda.current_stream())
+        if c is None:
+            return p
+        autotune.store(key, c)
+    p = p.copy()
+    p["lanes_per_layer"] = int(c["lanes"])
+    return p
+
+
 def run_lowered_f64(lowered, stream=None):
     """Run a lowered batch on the FP64 plain form; returns host arrays
     (log [n][n_log][width], status [n*2], updated layers)."""
@@ -72,6 +102,7 @@ def run_lowered_f64(lowered, stream=None):
     d_j = to_device(lowered.junctions)
     d_l, alpha = device_layers(lowered, stream)
     d_tab = to_device(lowered.tables) if lowered.tables is not None else None
+    p = tuned_f64_params(lowered, d_j, d_l, d_tab, stream)
     d_log = t.empty((n, max(n_log, 1), width), dtype=t.float64, device="cuda")
     d_status = t.zeros(2 * n, dtype=t.int32, device="cuda")
     rc = lib.cmtj_run_simulation_f64(ptr(d_j), n, ptr(d_l), ptr(d_tab), p.ctypes.data, ptr(d_log), ptr(d_status),

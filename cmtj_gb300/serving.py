@@ -26,7 +26,7 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from . import _abi, batch, engine
+from . import _abi, autotune, batch, engine
 from .core import SolverMode
 
 
@@ -304,6 +304,12 @@ class ServingEngine:
             p["log_mode"] = batch.LOG_NONE
             p["solver"] = solver
             p["red_every"] = red
+            if autotune.enabled():
+                # the resident-CTA bound the autotuner chose for this kind of
+                # partition, when it has met one (no trial launches here)
+                c = autotune.lookup(autotune.f32_key(nl, solver, v, 0, False, cnt))
+                if c is not None:
+                    v = (v & 0xffffff) | (int(c["bound"]) << 24)
             ticket = self.tickets[q * 16:]
             d_order.record_stream(s)  # kept alive for s when the groups are rebuilt
             rc = self.lib.cmtj_batch_run_f32(engine.ptr(self.pool.d_j), engine.ptr(self.pool.d_l),

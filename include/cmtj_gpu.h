@@ -494,8 +494,12 @@ typedef struct cmtj_f32_params {
 } cmtj_f32_params_t;
 
 /* Kernel variant of a batch partition: n_layers (1-4), solver, and the
- * CMTJ_FEAT_* terms its junctions use.  A variant that was not compiled
- * falls back to the generic one of the same layer count and solver. */
+ * CMTJ_FEAT_* terms its junctions use (bits 0-15 of `features`; bits 16-23:
+ * waves per junction; bits 24-27: the resident-CTA bound asked for, 0 for
+ * the variant's default).  A variant that was not compiled falls back to
+ * the generic one of the same layer count and solver.  The specialised
+ * variants are compiled at two bounds: their default and a lower one (more
+ * registers per thread), for batches too small to fill the GPU. */
 #define CMTJ_FEAT_FULL_DEMAG 1
 #define CMTJ_FEAT_DIPOLE 2
 #define CMTJ_FEAT_IDMI 4
@@ -526,8 +530,14 @@ int cmtj_batch_run_f32(const cmtj_f32_junction_t *d_junctions, const cmtj_f32_la
                        int32_t grid_blocks, void *stream);
 
 /* Feature set actually compiled for (n_layers, solver, features): the
- * variant cmtj_batch_run_f32 will run. */
+ * variant cmtj_batch_run_f32 will run, as features | waves << 16 |
+ * resident-CTA bound << 24. */
 int cmtj_batch_variant_f32(int32_t n_layers, int32_t solver, int32_t features);
+
+/* No counterpart in the reference (launch tuning): the resident-CTA bounds
+ * compiled for the variant of (n_layers, solver, features), default first,
+ * into bounds[0..n); returns how many, or CMTJ_ERR_ARG. */
+int cmtj_batch_bounds_f32(int32_t n_layers, int32_t solver, int32_t features, int32_t *bounds, int32_t n);
 
 /* No counterpart in the reference: an allocation-free form of
  * cmtj_batch_run_f32 for callers that cannot call cudaMalloc (code running
