@@ -561,14 +561,18 @@ def measure_rest(run, low, spec, n_steps, kern_ms, fft_ms, lib):
         peaks[name] = fn(5) / 1e12
     # the FP32 ceiling is the larger of scalar FFMA and packed FFMA2 issue
     peak = max(peaks.values())
-    # DRAM traffic of k_batch per launch, from the ncu capture of the
+    # DRAM traffic of k_batch per launch: the reads measured by ncu on the
     # 2000-step case of the same batch (profiles/k_batch_pimm_262k_2000steps.md:
-    # 313.5 MB read, 176.4 MB written): the records are read once, the
-    # decimated log writes grow with the steps run
-    traffic = 313.5e6 + 176.4e6 * (n_steps / 2000.0)
+    # 313.5 MB, the records read once, the same at any length), plus the
+    # writes at their algorithmic count (every decimated log sample and the
+    # final states).  The capture's own 176 MB of writes understate a launch:
+    # the last tiles were still in L2 when that kernel ended.
+    log_write = 4.0 * float(np.sum(run.samples)) + n * batch.F32_STATE_DTYPE.itemsize
+    traffic = 313.5e6 + log_write
     out["roofline"] = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                        "frac": achieved / peak, "traffic": traffic,
-                       "traffic_source": "ncu dram__bytes_read/write of the 2000-step capture, writes scaled by steps",
+                       "traffic_source": "ncu dram__bytes_read of the 2000-step capture (records, read once) + "
+                                         "algorithmic log and state writes",
                        "flop_per_layer_step": fpls,
                        "flop_model": "171 per layer-step in quiet bursts, 201 while the pulse is on; "
                                      "quiet share %.5f" % quiet,

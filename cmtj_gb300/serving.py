@@ -199,9 +199,9 @@ class ServingEngine:
         req.layer_steps = float(np.sum(low.n_steps * L))
         ids = slot + np.arange(n)
         parts = {}
-        for key in np.unique(L * (1 << 24) + variant):
-            sel = (L * (1 << 24) + variant) == key
-            parts[(int(key >> 24), int(req.solver), int(key & ((1 << 24) - 1)), int(req.red_every))] = \
+        for key in np.unique(L * (1 << 32) + variant):
+            sel = (L * (1 << 32) + variant) == key
+            parts[(int(key >> 32), int(req.solver), int(key & ((1 << 32) - 1)), int(req.red_every))] = \
                 ids[sel].astype(np.int32)
         meta = {"slot": slot, "parts": parts, "steps_max": int(low.n_steps.max()), "done": 0}
         self.active.append((req, meta))

@@ -63,6 +63,10 @@ def test_every_bound_and_tile_gives_the_same_bits(gpu_lib, solver, layers):
         spec, ns = sweeps.vsd_config(n_f=4, n_h=128, dt=DT, t_min=1e-10, t_max=2e-10)
         keep = np.nonzero(spec.n_layers == 4)[0]
         spec, ns = spec.take(keep), ns[keep]
+        # the rows of one kernel variant (one partition)
+        first = batch.BatchRun(batch.lower(spec, DT, ns), DT, mode)
+        rows = first.part_rows[0]
+        spec, ns = spec.take(rows), ns[rows]
     low = batch.lower(spec, DT, ns)
     lib = _abi.load()
     log_mode = batch.LOG_M if layers < 4 else batch.LOG_MIX
@@ -84,14 +88,14 @@ def test_every_bound_and_tile_gives_the_same_bits(gpu_lib, solver, layers):
 
 @pytest.mark.gpu
 def test_tuned_fp64_lanes_equal_defaults(gpu_lib, fresh_table, monkeypatch):
-    """The FP64 plain form on 2048 R(H) MTJs for 2000 steps: with the lane
+    """The FP64 plain form on 4096 R(H) MTJs for 3000 steps: with the lane
     layout the tuner picks and with the library's pick, the same bits."""
     from cmtj_gb300 import tune
     out = []
     for flag in ("1", "0"):
         monkeypatch.setenv("CMTJ_AUTOTUNE", flag)
-        js = tune.rh_junctions(2048, 2000 * DT)
-        low = engine.run_junctions(js, engine.plan_run(2000 * DT, DT, 100 * DT), cm.SolverMode.RK4)
+        js = tune.rh_junctions(4096, 3000 * DT)
+        engine.run_junctions(js, engine.plan_run(3000 * DT, DT, 100 * DT), cm.SolverMode.RK4)
         out.append(np.array([[l.mag.x, l.mag.y, l.mag.z] for j in js for l in j.layers]))
-    assert autotune.lookup(autotune.f64_key(2, 1, 2048)) is not None
+    assert autotune.lookup(autotune.f64_key(2, 1, 4096)) is not None
     assert np.array_equal(out[0], out[1])

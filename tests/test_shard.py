@@ -105,3 +105,46 @@ def test_sharded_sweep_gloo_world2_equals_unsharded(tmp_path):
     want = _oracle_runner(spec, n_steps)
     assert np.array_equal(got["steps"], n_steps)
     assert np.array_equal(got["m"], want["m"])
+
+
+def _gpu_runner(sub, n_steps):
+    """One rank's work on its GPU: the FP32 batched form over its rows, with
+    the on-device <I R> reduction; final m, reductions and step counts."""
+    from cmtj_gb300 import batch
+    run = batch.BatchRun(batch.lower(sub, DT, n_steps), DT, cm.SolverMode.RK4, batch.LOG_NONE, 0, red_every=1)
+    run.launch()
+    st = run.state()
+    return {"m": st["m"].copy(), "v": st["v_sum"].copy(), "status": st["status"].copy(),
+            "steps": st["step"].astype(np.int64)}
+
+
+def _gpu_worker(rank, world, port, out):
+    import torch
+    import torch.distributed as dist
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    torch.cuda.set_device(0)  # one GPU here: the ranks share it, and nothing on it waits on another rank
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        spec, n_steps = sweeps.vsd_config(n_f=8, n_h=64, seed=11, dt=DT, t_min=2e-10, t_max=6e-10)
+        res = shard.run_sharded(spec, n_steps, _gpu_runner, rank, world)
+        if rank == 0:
+            np.savez(out, **res)
+        dist.barrier()
+    finally:
+        dist.destroy_process_group()
+
+
+@pytest.mark.gpu
+def test_sharded_gpu_sweep_equals_unsharded(gpu_lib, tmp_path):
+    """The sharded path with the GPU solver: two gloo ranks, each running its
+    own rows of an uneven spin-diode sweep on the GPU (FP32 batched form),
+    gathered on rank 0, equal the unsharded GPU run bit for bit."""
+    out = str(tmp_path / "sharded_gpu.npz")
+    mp.spawn(_gpu_worker, args=(2, _free_port(), out), nprocs=2, join=True)
+    got = np.load(out)
+    spec, n_steps = sweeps.vsd_config(n_f=8, n_h=64, seed=11, dt=DT, t_min=2e-10, t_max=6e-10)
+    want = _gpu_runner(spec, n_steps)
+    assert np.all(got["status"] == 0) and np.array_equal(got["steps"], n_steps)
+    for k in ("m", "v"):
+        assert got[k].tobytes() == want[k].tobytes(), k
