@@ -30,13 +30,10 @@ UNITS = {
     "group_f64.cu": ["--fmad=false"],
     "group_lanes_f64.cu": ["--fmad=false"],
     "batch_f32.cu": [],
-    # the FP32 kernels fuse multiply-adds where the source or the front end
-    # asks for them, never in the assembler, whose choices could differ
-    # between the two resident-CTA bounds a variant is compiled at
-    "batch_f32_l1.cu": ["-Xptxas", "--fmad=false"],
-    "batch_f32_l2.cu": ["-Xptxas", "--fmad=false"],
-    "batch_f32_l3.cu": ["-Xptxas", "--fmad=false"],
-    "batch_f32_l4.cu": ["-Xptxas", "--fmad=false"],
+    "batch_f32_l1.cu": [],
+    "batch_f32_l2.cu": [],
+    "batch_f32_l3.cu": [],
+    "batch_f32_l4.cu": [],
     "reduce.cu": [],
     "alpha_noise.cu": [],
 }

@@ -24,7 +24,8 @@ mkdir -p "$OUT"
 EXT="$(python3 -c 'import sysconfig;print(sysconfig.get_config_var("EXT_SUFFIX"))')"
 PYBIND_INC="$(python3 -m pybind11 --includes)"
 TARGET="$OUT/_cmtj$EXT"
-if [ ! -f "$TARGET" ] || [ "$REF/core/junction.hpp" -nt "$TARGET" ]; then
+STUB="$HERE/stubs/third_party/kissfft/kissfft.hh"
+if [ ! -f "$TARGET" ] || [ "$REF/core/junction.hpp" -nt "$TARGET" ] || [ "$STUB" -nt "$TARGET" ]; then
   g++ -O3 -shared -fPIC -std=c++17 -fvisibility=hidden -Wno-unused-variable \
       -ffp-contract=off -DVERSION_INFO='"ref-local"' \
       -I"$REF" -I"$REF/core" -I"$HERE/stubs/third_party" \
@@ -33,7 +34,8 @@ if [ ! -f "$TARGET" ] || [ "$REF/core/junction.hpp" -nt "$TARGET" ]; then
 fi
 # The reference's BufferedAlphaNoise behind a C entry point (alpha_ref.cpp).
 ALPHA="$OUT/libalpha_ref.so"
-if [ ! -f "$ALPHA" ] || [ "$REF/core/noise.hpp" -nt "$ALPHA" ] || [ "$HERE/alpha_ref.cpp" -nt "$ALPHA" ]; then
+if [ ! -f "$ALPHA" ] || [ "$REF/core/noise.hpp" -nt "$ALPHA" ] || [ "$HERE/alpha_ref.cpp" -nt "$ALPHA" ] || \
+   [ "$STUB" -nt "$ALPHA" ]; then
   g++ -O2 -shared -fPIC -std=c++17 -ffp-contract=off -I"$REF/core" -I"$HERE/stubs/third_party" \
       "$HERE/alpha_ref.cpp" -o "$ALPHA.tmp"
   mv "$ALPHA.tmp" "$ALPHA"

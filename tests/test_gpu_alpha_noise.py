@@ -138,3 +138,27 @@ def test_fp64_runs_with_alpha_noise_match_oracle(gpu_lib, solver, axis, T):
             assert np.max(np.abs(la[k] - lb[k])) <= 1e-9, (k, float(np.max(np.abs(la[k] - lb[k]))))
         moved = max(moved, float(np.max(np.abs(la["free_my"] - la["free_my"][0]))))
     assert moved > 1e-3  # the noise moved m
+
+
+@pytest.mark.gpu
+def test_fp64_alpha_noise_switching_matches_reference(gpu_lib):
+    """The FP64 plain form on every alpha-noise p-bit case (alpha 0.5-1.5,
+    scale 0.01-0.03, axis all or x, with and without 300 K), 1024 runs
+    each in one launch: P(m_z < 0) within the 3-sigma binomial bound of the
+    reference's counts (its BufferedAlphaNoise on mt19937)."""
+    import thermal_cases
+    from test_thermal import binomial_ok, load_alpha_ref
+    cases, sw, runs = load_alpha_ref()
+    n = 1024
+    js = []
+    for q, case in enumerate(thermal_cases.ALPHA_CASES):
+        for k in range(n):
+            j, run = thermal_cases.alpha_pbit_junction(cm, *case)
+            j.layers[0].noise_seed = 7_000_000 + 100_000 * q + k
+            js.append(j)
+    plan = engine.plan_run(run["totalTime"], run["timeStep"], run["writeFrequency"])
+    engine.run_junctions(js, plan, cm.SolverMode.EulerHeun)
+    for q, case in enumerate(thermal_cases.ALPHA_CASES):
+        k = sum(1 for j in js[q * n:(q + 1) * n] if j.getLayerMagnetisation("free").z < 0)
+        ok, d, b = binomial_ok(k, n, int(sw[q]), int(runs[q]))
+        assert ok, (case, k / n, sw[q] / runs[q], d, b)

@@ -52,7 +52,9 @@ def test_tuned_fp32_batch_equals_defaults(gpu_lib, fresh_table, monkeypatch):
 @pytest.mark.parametrize("solver,layers", [("RK4", 2), ("EulerHeun", 1), ("RK4", 4)])
 def test_every_bound_and_tile_gives_the_same_bits(gpu_lib, solver, layers):
     """Each compiled resident-CTA bound of a variant, and log tiles of 4
-    and 16, run the same junctions to the same bits."""
+    and 16, run the same junctions to the same bits: final states and
+    every logged sample (the padding after a row's last sample is not a
+    result)."""
     mode = getattr(cm.SolverMode, solver)
     if layers == 1:
         spec, ns, _ = sweeps.pbit_config(n_j=4, n_per=256, dt=DT, t_min=1e-10, t_max=2e-10)
@@ -82,8 +84,12 @@ def test_every_bound_and_tile_gives_the_same_bits(gpu_lib, solver, layers):
             run._launch_part(0, None, engine.torch().cuda.current_stream(), tile, (code & 0xffffff) | (bound << 24))
             st = run.state()
             assert np.all(st["status"] == 0)
-            results.append((st.tobytes(), run.d_log.cpu().numpy().tobytes(), bound, tile))
-    assert len({r[0] for r in results}) == 1 and len({r[1] for r in results}) == 1, [r[2:] for r in results]
+            log = run.d_log.cpu().numpy()
+            samples = np.concatenate([run.log_of(k, log).ravel() for k in range(run.n)])
+            results.append((st.tobytes(), samples.tobytes(), bound, tile))
+    same_state = len({r[0] for r in results}) == 1
+    same_log = len({r[1] for r in results}) == 1
+    assert same_state and same_log, (same_state, same_log, [r[2:] for r in results])
 
 
 @pytest.mark.gpu

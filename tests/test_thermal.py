@@ -118,3 +118,34 @@ def test_oracle_full_sweep_statistics_match_reference():
             k = sum(ex.map(one, range(n)))
         ok, d, b = binomial_ok(k, n, int(sw[q]), int(runs[q]))
         assert ok, (jd, k / n, sw[q] / runs[q], d, b)
+
+
+def load_alpha_ref():
+    """The reference's switching counts of the p-bit layer with buffered
+    alpha noise (tests/golden/alpha_switching.npz: thermal_cases.ALPHA_CASES,
+    1024 runs each, the reference's BufferedAlphaNoise on mt19937)."""
+    g = np.load("%s/golden/alpha_switching.npz" % thermal_cases.__file__.rsplit("/", 1)[0])
+    return g["cases"], g["switched"], g["runs"]
+
+
+def test_oracle_alpha_noise_switching_matches_reference():
+    """The oracle (Philox white draws, its own restatement of fillBuffer) on
+    the first alpha-noise case, 384 runs: P(m_z < 0) within the 3-sigma
+    binomial bound of the reference's count."""
+    from concurrent.futures import ThreadPoolExecutor
+    cases, sw, runs = load_alpha_ref()
+    assert [tuple(c) for c in cases] == [tuple(map(float, c)) for c in thermal_cases.ALPHA_CASES]
+    oracle_harness.oracle_lib()
+    n, q = 384, 0
+
+    def one(k):
+        j, run = thermal_cases.alpha_pbit_junction(cmtj_gb300, *thermal_cases.ALPHA_CASES[q])
+        j.layers[0].noise_seed = 6_000_000 + k
+        r = dict(run)
+        oracle_harness.run_oracle([j], r.pop("totalTime"), **r)
+        return j.getLayerMagnetisation("free").z < 0
+
+    with ThreadPoolExecutor(8) as ex:
+        k = sum(ex.map(one, range(n)))
+    ok, d, b = binomial_ok(k, n, int(sw[q]), int(runs[q]))
+    assert ok, (k / n, sw[q] / runs[q], d, b)

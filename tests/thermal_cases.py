@@ -14,6 +14,7 @@ PBIT_T = 300.0
 
 
 def pbit_junction(cm, j_density, Ku=PBIT_KU, T=PBIT_T):
+    """The p-bit junction; T = None sets no temperature driver."""
     z = cm.CVector(0, 0, 0)
     l = cm.Layer.createSTTLayer("free", mag=cm.CVector(0, 0, 1), anis=cm.CVector(0, 0, 1), Ms=1.0,
                                 thickness=1.2e-9, cellSurface=7e-17, demagTensor=[z, z, z], damping=0.02,
@@ -22,7 +23,8 @@ def pbit_junction(cm, j_density, Ku=PBIT_KU, T=PBIT_T):
     j = cm.Junction([l])
     j.setLayerAnisotropyDriver("free", cm.constantDriver(Ku))
     j.setLayerCurrentDriver("free", cm.stepDriver(0, j_density, 0, 1e-9))
-    j.setLayerTemperatureDriver("free", cm.constantDriver(T))
+    if T is not None:
+        j.setLayerTemperatureDriver("free", cm.constantDriver(T))
     return j, dict(totalTime=2e-9, timeStep=1e-13, writeFrequency=1e-10,
                    solverMode=cm.SolverMode.EulerHeun)
 
@@ -61,4 +63,21 @@ def pbit_sweep_junction(cm, j_density, duration):
     j, run = pbit_junction(cm, j_density, Ku=SWEEP_KU)
     run = dict(run)
     run.update(totalTime=float(duration), writeFrequency=1e-9)
+    return j, run
+
+
+# The p-bit layer above with buffered 1/f^alpha noise (setAlphaNoise(alpha,
+# std 1, scale, axis)), 2 ns Euler-Heun: (current A/m^2, temperature K,
+# alpha, scale, axis: 3 all, 0 x only).  Without alpha noise the T = 0
+# cases never switch; with it most switch a good part of the time, and the
+# 300 K case switches about three times as often as thermal noise alone.
+ALPHA_CASES = [(1e11, 0.0, 1.0, 0.01, 3), (6e10, 0.0, 1.0, 0.03, 3), (0.0, 300.0, 1.0, 0.01, 3),
+               (1e11, 0.0, 0.5, 0.01, 3), (1e11, 0.0, 1.5, 0.01, 3), (1e11, 0.0, 1.0, 0.03, 0)]
+
+
+def alpha_pbit_junction(cm, j_density, T, alpha, scale, axis):
+    """The p-bit junction with alpha noise on its layer; T = 0 sets no
+    temperature."""
+    j, run = pbit_junction(cm, j_density, T=T if T else None)
+    j.getLayer("free").setAlphaNoise(alpha, 1.0, scale, cm.Axis(int(axis)))
     return j, run
