@@ -835,8 +835,10 @@ def vsd_accuracy(spec, n_steps, st, n_sample=64, seed=5):
 
 
 def _timed_run(run):
-    """One full launch of a BatchRun timed with CUDA events on its stream."""
+    """One full launch of a BatchRun timed with CUDA events on its stream
+    (its launch choices resolved first, outside the timed region)."""
     import torch
+    run.tune()
     torch.cuda.synchronize()
     a = torch.cuda.Event(enable_timing=True)
     b = torch.cuda.Event(enable_timing=True)

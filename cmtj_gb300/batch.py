@@ -680,6 +680,14 @@ class BatchRun:
         for e in ends:
             main.wait_event(e)
 
+    def tune(self, chunk_steps=None, stream=None):
+        """Resolve every partition's launch choices now (trial launches for
+        kinds of partition the autotuner has not met), so that a later
+        launch() runs no trials."""
+        from . import engine
+        main = stream if stream is not None else engine.torch().cuda.current_stream()
+        return [self._choice(q, chunk_steps, main) for q in range(len(self.parts))]
+
     def _choice(self, q, chunk_steps, stream):
         """(log tile, variant code) of partition q: the autotuner's choice
         (tuned now if this kind of partition is new), else the defaults."""

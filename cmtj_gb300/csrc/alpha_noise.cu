@@ -20,9 +20,11 @@
 //
 // Per batch of buffer rows (scratch: three M-point complex rows each, plus
 // a header of six doubles):
-//   k_alpha_fill     white draws (Philox, or the caller's) and zero padding
-//   k_alpha_weights  h by the reference's float recurrence, one thread/row
-//   k_alpha_bins     H_N, H_{N-1}, W_N, W_{N-1} (FP64, fixed order)
+//   k_alpha_fill     white draws (Philox, or the caller's), the factors of
+//                    the filter recurrence, zero padding
+//   k_alpha_weights  h as the reference's sequential float product, one
+//                    warp per row
+//   k_alpha_bins     H_N, H_{N-1}, W_N, W_{N-1} (FP64 sums, fixed order)
 //   k_fft_pass<R>    Stockham radix-4 passes (radix-2 tail), forward h and
 //                    w, pointwise product, inverse
 //   k_alpha_finish   c / M less the top-bin term, rounded to float
@@ -43,8 +45,11 @@ __device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(
 // i * a
 __device__ __forceinline__ float2 cmuli(float2 a) { return make_float2(-a.y, a.x); }
 
-// White draws and zero padding: A[row][m] = w_m (m < N), 0 beyond; the
-// weight row's padding [N, M) is zeroed here too.
+// White draws and zero padding: A[row][m] = w_m (m < N), 0 beyond.  The
+// weight row gets the factors of the filter recurrence (noise.hpp:171-176),
+// in the reference's float arithmetic: Hh[0] = 1 and, for 1 <= m < N,
+// Hh[m] = (float)(0.5 * alpha + (float)(m - 1)) / (float)m; 0 beyond.
+// alpha outside [0, 2] (which setAlphaNoise rejects) gives a NaN row.
 __global__ void k_alpha_fill(const cmtj_alpha_noise_t *__restrict__ specs, int row0, int rows, uint32_t N,
                              uint32_t M, const float *__restrict__ white, float2 *__restrict__ A,
                              float2 *__restrict__ Hh) {
@@ -53,44 +58,71 @@ __global__ void k_alpha_fill(const cmtj_alpha_noise_t *__restrict__ specs, int r
        idx += (uint64_t)gridDim.x * blockDim.x) {
     const int r = (int)(idx / M);
     const uint32_t m = (uint32_t)(idx % M);
-    float w = 0.f;
+    const cmtj_alpha_noise_t &s = specs[row0 + r];
+    float w = 0.f, h = 0.f;
     if (m < N) {
       if (white) {
         w = white[(size_t)(row0 + r) * N + m];
       } else {
-        const cmtj_alpha_noise_t &s = specs[row0 + r];
-        double g[3];
-        cmtj_alpha_gaussian3_f64(s.seed_lo, s.seed_hi, s.counter + m, g[0], g[1], g[2]);
-        w = (float)(s.std * g[s.component < 0 ? 0 : (s.component > 2 ? 2 : s.component)]);
+        const int c = s.component < 0 ? 0 : (s.component > 2 ? 2 : s.component);
+        w = (float)(s.std * cmtj_alpha_gaussian_f64(s.seed_lo, s.seed_hi, s.counter + m, c));
       }
-    } else {
-      Hh[idx] = make_float2(0.f, 0.f);
+      const bool ok = s.alpha >= 0.0 && s.alpha <= 2.0;
+      h = !ok ? __int_as_float(0x7fffffff)
+              : (m == 0 ? 1.0f : (float)(0.5 * s.alpha + (double)(float)(m - 1)) / (float)m);
     }
     A[idx] = make_float2(w, 0.f);
+    Hh[idx] = make_float2(h, 0.f);
   }
 }
 
-// The filter weights of noise.hpp:171-176, in the reference's float
-// arithmetic: weight_i = (float)(0.5 * alpha + (float)(i - 1)) / (float)i,
-// h_i = h_{i-1} * weight_i.  A sequential product, so one thread per row.
-// alpha outside [0, 2] (which setAlphaNoise rejects) gives NaN weights.
-__global__ void k_alpha_weights(const cmtj_alpha_noise_t *__restrict__ specs, int row0, int rows, uint32_t N,
-                                uint32_t M, float2 *__restrict__ Hh) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+// h_m = h_{m-1} * factor_m over each weight row, in place: the reference's
+// sequential float product, in order.  One warp per row: each round the
+// warp loads 32 x 8 factors (coalesced), then the running product passes
+// from lane to lane, each lane multiplying through its 8; the next round's
+// loads are issued before this round's chain.
+__global__ void __launch_bounds__(128) k_alpha_weights(int rows, uint32_t N, uint32_t M, float2 *__restrict__ Hh) {
+  constexpr int K = 8, CH = 32 * K;
+  const int lane = threadIdx.x & 31;
+  const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (r >= rows) return;
-  const double alpha = specs[row0 + r].alpha;
   float2 *h = Hh + (size_t)r * M;
-  float v = (alpha >= 0.0 && alpha <= 2.0) ? 1.0f : __int_as_float(0x7fffffff);
-  h[0] = make_float2(v, 0.f);
-  for (uint32_t i = 1; i < N; ++i) {
-    const float weight = (float)(0.5 * alpha + (double)(float)(i - 1)) / (float)i;
-    v = v * weight;
-    h[i] = make_float2(v, 0.f);
+  float v = h[0].x;  // 1 (or NaN)
+  float cur[K], nxt[K];
+  auto load = [&](uint32_t base, float *dst) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      const uint32_t i = base + (uint32_t)(lane * K + k);
+      dst[k] = i < N ? h[i].x : 1.0f;
+    }
+  };
+  load(1, cur);
+  for (uint32_t base = 1; base < N; base += CH) {
+    if (base + CH < N) load(base + CH, nxt);
+    for (int L = 0; L < 32; ++L) {
+      if (lane == L) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+          v = v * cur[k];
+          cur[k] = v;
+        }
+      }
+      v = __shfl_sync(0xffffffffu, v, L);
+    }
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      const uint32_t i = base + (uint32_t)(lane * K + k);
+      if (i < N) h[i] = make_float2(cur[k], 0.f);
+      cur[k] = nxt[k];
+    }
   }
 }
 
 // H_N, Re/Im H_{N-1}, W_N, Re/Im W_{N-1} of each row, summed in FP64 in a
-// fixed order (one block per row).
+// fixed order (one block per row).  The twiddle of bin N-1 comes from the
+// exact integer phase j (N-1) mod 2N through the float sincospi: its
+// ~1e-7 error enters only the top-bin term, itself of order 1/sqrt(N) of
+// the samples.
 __global__ void __launch_bounds__(kThreads) k_alpha_bins(int rows, uint32_t N, uint32_t M,
                                                          const float2 *__restrict__ A,
                                                          const float2 *__restrict__ Hh, double *__restrict__ bins) {
@@ -104,9 +136,10 @@ __global__ void __launch_bounds__(kThreads) k_alpha_bins(int rows, uint32_t N, u
     const double hj = h[j].x, wj = w[j].x;
     const double sgn = (j & 1u) ? -1.0 : 1.0;
     // e^{-2 pi i j (N-1) / 2N}: the phase j (N-1) mod 2N in integers
-    const uint64_t q = ((uint64_t)j * (uint64_t)(N - 1)) % twoN;
-    double s, c;
-    sincospi(-(double)q / (double)N, &s, &c);
+    const uint32_t q = (uint32_t)(((uint64_t)j * (uint64_t)(N - 1)) % twoN);
+    float sf, cf;
+    sincospif(-(float)q / (float)N, &sf, &cf);
+    const double s = sf, c = cf;
     acc[0] += hj * sgn;
     acc[1] += hj * c;
     acc[2] += hj * s;
@@ -283,7 +316,7 @@ extern "C" int cmtj_alpha_noise_f32(const cmtj_alpha_noise_t *d_specs, int32_t n
     const uint64_t elems = (uint64_t)rows * M;
     k_alpha_fill<<<grid_for(elems), kThreads, 0, s>>>(d_specs, row0, rows, n, M, d_white, P0, P1);
     CMTJ_LAUNCH_CHECK("k_alpha_fill");
-    k_alpha_weights<<<(rows + 63) / 64, 64, 0, s>>>(d_specs, row0, rows, n, M, P1);
+    k_alpha_weights<<<(rows + 3) / 4, 128, 0, s>>>(rows, n, M, P1);
     CMTJ_LAUNCH_CHECK("k_alpha_weights");
     k_alpha_bins<<<rows, kThreads, 0, s>>>(rows, n, M, P0, P1, bins);
     CMTJ_LAUNCH_CHECK("k_alpha_bins");

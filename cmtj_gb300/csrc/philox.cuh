@@ -57,6 +57,25 @@ __device__ __forceinline__ void cmtj_gaussian3_f64(uint32_t seed_lo, uint32_t se
   cmtj_gaussian3_of_words(cmtj_thermal_words(seed_lo, seed_hi, step), g0, g1, g2);
 }
 
+// Normal `c` (0, 1 or 2) of the alpha-noise stream's draw i alone: the
+// same operations as that component of cmtj_alpha_gaussian3_f64, so the
+// same bits, without the other two transcendental chains.
+__device__ __forceinline__ double cmtj_alpha_gaussian_f64(uint32_t seed_lo, uint32_t seed_hi, uint64_t i, int c) {
+  const uint4 w =
+      cmtj_philox4x32_10(make_uint4((uint32_t)i, (uint32_t)(i >> 32), CMTJ_ALPHA_TAG, 0u), seed_lo, seed_hi);
+  const double s = 2.3283064365386963e-10;  // 2^-32
+  if (c < 2) {
+    const double u0 = ((double)w.x + 0.5) * s, u1 = ((double)w.y + 0.5) * s;
+    const double r0 = sqrt(-2.0 * log(u0));
+    const double a0 = 6.283185307179586 * u1;
+    return c == 0 ? r0 * cos(a0) : r0 * sin(a0);
+  }
+  const double u2 = ((double)w.z + 0.5) * s, u3 = ((double)w.w + 0.5) * s;
+  const double r1 = sqrt(-2.0 * log(u2));
+  const double a1 = 6.283185307179586 * u3;
+  return r1 * cos(a1);
+}
+
 // FP64 white draws of the buffered alpha noise.
 __device__ __forceinline__ void cmtj_alpha_gaussian3_f64(uint32_t seed_lo, uint32_t seed_hi, uint64_t i,
                                                          double &g0, double &g1, double &g2) {
