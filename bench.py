@@ -350,9 +350,15 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--profile", action="store_true",
                     help="262144 junctions x 2000 steps, no extra measurements (for ncu captures)")
+    ap.add_argument("--profile-alpha", action="store_true",
+                    help="the alpha-noise generator alone: 192 buffers of 100,000 samples, a warm-up call and one "
+                         "timed call (for ncu captures)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference_arm(args)
+        return
+    if args.profile_alpha:
+        profile_alpha()
         return
 
     import torch
@@ -523,6 +529,25 @@ def main():
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def profile_alpha(rows=192, n=100_000):
+    """The buffered alpha-noise generator (cmtj_alpha_noise_f32) on `rows`
+    buffers of n samples (three axes of rows / 3 layers; FFT size 262,144
+    for n = 100,000): one warm-up call, one call timed with CUDA events."""
+    import torch
+    from cmtj_gb300 import noise
+    specs = noise.specs_array([(1.0, 1.0, 77 + r // 3, 0, r % 3) for r in range(rows)])
+    noise.device_buffers(specs, n)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    noise.device_buffers(specs, n)
+    b.record()
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b)
+    print(json.dumps({"alpha_noise_generator": {"rows": rows, "samples": n, "ms": ms,
+                                                "samples_per_s": rows * n / (ms / 1e3)}}))
 
 
 def build_peak_probe():
