@@ -88,23 +88,27 @@ def compute_spectrum_strip(input_m, int_step, max_frequency):
 
 
 class FieldScan:
-    """cmtj/utils/linear.py:6-124: field-vector constructors for sweeps."""
+    """cmtj/utils/linear.py:6-124: field-vector constructors for sweeps.
+    The arithmetic (sin/cos of the degree angles, then the products in the
+    reference's order) is the reference's, so sweeps built here equal its
+    own to the bit."""
 
     @staticmethod
     def _trig_compute(theta, phi):
+        """(sin theta, cos theta, sin phi, cos phi), angles in degrees."""
         return (np.sin(np.deg2rad(theta)), np.cos(np.deg2rad(theta)), np.sin(np.deg2rad(phi)),
                 np.cos(np.deg2rad(phi)))
 
     @staticmethod
     def angle2vector(theta, phi, amplitude=1):
-        st, ct, sp, cp = FieldScan._trig_compute(theta, phi)
-        return CVector(st * cp * amplitude, st * sp * amplitude, ct * amplitude)
+        sin_t, cos_t, sin_p, cos_p = FieldScan._trig_compute(theta, phi)
+        return CVector(sin_t * cos_p * amplitude, sin_t * sin_p * amplitude, cos_t * amplitude)
 
     @staticmethod
     def vector2angle(x, y, z):
         """(theta, phi, r) in degrees of a cartesian vector."""
-        r = np.sqrt(x ** 2 + y ** 2 + z ** 2)
-        return np.rad2deg(np.arctan2(np.sqrt(x ** 2 + y ** 2), z)), np.rad2deg(np.arctan2(y, x)), r
+        norm = np.sqrt(x ** 2 + y ** 2 + z ** 2)
+        return np.rad2deg(np.arctan2(np.sqrt(x ** 2 + y ** 2), z)), np.rad2deg(np.arctan2(y, x)), norm
 
     @staticmethod
     def cvector2angle(vector):
@@ -113,28 +117,29 @@ class FieldScan:
     @staticmethod
     def theta_scan(start, stop, steps, amplitude, phi):
         """Polar-angle sweep at fixed amplitude and azimuth (degrees)."""
-        span = np.linspace(start, stop, endpoint=True, num=steps)
-        st, ct, sp, cp = FieldScan._trig_compute(span, phi)
-        return span, np.vstack((st * cp * amplitude, st * sp * amplitude, ct * amplitude)).T
+        angles = np.linspace(start, stop, endpoint=True, num=steps)
+        sin_t, cos_t, sin_p, cos_p = FieldScan._trig_compute(angles, phi)
+        return angles, np.vstack((sin_t * cos_p * amplitude, sin_t * sin_p * amplitude, cos_t * amplitude)).T
 
     @staticmethod
     def phi_scan(start, stop, steps, amplitude, theta):
         """Azimuth sweep at fixed amplitude and polar angle (degrees)."""
-        span = np.linspace(start, stop, endpoint=True, num=steps)
-        st, ct, sp, cp = FieldScan._trig_compute(theta, span)
-        Hy = st * sp * amplitude
-        return span, np.vstack((st * cp * amplitude, Hy, ct * amplitude * np.ones_like(Hy))).T
+        angles = np.linspace(start, stop, endpoint=True, num=steps)
+        sin_t, cos_t, sin_p, cos_p = FieldScan._trig_compute(theta, angles)
+        y_part = sin_t * sin_p * amplitude
+        return angles, np.vstack((sin_t * cos_p * amplitude, y_part, cos_t * amplitude * np.ones_like(y_part))).T
 
     @staticmethod
     def amplitude_scan(start, stop, steps, theta, phi, back=False):
-        Hspan = np.linspace(start, stop, endpoint=True, num=steps)
-        st, ct, sp, cp = FieldScan._trig_compute(theta, phi)
-        Hx, Hy, Hz = st * cp * Hspan, st * sp * Hspan, ct * Hspan
+        """Field-magnitude sweep along a fixed direction; with `back` the
+        sweep returns to its start (the turning point once)."""
+        magnitudes = np.linspace(start, stop, endpoint=True, num=steps)
+        sin_t, cos_t, sin_p, cos_p = FieldScan._trig_compute(theta, phi)
+        vectors = np.vstack((sin_t * cos_p * magnitudes, sin_t * sin_p * magnitudes, cos_t * magnitudes)).T
         if back:
-            forward = np.vstack((Hx, Hy, Hz)).T
-            return (np.concatenate((Hspan[:-1], Hspan[::-1]), axis=0),
-                    np.concatenate((forward[:-1], forward[::-1]), axis=0))
-        return Hspan, np.vstack((Hx, Hy, Hz)).T
+            return (np.concatenate((magnitudes[:-1], magnitudes[::-1]), axis=0),
+                    np.concatenate((vectors[:-1], vectors[::-1]), axis=0))
+        return magnitudes, vectors
 
 
 # ---------------------------------------------------------------- engine

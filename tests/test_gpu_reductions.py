@@ -220,3 +220,33 @@ def test_spectrum_kernel_matches_numpy(gpu_lib, nfft):
     ref = np.abs(np.fft.fft(x[:, length - nfft:length].astype(np.float64), axis=1))[:, lo:hi]
     tol = 4 * np.finfo(np.float32).eps * np.log2(nfft) * np.linalg.norm(x[:, length - nfft:length], axis=1)
     assert np.all(np.max(np.abs(got - ref), axis=1) <= tol)
+
+
+@pytest.mark.gpu
+def test_windowed_mean_r_matches_fp64(gpu_lib):
+    """The on-device time-averaged R over a window (the R(H) sweep's mean over
+    its last fifth; procedures.py:292-296, compute.hpp:75-76): the 2-layer
+    MTJ of the R(H) sweep from +z under fields of 400-800 kA/m along +-x
+    (FP64 moves <= 5e-6 under a 1e-7 nudge of m0 here), 20,000 RK4 steps,
+    R summed on the device over the last 4,000, against the mean of the
+    oracle's FP64 R log over the same steps.  The window matters: the mean
+    over the whole run differs by 10-15 ohm."""
+    import cases
+    n, w0 = 20000, 16000
+    fields = [-8e5, -7e5, -6e5, -5e5, -4e5, 4e5, 5e5, 6e5, 7e5, 8e5]
+    js32 = [cases.mtj_rh_point(cm, hx=h, total=n * DT)[0] for h in fields]
+    js64 = [cases.mtj_rh_point(cm, hx=h, total=n * DT)[0] for h in fields]
+    spec = batch.BatchSpec.from_junctions(js32)
+    run = batch.BatchRun(batch.lower(spec, DT, n, win_start=w0), DT, cm.SolverMode.RK4, batch.LOG_NONE, 0,
+                         red_every=1)
+    run.launch()
+    st = run.state()
+    assert np.all(st["status"] == 0) and np.all(st["n_red"] == n - w0)
+    r32 = (st["r_sum"].astype(np.float64) + st["r_c"]) / (n - w0)
+    oracle_harness.run_oracle(js64, n * DT, DT, DT, threads=8)
+    for k, j in enumerate(js64):
+        R = j.getLogArrays()["R_free_ref"]
+        r64, r_all = float(np.mean(R[w0:])), float(np.mean(R))
+        assert abs(r_all - r64) > 5.0, (fields[k], r_all, r64)
+        tol = _mean_r_tolerance(100.0, r64)
+        assert abs(r32[k] - r64) <= tol, (fields[k], r32[k], r64, tol)
