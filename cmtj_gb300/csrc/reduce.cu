@@ -9,7 +9,8 @@
 // (self-sorting, no bit reversal) in radix-8 stages, with a final radix-4
 // or radix-2 stage when log2(n/2) is not a multiple of 3.  Every thread
 // keeps its 8 points in registers through a stage; stages exchange through
-// one shared-memory buffer (n/2 complex floats), so an n = 4096 spectrum
+// one shared-memory buffer (n/2 complex floats, one padding word per 32
+// against bank conflicts in the strided stores), so an n = 4096 spectrum
 // takes 4 stages and 8 CTA barriers.  The first stage reads the row
 // straight from HBM (coalesced); the last pass writes |X[k]| for k in
 // [bin_lo, bin_hi).
@@ -18,6 +19,11 @@
 namespace {
 
 constexpr int kMaxFft = 8192;
+
+// Shared-memory slot of point i: one padding word after every 32, so the
+// strided stores of the first stages (stride 8 in the first radix-8 stage)
+// fall in distinct banks.
+__device__ __forceinline__ int pad(int i) { return i + (i >> 5); }
 
 struct C2 {
   float r, i;
@@ -86,7 +92,7 @@ __device__ __forceinline__ void stage(const float *__restrict__ src_re, const fl
       const int idx = g + r * stride;
       // from global: point idx of the half-length complex sequence
       // z[m] = x[2m] + i x[2m+1] of the real row x
-      v[q][r] = from_global ? c2(grow[2 * idx], grow[2 * idx + 1]) : c2(src_re[idx], src_im[idx]);
+      v[q][r] = from_global ? c2(grow[2 * idx], grow[2 * idx + 1]) : c2(src_re[pad(idx)], src_im[pad(idx)]);
     }
     const int k = g % Ns;
     if (!first && k) {
@@ -112,8 +118,8 @@ __device__ __forceinline__ void stage(const float *__restrict__ src_re, const fl
     const int base = (g / Ns) * Ns * R + k;
 #pragma unroll
     for (int r = 0; r < R; ++r) {
-      dst_re[base + r * Ns] = v[q][r].r;
-      dst_im[base + r * Ns] = v[q][r].i;
+      dst_re[pad(base + r * Ns)] = v[q][r].r;
+      dst_im[pad(base + r * Ns)] = v[q][r].i;
     }
   }
   __syncthreads();
@@ -124,13 +130,13 @@ __device__ __forceinline__ void stage(const float *__restrict__ src_re, const fl
 // E[k] = (Z[k] + conj Z[h-k]) / 2, O[k] = (Z[k] - conj Z[h-k]) / 2i and
 // X[k] = E[k] + W_n^k O[k] (h = n/2, indices mod h); bins above n/2 use
 // |X[k]| = |X[n-k]|.
-__global__ void __launch_bounds__(512) k_spectrum(const float *__restrict__ series, int64_t row_stride,
+__global__ void __launch_bounds__(512, 2) k_spectrum(const float *__restrict__ series, int64_t row_stride,
                                                   int32_t series_len, int32_t n, int32_t bin_lo, int32_t bin_hi,
                                                   float *__restrict__ out) {
   extern __shared__ __align__(16) float sm[];
   const int h = n / 2;
   float *re = sm;
-  float *im = sm + h;
+  float *im = sm + pad(h);
   const int64_t row = blockIdx.x;
   const float *src = series + row * row_stride + (series_len - n);
   int Ns = 1;
@@ -156,8 +162,8 @@ __global__ void __launch_bounds__(512) k_spectrum(const float *__restrict__ seri
     if (q > h) q = n - q;
     const int a = q == h ? 0 : q;
     const int b = q == 0 ? 0 : h - q;
-    const C2 zk = c2(re[a], im[a]);
-    const C2 zc = c2(re[b], -im[b]);
+    const C2 zk = c2(re[pad(a)], im[pad(a)]);
+    const C2 zc = c2(re[pad(b)], -im[pad(b)]);
     const C2 e = c2(0.5f * (zk.r + zc.r), 0.5f * (zk.i + zc.i));
     const C2 o = c2(0.5f * (zk.i - zc.i), -0.5f * (zk.r - zc.r));
     float sn, cs;
@@ -187,7 +193,8 @@ extern "C" int cmtj_spectrum_f32(const float *d_series, int64_t row_stride, int3
     cmtj_set_error("cmtj_spectrum_f32: null buffer");
     return CMTJ_ERR_ARG;
   }
-  const size_t smem = (size_t)n_fft * sizeof(float);  // n/2 complex points
+  // n/2 complex points, re and im each padded by one word per 32
+  const size_t smem = 2 * (size_t)(n_fft / 2 + n_fft / 64) * sizeof(float);
   if (smem > 48 * 1024) {
     CMTJ_CUDA_TRY(cudaFuncSetAttribute(k_spectrum, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   }
