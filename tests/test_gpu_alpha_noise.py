@@ -162,3 +162,35 @@ def test_fp64_alpha_noise_switching_matches_reference(gpu_lib):
         k = sum(1 for j in js[q * n:(q + 1) * n] if j.getLayerMagnetisation("free").z < 0)
         ok, d, b = binomial_ok(k, n, int(sw[q]), int(runs[q]))
         assert ok, (case, k / n, sw[q] / runs[q], d, b)
+
+
+@pytest.mark.gpu
+def test_noise_module_classes(gpu_lib):
+    """cmtj.noise (python/cmtj.cpp:448-462): BufferedAlphaNoise.tick walks
+    the device buffer times its scale and draws a new buffer when it wraps;
+    VectorAlphaNoise.tickVector is the normalised sample vector times the
+    scale for Axis.all (one axis otherwise) and keeps the previous sample;
+    Layer.getOneFVector ticks the layer's buffered noise."""
+    import cmtj
+    b = cmtj.noise.BufferedAlphaNoise(64, 1.0, 2.0, 3.0)
+    first = [b.tick() for _ in range(64)]
+    buf = b.getFullBuffer()
+    assert np.allclose(first, 3.0 * buf.astype(np.float64))
+    second = [b.tick() for _ in range(64)]
+    assert not np.allclose(first, second)  # a fresh buffer after the wrap
+    v = cmtj.noise.VectorAlphaNoise(32, 1.0, 1.0, 0.5, cm.Axis.all)
+    prev = None
+    for _ in range(40):
+        s = v.tickVector()
+        assert abs(s.length() - 0.5) < 1e-12
+        if prev is not None:
+            assert v.getPrevSample().tolist() == [x / 0.5 for x in prev.tolist()]
+        prev = s
+    z = cmtj.noise.VectorAlphaNoise(32, 1.0, 1.0, 2.0, cm.Axis.zaxis)
+    s = z.tickVector()
+    assert s.x == 0.0 and s.y == 0.0 and s.z != 0.0
+    demag = [cm.CVector(0, 0, 0)] * 3
+    layer = cm.Layer("free", cm.CVector(0, 0, 1), cm.CVector(0, 0, 1), 1.0, 1e-9, 1e-16, demag, 0.01)
+    layer.setAlphaNoise(1.0, 1.0, 0.25)
+    layer.createBufferedAlphaNoise(16)
+    assert abs(layer.getOneFVector().length() - 0.25) < 1e-12
