@@ -90,20 +90,22 @@ def test_fp32_batch_boltzmann_equilibrium(gpu_lib):
 
 
 @pytest.mark.gpu
-def test_fp32_and_fp64_forms_share_the_noise_stream(gpu_lib):
-    """The same seeded p-bit junctions, 300 Euler-Heun steps at 300 K, in the
-    FP32 batched form and the FP64 plain form: the same Philox words drive
-    both, so the trajectories agree to the FP32 bound.  Independent (or
-    sign-flipped) noise would leave them about 1e-2 apart."""
+@pytest.mark.parametrize("solver", ["EulerHeun", "Heun"])
+def test_fp32_and_fp64_forms_share_the_noise_stream(gpu_lib, solver):
+    """The same seeded p-bit junctions, 300 Euler-Heun (or Heun) steps at
+    300 K, in the FP32 batched form and the FP64 plain form: the same Philox
+    words drive both, so the trajectories agree to the FP32 bound.
+    Independent (or sign-flipped) noise would leave them about 1e-2 apart."""
+    mode = getattr(cmtj_gb300.SolverMode, solver)
     a, run = seeded_pbits(cmtj_gb300, 8e10, 32, 31337)
     b, _ = seeded_pbits(cmtj_gb300, 8e10, 32, 31337)
     steps, dt = 300, run["timeStep"]
     spec = batch.BatchSpec.from_junctions(a)
-    r = batch.BatchRun(batch.lower(spec, dt, steps), dt, cmtj_gb300.SolverMode.EulerHeun)
+    r = batch.BatchRun(batch.lower(spec, dt, steps), dt, mode)
     r.launch()
     st = r.state()
     assert np.all(st["status"] == 0)
-    engine.run_junctions(b, engine.plan_run(steps * dt, dt, 10 * dt), cmtj_gb300.SolverMode.EulerHeun)
+    engine.run_junctions(b, engine.plan_run(steps * dt, dt, 10 * dt), mode)
     m32 = st["m"][:, 0, :].astype(np.float64)
     m64 = np.array([[j.layers[0].mag.x, j.layers[0].mag.y, j.layers[0].mag.z] for j in b])
     m0 = np.array([[j.layers[0].mag.x, j.layers[0].mag.y, j.layers[0].mag.z] for j in seeded_pbits(
