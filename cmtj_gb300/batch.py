@@ -680,6 +680,26 @@ class BatchRun:
         for e in ends:
             main.wait_event(e)
 
+    def graph(self, chunk_steps=None):
+        """A CUDA graph of one launch() -- every partition on its stream,
+        forked from and joined to the capture stream -- for replay with
+        graph.replay(): each replay advances every junction by up to
+        chunk_steps iterations from the state it finds, with no host work.
+        Launch choices are resolved before the capture."""
+        from . import engine
+        t = engine.torch()
+        self.tune(chunk_steps)
+        if len(self.parts) > 1 and self._streams is None:
+            self._streams = [t.cuda.Stream() for _ in range(min(len(self.parts), 8))]
+        g = t.cuda.CUDAGraph()
+        side = t.cuda.Stream()
+        side.wait_stream(t.cuda.current_stream())
+        with t.cuda.stream(side):
+            with t.cuda.graph(g, stream=side):
+                self.launch(chunk_steps, stream=side)
+        t.cuda.current_stream().wait_stream(side)
+        return g
+
     def tune(self, chunk_steps=None, stream=None):
         """Resolve every partition's launch choices now (trial launches for
         kinds of partition the autotuner has not met), so that a later
