@@ -602,6 +602,12 @@ def measure_rest(run, low, spec, n_steps, kern_ms, fft_ms, lib):
         peaks[name] = fn(5) / 1e12
     # the FP32 ceiling is the larger of scalar FFMA and packed FFMA2 issue
     peak = max(peaks.values())
+    # SM cycles a warp spends per FP64 FMA (one chain: latency; four
+    # independent chains: whether a warp's FP64 instructions overlap)
+    fn = probe.cmtj_probe_fp64_cycles
+    fn.restype = ctypes.c_double
+    fn.argtypes = [ctypes.c_int]
+    fp64_cycles = {"one_chain": fn(1), "four_chains": fn(4)}
     # DRAM traffic of k_batch per launch: the reads measured by ncu on the
     # 2000-step case of the same batch (profiles/k_batch_pimm_262k_2000steps.md:
     # 313.5 MB, the records read once, the same at any length), plus the
@@ -702,6 +708,27 @@ def measure_rest(run, low, spec, n_steps, kern_ms, fft_ms, lib):
         "rows": int(m64.shape[0] * m64.shape[1]), "tolerance": "max|dm| <= 1e-9, R relative <= 1e-9",
         "pass": bool(np.max(np.abs(m64 - mo)) <= 1e-9 and np.max(np.abs(r64 - ro) / np.abs(ro)) <= 1e-9)}
     rh_gpu["cpu_oracle"] = {k: v for k, v in rh_cpu.items() if k != "mean_R_last_2ns"}
+    rh_gpu["fp64_pipe_probe"] = {
+        "cycles_per_dfma": fp64_cycles,
+        "note": "one warp, clock64 around dependent DFMA chains (bench_peak.cu); a step of the FP64 plain "
+                "form costs about this per FP64 instruction on its warp"}
+    fz = rh_gpu["fused"]
+    mf, rf = fz.pop("logs")
+    dmf = np.max(np.abs(mf - mo), axis=(1, 2))
+    rel = np.max(np.abs(rf - ro) / np.abs(ro), axis=1)
+    ok = (dmf <= 1e-9) & (rel <= 1e-9)
+    spread = np.load(os.path.join(ROOT, "tests", "golden", "rh_fma_spread.npz"))
+    fz["vs_oracle_full_logs"] = {
+        "max_abs_dm": float(dmf.max()), "max_rel_dR": float(rel.max()),
+        "fields_within_1e-9": int(ok.sum()), "fields": int(len(ok)),
+        "other_fields": [{"field_index": int(i), "max_abs_dm": float(dmf[i]), "max_rel_dR": float(rel[i]),
+                          "fma_built_reference_max_abs_dm": float(spread["max_abs_dm"][i])}
+                         for i in np.flatnonzero(~ok)],
+        "fma_built_reference_fields_within_1e-9": int(np.sum(spread["max_abs_dm"] <= 1e-9)),
+        "note": "fma_built_reference: the reference compiled with FMA contraction (GCC's default on aarch64) "
+                "against its x86-64 build, per field, from tests/golden/rh_fma_spread.npz"}
+    fz["vs_cpu_oracle"] = rh_cpu["seconds"] / fz["kernel_s"]
+    del mf, rf
     for key, leg in (("dp", "dormand_prince_fmr_4096"), ("group", "groups_dipole_64x16")):
         cpu = out["cpu_baseline"].pop(key)
         gpu = out["other_workloads"][leg]
@@ -977,6 +1004,22 @@ def other_workloads():
                                                   for j in js],
                               "logs": rh_logs(js),
                               "sample": "64 fields x 100,000 RK4 steps, log every step"}
+    del js
+    # The same sweep in the fused FP64 arithmetic (cmtj_arithmetic
+    # CMTJ_ARITH_FUSED); its error is set beside how far the reference itself
+    # moves when compiled with FMA contraction (tests/golden/rh_fma_spread.npz,
+    # made by tests/golden/make_rh_fma.py from both builds of the reference)
+    kf = tune.time_fp64(64, 100_000, 1, 0, arithmetic="fused")
+    js = tune.rh_junctions(64, 1e-8)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    engine.run_junctions(js, plan, batch.SolverMode.RK4, arithmetic="fused")
+    torch.cuda.synchronize()
+    elf = time.perf_counter() - t0
+    out["rh_config0_fp64"]["fused"] = {
+        "kernel_s": kf["best_ms"] / 1e3, "e2e_s": elf, "us_per_step": kf["us_per_step"],
+        "layer_steps_per_s_kernel": kf["layer_steps_per_s"], "all_ok": kf["all_ok"], "logs": rh_logs(js),
+        "arithmetic": "CMTJ_ARITH_FUSED: H = Hconst + A m, FMA contraction, series normalisation"}
     del js
     # Dormand-Prince: 4096 sine-driven free layers, 5 ns, adaptive steps
     js = dp_junctions(cm)

@@ -11,6 +11,7 @@ import os
 
 import numpy as np
 
+ABI_VERSION = 2  # CMTJ_ABI_VERSION
 MAX_LAYERS = 8
 ALPHA_MAX_LEN = 8388608  # CMTJ_ALPHA_MAX_LEN: samples per alpha-noise buffer
 MAX_LAYERS_F32 = 4
@@ -82,8 +83,12 @@ SIM_PARAMS_DTYPE = np.dtype(
     [("time_step", "<f8"), ("total_iterations", "<u4"), ("write_every", "<u4"), ("n_log", "<u4"),
      ("solver", "<i4"), ("calculate_energies", "<i4"), ("log_width", "<i4"),
      ("c", CONSTANTS_DTYPE), ("total_time", "<f8"), ("write_frequency", "<f8"), ("max_attempts", "<u8"),
-     ("max_layers", "<i4"), ("lanes_per_layer", "<i4")],
+     ("max_layers", "<i4"), ("lanes_per_layer", "<i4"), ("arithmetic", "<i4"), ("reserved", "<i4")],
     align=True)
+
+# enum cmtj_arithmetic
+ARITH_REFERENCE, ARITH_FUSED = 0, 1
+ARITHMETIC = {"reference": ARITH_REFERENCE, "fused": ARITH_FUSED}
 
 # Order of cmtj_struct_sizes() output.
 STRUCT_SIZES = {
@@ -172,7 +177,7 @@ def check_layout(lib):
     for (name, size), got in zip(sizes.items(), buf):
         if size != got:
             raise RuntimeError("ABI mismatch for %s: numpy %d bytes, library %d bytes" % (name, size, got))
-    if lib.cmtj_abi_version() != 1:
+    if lib.cmtj_abi_version() != ABI_VERSION:
         raise RuntimeError("unexpected libcmtj_gpu ABI version %d" % lib.cmtj_abi_version())
 
 

@@ -302,7 +302,7 @@ def alpha_noise_rows(layers, larr, plan):
     return specs_array(rows), np.asarray(which, dtype=np.int64)
 
 
-def lower(junctions, plan, solver, calculate_energies):
+def lower(junctions, plan, solver, calculate_energies, arithmetic="reference"):
     solver = SolverMode(int(solver))
     plan = plan.for_solver(solver)
     validate(junctions, solver)
@@ -320,7 +320,7 @@ def lower(junctions, plan, solver, calculate_energies):
                                  else (None, None))
     max_layers = max(j.layerNo for j in junctions)
     width = _abi.log_width(max_layers, calculate_energies)
-    params = make_params(plan, solver, calculate_energies, width, max_layers)
+    params = make_params(plan, solver, calculate_energies, width, max_layers, arithmetic)
     return Lowered(jarr, larr, tables.array(), params, width, alpha_specs, alpha_layers)
 
 
@@ -337,8 +337,15 @@ def with_alpha_buffers(lowered, base_address):
     return larr
 
 
-def make_params(plan, solver, calculate_energies, width, max_layers=0):
+def make_params(plan, solver, calculate_energies, width, max_layers=0, arithmetic="reference"):
+    """cmtj_sim_params_t of a run.  arithmetic: "reference" (the reference's
+    operations in its order: its bits) or "fused" (CMTJ_ARITH_FUSED: field-only
+    RK4 layers with constant anisotropy and IEC in fused FP64 arithmetic, not
+    bit-identical)."""
+    if arithmetic not in _abi.ARITHMETIC:
+        raise ValueError("arithmetic must be one of %s, not %r" % (sorted(_abi.ARITHMETIC), arithmetic))
     p = np.zeros(1, dtype=_abi.SIM_PARAMS_DTYPE)
+    p["arithmetic"] = _abi.ARITHMETIC[arithmetic]
     p["max_layers"] = max_layers
     p["time_step"] = plan.time_step
     p["total_iterations"] = plan.total_iterations

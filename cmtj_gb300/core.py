@@ -1039,13 +1039,18 @@ class Junction:
         return local
 
     def runSimulation(self, totalTime, timeStep=1e-13, writeFrequency=1e-11, verbose=False,
-                      calculateEnergies=False, solverMode=SolverMode.RK4):
+                      calculateEnergies=False, solverMode=SolverMode.RK4, *, arithmetic="reference"):
+        """Junction::runSimulation (junction.hpp:1948-2056).  The keyword
+        arithmetic has no counterpart in the reference: "fused" runs
+        field-only RK4 layers in fused FP64 arithmetic (cmtj_arithmetic in
+        include/cmtj_gpu.h), close to but not bit-identical with the
+        default "reference"."""
         from . import engine
         begin = _time.perf_counter()
         plan = engine.plan_run(totalTime, timeStep, writeFrequency)
         solver = self.getSolver(solverMode)
         plan = plan.for_solver(solver)
-        engine.run_junctions([self], plan, solver, bool(calculateEnergies))
+        engine.run_junctions([self], plan, solver, bool(calculateEnergies), arithmetic)
         if verbose:
             print("Steps in simulation: %d" % plan.total_iterations)
             print("Write every: %d" % plan.write_every)

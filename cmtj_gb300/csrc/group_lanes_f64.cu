@@ -50,6 +50,7 @@ __global__ void __launch_bounds__(kGroupLaneThreads)
   const int64_t off = mine_j ? junctions[gj].layer_offset : 0;
   const cmtj_layer_t &L = params[mine ? off + g.l : 0];
   const int mr_mode = mine_j ? junctions[gj].mr_mode : CMTJ_MR_NONE;
+  const double half_span = mine_j ? classic_half_span(junctions[gj]) : 0.0;
   const int ti = mine_j ? top[gj] : 0;
   const bool lead = mine_j && g.jl == 0;
   const cmtj_pair_t *row_pairs = pairs + Gr.pair_offset + (int64_t)(mine_j ? jj : 0) * N;
@@ -85,7 +86,7 @@ __global__ void __launch_bounds__(kGroupLaneThreads)
     if (s_nan) break;
     if (!(i % p.write_every)) {
       lane_log_row(mine_j ? log + ((size_t)gj * p.n_log + row) * p.log_width : nullptr, mine_j && n > 0, mine,
-                   junctions, gj, L, mag, side, g, n, G, mr_mode, false, t);
+                   junctions, gj, L, mag, side, g, n, G, mr_mode, false, t, half_span);
       ++row;
     }
   }

@@ -7,10 +7,12 @@
 // three products gathered from the quad, a cross product component is
 // a_i*b_j - a_j*b_i from the quad's other two lanes, and a tensor row is
 // (t0*mx + t1*my) + t2*mz.  Values therefore do not depend on the layout.
-// A step is bound by the latency of its dependent chain, and idle lanes
-// cost little, so spreading the components cuts the FP64 instructions on
-// the chain about 2.5-fold for a few shuffles.  The lanes of a quad always take the same branches (they hold
-// one layer), so the quad-masked shuffles below are always converged.
+// A step is bound by its warp's FP64 instructions (each holds the SM
+// sub-partition's FP64 pipe for about 64 cycles on GB300, whatever the lane
+// mask), so spreading the components cuts a step's FP64 instructions about
+// 2.5-fold for a few shuffles.  The lanes of a quad always take the same
+// branches (they hold one layer), so the quad-masked shuffles below are
+// always converged.
 #pragma once
 #include "plain_f64.cuh"
 
@@ -85,9 +87,15 @@ static __device__ __forceinline__ void store3(double *dst, const D3 &a) {
 static __device__ __forceinline__ bool scalar_owner(const C3 &) { return (threadIdx.x & 3) == 0; }
 static __device__ __forceinline__ bool scalar_owner(const D3 &) { return true; }
 
+// isnan(v) as an integer test on the bits (exponent all ones, mantissa
+// non-zero), which takes no FP64 pipe slot.
+static __device__ __forceinline__ bool nan_bits(double v) {
+  return ((unsigned long long)__double_as_longlong(v) << 1) > 0xffe0000000000000ull;
+}
+
 // isnan of the x component, true on the lane that holds it.
-static __device__ __forceinline__ bool x_is_nan(const C3 &a) { return (threadIdx.x & 3) == 0 && isnan(a.v); }
-static __device__ __forceinline__ bool x_is_nan(const D3 &a) { return isnan(a.x); }
+static __device__ __forceinline__ bool x_is_nan(const C3 &a) { return (threadIdx.x & 3) == 0 && nan_bits(a.v); }
+static __device__ __forceinline__ bool x_is_nan(const D3 &a) { return nan_bits(a.x); }
 
 // isnan of the x component, on every lane of the quad.
 static __device__ __forceinline__ bool x_nan_all(const C3 &a) {

@@ -137,6 +137,10 @@ extern "C" int cmtj_run_simulation_f64(const cmtj_junction_t *d_junctions, int32
     cmtj_set_error("cmtj_run_simulation_f64: unknown solver %d", p->solver);
     return CMTJ_ERR_ARG;
   }
+  if (p->arithmetic != CMTJ_ARITH_REFERENCE && p->arithmetic != CMTJ_ARITH_FUSED) {
+    cmtj_set_error("cmtj_run_simulation_f64: unknown arithmetic %d", p->arithmetic);
+    return CMTJ_ERR_ARG;
+  }
   if (p->solver == CMTJ_DORMAND_PRINCE &&
       !(p->write_frequency > 0 && p->time_step > 0 && p->total_time >= 0 && p->max_attempts > 0)) {
     cmtj_set_error("cmtj_run_simulation_f64: Dormand-Prince needs time_step > 0, write_frequency > 0, "

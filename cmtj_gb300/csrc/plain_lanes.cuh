@@ -135,6 +135,135 @@ __device__ __forceinline__ V rhs_field_only(const FieldOnly<V> &f, const cmtj_la
   return dmdt * -f.gyro * f.conv;
 }
 
+// ---- CMTJ_ARITH_FUSED: field-only RK4 layers ------------------------------
+// On GB300 every FP64 warp instruction holds its SM sub-partition's FP64
+// pipe for about 64 cycles whatever the lane mask, and independent FP64
+// instructions of one warp do not overlap, so a step costs about 64 cycles
+// per FP64 instruction on its warp.  The reference's operation order needs
+// about 290 per RK4 step of a field-only layer (four divisions by Ms, the
+// IEC division, the division by 6, a square root and a division in the
+// normalisation, each a sequence of about nine).  With constant anisotropy
+// and IEC, calculateHeff of such a layer is affine in m:
+//   H = Hext + Hoe + Hdmi + Hres + Hiec + A m,
+//   A = (2K/Ms) k k^T - N Ms/mu0,
+// so the fused form evaluates it as three FMAs per component from a matrix
+// formed once per run, with g = -gyro * convTerm * dt folded into A and the
+// constant field so that k = dt * dm/dt = p + damping * (m x p), p = m x gH.
+// About 50 FP64 instructions per step.
+
+// a * s + b, one rounding per component.
+static __device__ __forceinline__ C3 fmav(const C3 &a, double s, const C3 &b) { return C3{fma(a.v, s, b.v)}; }
+static __device__ __forceinline__ D3 fmav(const D3 &a, double s, const D3 &b) {
+  return d3(fma(a.x, s, b.x), fma(a.y, s, b.y), fma(a.z, s, b.z));
+}
+// a x b, each component a_i b_j - a_j b_i as fma(a_i, b_j, -(a_j b_i)).
+static __device__ __forceinline__ C3 cross_fused(const C3 &a, const C3 &b) {
+  const int c = quad_comp();
+  const int i = c == 2 ? 0 : c + 1, j = c == 0 ? 2 : c - 1;
+  const double ai = quad_get(a.v, i), aj = quad_get(a.v, j), bi = quad_get(b.v, i), bj = quad_get(b.v, j);
+  return C3{fma(ai, bj, -(aj * bi))};
+}
+static __device__ __forceinline__ D3 cross_fused(const D3 &a, const D3 &b) {
+  return d3(fma(a.y, b.z, -(a.z * b.y)), fma(a.z, b.x, -(a.x * b.z)), fma(a.x, b.y, -(a.y * b.x)));
+}
+
+// v / |v| (CVector::normalize, cvector.hpp:185-192) with 1/|v| from the
+// series 1 - e/2 + 3e^2/8 in e = |v|^2 - 1: the first omitted term is below
+// 2^-54 for |e| < 2^-27 (two terms) and below 0.6 ulp for |e| < 2^-17 (three
+// terms); beyond that 1/|v| is rsqrt(|v|^2).  A zero vector is returned as
+// is.  The range tests read the exponent bits of e (integer instructions).
+// Every lane of a C3 quad forms the same s, so the quad branches together.
+template <class V>
+__device__ __forceinline__ V normalized_fused(const V &v) {
+  const double x = comp_of(v, 0), y = comp_of(v, 1), z = comp_of(v, 2);
+  const double s = fma(z, z, fma(y, y, x * x));
+  const double e = s - 1.0;
+  const unsigned ex = (unsigned)((unsigned long long)__double_as_longlong(e) >> 52) & 0x7ffu;
+  double r;
+  if (ex < 1023u - 27u) {
+    r = fma(e, -0.5, 1.0);
+  } else if (ex < 1023u - 17u) {
+    r = fma(e, fma(e, 0.375, -0.5), 1.0);
+  } else {
+    if ((__double_as_longlong(s) & 0x7fffffffffffffffll) == 0) return v;
+    r = rsqrt(s);
+  }
+  return v * r;
+}
+
+// The per-run constants of a fused field-only layer: the columns of g A,
+// g times the constant field slots, g Jbottom/(Ms t), g Jtop/(Ms t).
+template <class V>
+struct Fused {
+  V a0, a1, a2, gHc;
+  double gcb, gct, g, alpha;
+};
+
+template <class V>
+__device__ __forceinline__ Fused<V> fused_load(const FieldOnly<V> &f, double dt) {
+  Fused<V> u;
+  const double g = -f.gyro * f.conv * dt;
+  const double kk = (2 * f.K) / f.Ms;
+  const double ax = comp_of(f.anis, 0), ay = comp_of(f.anis, 1), az = comp_of(f.anis, 2);
+  const double *N = f.demag;
+  u.a0 = (f.anis * (kk * ax) - V::make(N[0], N[3], N[6]) * f.ms_mu0) * g;
+  u.a1 = (f.anis * (kk * ay) - V::make(N[1], N[4], N[7]) * f.ms_mu0) * g;
+  u.a2 = (f.anis * (kk * az) - V::make(N[2], N[5], N[8]) * f.ms_mu0) * g;
+  u.gHc = (f.Hext + f.Hoe + f.Hdmi + f.Hres) * g;
+  u.gcb = g * (f.Jb / f.Mst);
+  u.gct = g * (f.Jt / f.Mst);
+  u.g = g;
+  u.alpha = f.damping;
+  return u;
+}
+
+// One RK4 step (Layer::rk4_step, junction.hpp:1017-1041, neighbours frozen
+// as in runMultiLayerSolver 1680-1707) of a fused field-only layer.  DYN:
+// the field slots are read at each stage time.  Returns as lane_step does.
+template <class V, bool DYN>
+__device__ __forceinline__ int lane_step_fused(const cmtj_layer_t &L, const Fused<V> &u, V &mag, bool step,
+                                               const LaneGeo &g, int n, uint32_t i, double t, double dt,
+                                               const double *tables, uint32_t dyn) {
+  V below = shfl_vec(mag, g.below_src), above = shfl_vec(mag, g.above_src);
+  if (g.l == 0) below = V::zero();
+  if (g.l >= n - 1) above = V::zero();
+  V next = mag;
+  bool nan = false;
+  if (step) {
+    const V giec = fmav(above, u.gct, below * u.gcb);
+    const V gs = DYN ? V::zero() : u.gHc + giec;
+    V k = V::zero(), acc = V::zero(), mi = mag;
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+      V gh = gs;
+      if (DYN) {
+        const double ts = s == 0 ? t : (s == 3 ? t + dt : t + 0.5 * dt);
+        const DriverCtx dc = {tables, i, s == 0 ? 0 : (s == 3 ? 2 : 1)};
+        const V Hc = V::axial(L, CMTJ_SLOT_HEXT, ts, dc, dyn) + V::axial(L, CMTJ_SLOT_HOE, ts, dc, dyn) +
+                     V::axial(L, CMTJ_SLOT_HDMI, ts, dc, dyn) + V::axial(L, CMTJ_SLOT_HRES, ts, dc, dyn);
+        gh = fmav(Hc, u.g, giec);
+      }
+      const double mx = comp_of(mi, 0), my = comp_of(mi, 1), mz = comp_of(mi, 2);
+      const V h = fmav(u.a2, mz, fmav(u.a1, my, fmav(u.a0, mx, gh)));
+      const V p = cross_fused(mi, h);
+      const V p2 = cross_fused(mi, p);
+      k = fmav(p2, u.alpha, p);
+      acc = s == 0 ? k : (s == 3 ? acc + k : fmav(k, 2.0, acc));
+      mi = s < 2 ? fmav(k, 0.5, mag) : mag + k;
+    }
+    next = normalized_fused(fmav(acc, 1.0 / 6.0, mag));
+    nan = x_is_nan(next);
+  }
+  const unsigned bad = __ballot_sync(kWarpAll, nan) & g.group;
+  if (bad) {
+    const int first = (__ffs(bad) - 1 - g.lead) / V::kLanes;
+    if (step && g.l <= first) mag = next;
+    return first;
+  }
+  if (step) mag = next;
+  return -1;
+}
+
 // One iteration of the fixed-step runner (RK4, Euler-Heun or Heun;
 // core/junction.hpp:1668-1815) for the lane's layer of a junction whose
 // n layers step (1 under runSingleLayerSolver).  cur overrides the current
@@ -263,31 +392,43 @@ __device__ __forceinline__ double classic_cos(const cmtj_layer_t &L, const V &ma
   return n == 1 ? cref : c01;
 }
 
+// (Rap - Rp) / 2.0 of calculateMagnetoresistance (junction.hpp:1865-1867),
+// the same value on every call: kernels form it once per junction.
+__device__ __forceinline__ double classic_half_span(const cmtj_junction_t &J) { return (J.Rap - J.Rp) / 2.0; }
+
 // One log row of the junction (logLayerParams, junction.hpp:1580-1636, and
 // the R columns of stripMagnetoResistance 1835-1857).  write: the junction
-// logs this step (the same on all its lanes); mine: the lane holds a layer.
+// logs this step (the same on all its lanes); mine: the lane holds a layer;
+// half_span: classic_half_span() of the junction.
 template <class V>
 __device__ __forceinline__ void lane_log_row(double *r, bool write, bool mine, const cmtj_junction_t *junctions,
                                              int j, const cmtj_layer_t &L, const V &mag, const SideT<V> &side,
-                                             const LaneGeo &g, int n, int G, int mr_mode, bool energies, double t) {
+                                             const LaneGeo &g, int n, int G, int mr_mode, bool energies, double t,
+                                             double half_span) {
   const int width = energies ? CMTJ_ENERGY_COLS : 3;
-  const double cosT = classic_cos(L, mag, g, n, G, write && g.l == 0);
-  const double mx = comp_of(mag, 0), my = comp_of(mag, 1), mz = comp_of(mag, 2);
-  double inv_x = 0.0, inv_y = 0.0;
-  if (write && mine && mr_mode == CMTJ_MR_STRIP) {
-    const cmtj_junction_t &J = junctions[j];
-    const double Rx = J.Rx0[g.l] + J.AMR_X[g.l] * (mx * mx) + J.SMR_X[g.l] * (my * my);
-    const double Ry = J.Ry0[g.l] + 0.5 * J.AHE[g.l] * mz + (J.AMR_Y[g.l] + J.SMR_Y[g.l]) * mx * my;
-    inv_x = 1. / Rx;
-    inv_y = 1. / Ry;
-  }
+  // each MR form only when some junction of the warp logs it now (the
+  // warp-wide shuffles inside stay converged)
+  const double cosT = __any_sync(kWarpAll, write && mr_mode == CMTJ_MR_CLASSIC)
+                          ? classic_cos(L, mag, g, n, G, write && g.l == 0)
+                          : 0.0;
   double Rx_acc = 0.0, Ry_acc = 0.0;
-  for (int q = 0; q < G; ++q) {
-    const double a = __shfl_sync(kWarpAll, inv_x, g.lead + q * V::kLanes);
-    const double b = __shfl_sync(kWarpAll, inv_y, g.lead + q * V::kLanes);
-    if (q < n) {
-      Rx_acc = Rx_acc + a;
-      Ry_acc = Ry_acc + b;
+  if (__any_sync(kWarpAll, write && mr_mode == CMTJ_MR_STRIP)) {
+    const double mx = comp_of(mag, 0), my = comp_of(mag, 1), mz = comp_of(mag, 2);
+    double inv_x = 0.0, inv_y = 0.0;
+    if (write && mine && mr_mode == CMTJ_MR_STRIP) {
+      const cmtj_junction_t &J = junctions[j];
+      const double Rx = J.Rx0[g.l] + J.AMR_X[g.l] * (mx * mx) + J.SMR_X[g.l] * (my * my);
+      const double Ry = J.Ry0[g.l] + 0.5 * J.AHE[g.l] * mz + (J.AMR_Y[g.l] + J.SMR_Y[g.l]) * mx * my;
+      inv_x = 1. / Rx;
+      inv_y = 1. / Ry;
+    }
+    for (int q = 0; q < G; ++q) {
+      const double a = __shfl_sync(kWarpAll, inv_x, g.lead + q * V::kLanes);
+      const double b = __shfl_sync(kWarpAll, inv_y, g.lead + q * V::kLanes);
+      if (q < n) {
+        Rx_acc = Rx_acc + a;
+        Ry_acc = Ry_acc + b;
+      }
     }
   }
   if (!write) return;
@@ -296,7 +437,7 @@ __device__ __forceinline__ void lane_log_row(double *r, bool write, bool mine, c
     const cmtj_junction_t &J = junctions[j];
     double r0 = 0.0, r1 = 0.0;
     if (mr_mode == CMTJ_MR_CLASSIC) {
-      r0 = J.Rp + (((J.Rap - J.Rp) / 2.0) * (1.0 - cosT));
+      r0 = J.Rp + (half_span * (1.0 - cosT));
     } else if (mr_mode == CMTJ_MR_STRIP) {
       r0 = 1 / Rx_acc;
       r1 = 1 / Ry_acc;

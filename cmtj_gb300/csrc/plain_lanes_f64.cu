@@ -14,19 +14,24 @@
 // depend on the layout.  The serial chain of a step is one layer's instead
 // of n layers'.
 //
-// A step is bound by the latency of its dependent chain of FP64 operations
-// and shuffles, not by the FP64 pipe, and idle lanes cost little, so the
-// quad layout, with about 2.5x fewer FP64 instructions on the chain, is the
-// faster one until the batch fills the GPU.
+// A step is bound by its warp's FP64 instructions: on GB300 each holds the
+// SM sub-partition's FP64 pipe for about 64 cycles whatever the lane mask,
+// and a warp's independent FP64 instructions do not overlap.  Idle lanes
+// therefore cost nothing, and the quad layout, with about 2.5x fewer FP64
+// instructions per step, is the faster one until the batch fills the GPU.
 // A block is one warp; blocks spread over the SMs.  Driver slots whose
 // driver is constant are read directly (slot mask per lane), and the four
 // RK4 stages run as a rolled loop so the field code is compiled once per
 // kernel.  A warp whose layers are all field-only (RK4) runs a variant
 // without the per-term branches, with the layer constants in registers and
 // the IEC term formed once per step; its field and anisotropy drivers may
-// be time-dependent.
+// be time-dependent.  Under CMTJ_ARITH_FUSED such a warp, if its
+// anisotropy and IEC drivers are constant, runs lane_step_fused instead
+// (plain_lanes.cuh): not the reference's bits, about a sixth of the FP64
+// instructions.
 //
-// This unit is compiled with --fmad=false like plain_f64.cu.
+// This unit is compiled with --fmad=false like plain_f64.cu; the fused step
+// calls fma() explicitly.
 #include "plain_lanes.cuh"
 #include "plain_lanes.h"
 
@@ -38,8 +43,10 @@ namespace {
 // warp has a time-dependent driver slot: every slot then reads its
 // constantValue, a loop invariant.  FIELD (RK4): every layer of the warp is
 // field-only (FieldOnly), with its constants in registers; with DYN, its
-// field and anisotropy drivers may be time-dependent.
-template <int SOLVER, class V, bool DYN, bool FIELD>
+// field and anisotropy drivers may be time-dependent.  FUSED (with FIELD):
+// the CMTJ_ARITH_FUSED step (lane_step_fused); only the field drivers may
+// then be time-dependent.
+template <int SOLVER, class V, bool DYN, bool FIELD, bool FUSED = false>
 __device__ __forceinline__ void run_lanes(const cmtj_junction_t *__restrict__ junctions, int32_t n_junctions,
                                           const cmtj_layer_t *params, cmtj_layer_t *layers,
                                           const double *__restrict__ tables, const cmtj_sim_params_t &p, int G,
@@ -51,10 +58,12 @@ __device__ __forceinline__ void run_lanes(const cmtj_junction_t *__restrict__ ju
   int64_t off = 0;
   uint32_t code = CMTJ_STATUS_OK;
   int mr_mode = CMTJ_MR_NONE;
+  double half_span = 0.0;
   if (have) {
     n = junctions[j].n_layers;
     off = junctions[j].layer_offset;
     mr_mode = junctions[j].mr_mode;
+    half_span = classic_half_span(junctions[j]);
     if (n < 1 || n > G) {
       code = CMTJ_STATUS_BAD_INPUT;
       n = 0;
@@ -77,22 +86,27 @@ __device__ __forceinline__ void run_lanes(const cmtj_junction_t *__restrict__ ju
   }
   FieldOnly<V> fo;
   if (FIELD) fo = field_only_load<V>(L, c);
+  Fused<V> fu;
+  if (FUSED) fu = fused_load<V>(fo, dt);
   double *out = have ? log + (size_t)j * p.n_log * p.log_width : nullptr;
   uint32_t row = 0;
 
   for (uint32_t i = 0; i < p.total_iterations; ++i) {
     if (!__any_sync(kWarpAll, run)) break;
     const double t = (double)i * dt;
-    const int first =
-        lane_step<SOLVER, V, DYN && FIELD>(L, c, mag, side, mine && run, g, n, i, t, dt, tables, energies, nullptr,
-                                           dyn, nullptr, FIELD ? &fo : nullptr);
+    int first;
+    if constexpr (FUSED)
+      first = lane_step_fused<V, DYN>(L, fu, mag, mine && run, g, n, i, t, dt, tables, dyn);
+    else
+      first = lane_step<SOLVER, V, DYN && FIELD>(L, c, mag, side, mine && run, g, n, i, t, dt, tables, energies,
+                                                 nullptr, dyn, nullptr, FIELD ? &fo : nullptr);
     if (first >= 0) {
       if (run) code = CMTJ_STATUS_NAN;
       run = false;
     }
     if (!(i % p.write_every)) {
       lane_log_row(run ? out + (size_t)row * p.log_width : nullptr, run, mine, junctions, j, L, mag, side, g, n, G,
-                   mr_mode, energies, t);
+                   mr_mode, energies, t, half_span);
       if (run) ++row;
     }
   }
@@ -115,7 +129,7 @@ __global__ void __launch_bounds__(32)
   const int lane = threadIdx.x;
   const int l = (lane % span) / V::kLanes;
   const int j = blockIdx.x * (32 / span) + lane / span;
-  bool varying = false, general = false;
+  bool varying = false, general = false, unfused = false;
   if (j < n_junctions) {
     const int n = junctions[j].n_layers;
     if (l < n && n <= G) {
@@ -123,10 +137,18 @@ __global__ void __launch_bounds__(32)
       const uint32_t dyn = dynamic_slots(L);
       varying = dyn != 0u;
       general = !field_only(L) || (dyn & kFieldOnlyFixedSlots) != 0u;
+      unfused = general || (dyn & (1u << CMTJ_SLOT_ANIS)) != 0u;
     }
   }
   const bool dyn = __any_sync(kWarpAll, varying);
   if constexpr (SOLVER == CMTJ_RK4) {
+    if (p.arithmetic == CMTJ_ARITH_FUSED && !p.calculate_energies && !__any_sync(kWarpAll, unfused)) {
+      if (dyn)
+        run_lanes<SOLVER, V, true, true, true>(junctions, n_junctions, params, layers, tables, p, G, log, status);
+      else
+        run_lanes<SOLVER, V, false, true, true>(junctions, n_junctions, params, layers, tables, p, G, log, status);
+      return;
+    }
     if (!__any_sync(kWarpAll, general)) {
       if (dyn)
         run_lanes<SOLVER, V, true, true>(junctions, n_junctions, params, layers, tables, p, G, log, status);

@@ -50,6 +50,7 @@ __global__ void __launch_bounds__(kStackLaneThreads)
   const int64_t off = mine_j ? junctions[gj].layer_offset : 0;
   const cmtj_layer_t &L = params[mine ? off + g.l : 0];
   const int mr_mode = mine_j ? junctions[gj].mr_mode : CMTJ_MR_NONE;
+  const double half_span = mine_j ? classic_half_span(junctions[gj]) : 0.0;
   const int top_i = mine_j ? top_bottom[2 * gj] : 0, bot_i = mine_j ? top_bottom[2 * gj + 1] : -1;
   const double *cs = couplings + S.coupling_offset;
   const cmtj_constants_t c = p.c;
@@ -100,7 +101,7 @@ __global__ void __launch_bounds__(kStackLaneThreads)
       if (lead) {
         if (first >= 0) atomicExch(&s_nan, 1);
         const cmtj_junction_t &J = junctions[gj];
-        s_R[jj] = J.Rp + (((J.Rap - J.Rp) / 2.0) * (1.0 - cosT));
+        s_R[jj] = J.Rp + (half_span * (1.0 - cosT));
         s_I[jj] = s_total;
       }
     } else if (S.delayed) {
@@ -129,7 +130,7 @@ __global__ void __launch_bounds__(kStackLaneThreads)
       if (lead) {
         if (first >= 0) atomicExch(&s_nan, 1);
         const cmtj_junction_t &J = junctions[gj];
-        s_R[jj] = J.Rp + (((J.Rap - J.Rp) / 2.0) * (1.0 - cosT));
+        s_R[jj] = J.Rp + (half_span * (1.0 - cosT));
         s_I[jj] = drv(cur, t, dc0);
       }
     } else {
@@ -159,7 +160,7 @@ __global__ void __launch_bounds__(kStackLaneThreads)
         if (me && g.jl == 0) {
           if (first >= 0) atomicExch(&s_nan, 1);
           const cmtj_junction_t &J = junctions[gj];
-          s_R[k] = J.Rp + (((J.Rap - J.Rp) / 2.0) * (1.0 - cosT));
+          s_R[k] = J.Rp + (half_span * (1.0 - cosT));
           s_I[k] = drv(cur, t, dc0);
         }
         // the next junction reads this one's updated top/bottom layers
@@ -189,7 +190,7 @@ __global__ void __launch_bounds__(kStackLaneThreads)
         sr[2 * N] = t;
       }
       lane_log_row(mine_j ? log + ((size_t)gj * p.n_log + row) * p.log_width : nullptr, mine_j && n > 0, mine,
-                   junctions, gj, L, mag, side, g, n, G, mr_mode, false, t);
+                   junctions, gj, L, mag, side, g, n, G, mr_mode, false, t, half_span);
       ++row;
     }
     __syncthreads();

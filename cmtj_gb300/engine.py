@@ -115,11 +115,12 @@ def run_lowered_f64(lowered, stream=None):
     return log, status, layers
 
 
-def run_junctions(junctions, plan, solver, calculate_energies=False):
+def run_junctions(junctions, plan, solver, calculate_energies=False, arithmetic="reference"):
     """Junction::runSimulation for a list of junctions sharing one plan
-    (each junction keeps its own layers, drivers and log)."""
+    (each junction keeps its own layers, drivers and log).  arithmetic:
+    "reference" (the reference's bits) or "fused" (cmtj_arithmetic)."""
     plan = plan.for_solver(solver)
-    lowered = lower(junctions, plan, solver, calculate_energies)
+    lowered = lower(junctions, plan, solver, calculate_energies, arithmetic)
     require_gpu()
     log, status, layers = run_lowered_f64(lowered)
     lowered.layers = layers

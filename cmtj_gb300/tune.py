@@ -136,7 +136,7 @@ def rh_junctions(n, total):
     return js
 
 
-def time_fp64(n, steps, reps, lanes, dt=1e-13):
+def time_fp64(n, steps, reps, lanes, dt=1e-13, arithmetic="reference"):
     """Best-of-`reps` CUDA-event time of one cmtj_run_simulation_f64 launch
     (after one warm-up launch) on the R(H) batch of n junctions."""
     import numpy as np
@@ -145,7 +145,7 @@ def time_fp64(n, steps, reps, lanes, dt=1e-13):
     from ._lower import lower, plan_run
     from .core import SolverMode
     plan = plan_run(steps * dt, dt, dt).for_solver(SolverMode.RK4)
-    low = lower(rh_junctions(n, steps * dt), plan, SolverMode.RK4, False)
+    low = lower(rh_junctions(n, steps * dt), plan, SolverMode.RK4, False, arithmetic)
     low.params["lanes_per_layer"] = lanes
     lib = engine.require_gpu()
     d_j, d_l0 = engine.to_device(low.junctions), engine.to_device(low.layers)
@@ -167,7 +167,8 @@ def time_fp64(n, steps, reps, lanes, dt=1e-13):
             times.append(a.elapsed_time(b))
     st = d_st.cpu().numpy().view(np.uint32)
     best = min(times)
-    return {"workload": "fp64_rh", "n": n, "lanes_per_layer": lanes, "steps": steps, "ms": times, "best_ms": best,
+    return {"workload": "fp64_rh", "n": n, "lanes_per_layer": lanes, "arithmetic": arithmetic, "steps": steps,
+            "ms": times, "best_ms": best,
             "us_per_step": best * 1e3 / steps, "layer_steps_per_s": n * steps * 2 / (best / 1e3),
             "all_ok": bool(np.all(st[0::2] == 0) and np.all(st[1::2] == steps))}
 
@@ -184,6 +185,8 @@ def main(argv=None):
     ap.add_argument("--fp64", action="store_true", help="time the FP64 fixed-step lane layouts instead")
     ap.add_argument("--n", type=int, nargs="+", default=[1, 64, 1024, 16384], help="--fp64 batch sizes")
     ap.add_argument("--lanes", type=int, nargs="+", default=[0, 1, 4], help="--fp64 lanes per layer")
+    ap.add_argument("--arithmetic", nargs="+", default=["reference"], choices=["reference", "fused"],
+                    help="--fp64 arithmetic (cmtj_arithmetic)")
     ap.add_argument("--vsd-shape", type=float, nargs=4, default=[128, 1024, 5.0, 50.0],
                     metavar=("FREQS", "FIELDS", "T_MIN_NS", "T_MAX_NS"),
                     help="spin-diode sweep: frequencies x fields, durations uniform in [T_MIN, T_MAX] ns")
@@ -193,7 +196,8 @@ def main(argv=None):
         B.build()
         for n in a.n:
             for lanes in a.lanes:
-                print(json.dumps(time_fp64(n, a.steps, a.reps, lanes)), flush=True)
+                for arith in a.arithmetic:
+                    print(json.dumps(time_fp64(n, a.steps, a.reps, lanes, arithmetic=arith)), flush=True)
         return
     if a.time_lib:
         print(json.dumps(time_library(a.time_lib, a.n_h, a.n_draw, a.steps, a.reps, a.workload,

@@ -22,7 +22,7 @@
 extern "C" {
 #endif
 
-#define CMTJ_ABI_VERSION 1
+#define CMTJ_ABI_VERSION 2
 #define CMTJ_MAX_LAYERS 8        /* FP64 plain form: layers per junction   */
 #define CMTJ_MAX_LAYERS_F32 4    /* FP32 batched form: layers per junction */
 
@@ -208,7 +208,27 @@ typedef struct cmtj_sim_params {
                                 x, y, z on three lanes); 0: the library picks 4
                                 for batches up to two quad warps per SM
                                 sub-partition, else 1.  Results are the same. */
+  int32_t arithmetic;        /* enum cmtj_arithmetic                         */
+  int32_t reserved;          /* 0                                            */
 } cmtj_sim_params_t;
+
+/* How cmtj_run_simulation_f64 evaluates fixed-step RK4 layers.
+ *   CMTJ_ARITH_REFERENCE  the reference's operations in its order, no FMA
+ *                         contraction: the reference's bits (the default).
+ *   CMTJ_ARITH_FUSED      a warp whose layers are all field-only (no dipole,
+ *                         IDMI, K2, biquadratic IEC, STT or SOT) with constant
+ *                         anisotropy and IEC drivers, and without
+ *                         calculate_energies, forms the field as
+ *                         H = Hconst + A m (A = (2K/Ms) k k^T - N Ms/mu0, one
+ *                         constant matrix per layer), contracts products into
+ *                         FMAs and normalises |m| by a series in |m|^2 - 1.
+ *                         Each result differs from the reference's in the last
+ *                         bits; the difference a run accumulates depends on
+ *                         how sensitive its trajectory is (the library's tests
+ *                         state the bound they check).  Other warps, other
+ *                         solvers, stacks and groups use the reference
+ *                         arithmetic. */
+enum cmtj_arithmetic { CMTJ_ARITH_REFERENCE = 0, CMTJ_ARITH_FUSED = 1 };
 
 /* Log row layout (per junction, per row): for each layer l, either 3
  * doubles (mx, my, mz) or, with calculate_energies, CMTJ_ENERGY_COLS doubles

@@ -74,3 +74,25 @@ def test_f32_batch_rejects_chunk_inside_a_log_tile(lib):
         rc = lib.cmtj_batch_run_f32(dummy, dummy, dummy, dummy, 1, 1, 0, p.ctypes.data, dummy, dummy, 0, None)
         assert rc == _abi.CMTJ_ERR_ARG, chunk
         assert "not a multiple of log_every * log_tile = 40" in _abi.last_error(lib)
+
+
+def test_f64_rejects_unknown_arithmetic(lib):
+    """cmtj_sim_params_t.arithmetic outside enum cmtj_arithmetic is refused
+    before any device work (no GPU needed), and the Python lowering refuses
+    an unknown name."""
+    import ctypes
+    import numpy as np
+    import pytest
+    from cmtj_gb300 import _abi, _lower
+    p = np.zeros(1, dtype=_abi.SIM_PARAMS_DTYPE)
+    p["solver"] = 0  # RK4
+    p["write_every"] = 1
+    p["arithmetic"] = 7
+    dummy = ctypes.c_void_p(16)
+    rc = lib.cmtj_run_simulation_f64(dummy, 1, dummy, None, p.ctypes.data, dummy, dummy, None)
+    assert rc == _abi.CMTJ_ERR_ARG
+    assert "unknown arithmetic 7" in _abi.last_error(lib)
+    plan = _lower.plan_run(1e-12, 1e-13, 1e-13)
+    with pytest.raises(ValueError, match="arithmetic"):
+        _lower.make_params(plan, 0, False, 10, 2, "fast")
+    assert int(_lower.make_params(plan, 0, False, 10, 2, "fused")["arithmetic"][0]) == _abi.ARITH_FUSED

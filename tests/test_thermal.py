@@ -149,3 +149,19 @@ def test_oracle_alpha_noise_switching_matches_reference():
         k = sum(ex.map(one, range(n)))
     ok, d, b = binomial_ok(k, n, int(sw[q]), int(runs[q]))
     assert ok, (k / n, sw[q] / runs[q], d, b)
+
+
+def test_rh_fma_spread_fixture():
+    """The committed spread of the FMA-built reference on the R(H) sweep
+    (tests/golden/make_rh_fma.py): 64 fields over +-800 kA/m; the builds
+    agree to 1e-10 except near the switching fields of the free layer, and
+    the sweep is symmetric in H, so mirrored fields move alike."""
+    import os
+    import numpy as np
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "rh_fma_spread.npz"))
+    assert np.array_equal(d["fields"], np.linspace(-800e3, 800e3, 64))
+    dm = d["max_abs_dm"]
+    assert np.all(np.isfinite(dm)) and np.all(dm >= 0)
+    rough = set(np.flatnonzero(dm > 1e-10).tolist())
+    assert rough == {27, 28, 35, 36}, rough
+    assert np.allclose(dm, dm[::-1], rtol=0.5, atol=1e-10)
