@@ -353,12 +353,18 @@ def main():
     ap.add_argument("--profile-alpha", action="store_true",
                     help="the alpha-noise generator alone: 192 buffers of 100,000 samples, a warm-up call and one "
                          "timed call (for ncu captures)")
+    ap.add_argument("--profile-fft", type=int, metavar="ROWS", default=0,
+                    help="the spectrum kernel alone on ROWS log rows of the benchmark's shape (5000 samples, "
+                         "4096-point FFT, the benchmark's bins): a warm-up call and three timed calls")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference_arm(args)
         return
     if args.profile_alpha:
         profile_alpha()
+        return
+    if args.profile_fft:
+        profile_fft(args.profile_fft)
         return
 
     import torch
@@ -564,6 +570,42 @@ def profile_alpha(rows=192, n=100_000):
     ms = a.elapsed_time(b)
     print(json.dumps({"alpha_noise_generator": {"rows": rows, "samples": n, "ms": ms,
                                                 "samples_per_s": rows * n / (ms / 1e3)}}))
+
+
+def profile_fft(rows, samples=5000):
+    """cmtj_spectrum_f32 alone on `rows` seeded Gaussian rows of `samples`
+    floats (the benchmark's log rows: 5000 samples, the last 4096
+    transformed, the benchmark's bins): one warm-up call, three calls timed
+    with CUDA events, each after writing a buffer larger than L2."""
+    import torch
+    from cmtj_gb300 import _abi, engine
+    lib = engine.require_gpu()
+    g = torch.Generator(device="cuda")
+    g.manual_seed(5)
+    series = torch.randn((rows, samples), generator=g, device="cuda", dtype=torch.float32)
+    b_lo, b_hi = fft_bins()
+    out = torch.empty((rows, b_hi - b_lo), device="cuda", dtype=torch.float32)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def call():
+        rc = lib.cmtj_spectrum_f32(engine.ptr(series), samples, rows, samples, N_FFT, b_lo, b_hi, engine.ptr(out),
+                                   engine.stream_ptr())
+        _abi.check(rc, lib)
+
+    call()
+    ms = []
+    for _ in range(3):
+        flush.fill_(1)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        call()
+        b.record()
+        torch.cuda.synchronize()
+        ms.append(a.elapsed_time(b))
+    nbytes = 4.0 * rows * (N_FFT + (b_hi - b_lo))
+    print(json.dumps({"spectrum": {"rows": rows, "n_fft": N_FFT, "bins": b_hi - b_lo, "ms": ms,
+                                   "algorithmic_bytes": nbytes, "gbs": nbytes / (min(ms) / 1e3) / 1e9,
+                                   "checksum": float(out.double().sum())}}))
 
 
 def build_peak_probe():
