@@ -476,29 +476,35 @@ def main():
                                    engine.ptr(out), engine.stream_ptr())
         _abi.check(rc, lib)
 
-    def e2e_step(k):
+    marks = []  # per timed step: (upload start, upload end, compute start, compute end, download start, end)
+
+    def e2e_step(k, timed=False):
         q = k % 2
         r = runs[q]
+        ev = [torch.cuda.Event(enable_timing=timed) for _ in range(6)]
         with torch.cuda.stream(up_stream):
             if out_done[q] is not None:
                 up_stream.wait_event(out_done[q])
+            ev[0].record(up_stream)
             r.d_j.copy_(h_j, non_blocking=True)
             r.d_l.copy_(h_l, non_blocking=True)
-            inputs = torch.cuda.Event()
-            inputs.record(up_stream)
-        stream.wait_event(inputs)
+            ev[1].record(up_stream)
+        stream.wait_event(ev[1])
         with torch.cuda.stream(stream):
+            ev[2].record(stream)
             r.d_s.copy_(state0)
             r.launch(stream=stream)
             spectrum_of(r, specs[q])
-            computed = torch.cuda.Event()
-            computed.record(stream)
+            ev[3].record(stream)
         with torch.cuda.stream(down_stream):
-            down_stream.wait_event(computed)
+            down_stream.wait_event(ev[3])
+            ev[4].record(down_stream)
             h_specs[q].copy_(specs[q], non_blocking=True)
             h_states[q].copy_(r.d_s, non_blocking=True)
-            out_done[q] = torch.cuda.Event()
-            out_done[q].record(down_stream)
+            ev[5].record(down_stream)
+            out_done[q] = ev[5]
+        if timed:
+            marks.append(ev)
 
     for k in range(max(2, args.warmup // 2)):
         e2e_step(k)
@@ -510,12 +516,20 @@ def main():
     with ClockSampler(local) as e2e_clk:
         a.record(stream)
         for k in range(args.steps):
-            e2e_step(k)
+            e2e_step(k, timed=True)
         for e in out_done:
             stream.wait_event(e)
         b.record(stream)
         torch.cuda.synchronize()
     e2e_s = a.elapsed_time(b) / 1e3
+    up_ms = [m[0].elapsed_time(m[1]) for m in marks]
+    comp_ms = [m[2].elapsed_time(m[3]) for m in marks]
+    down_ms = [m[4].elapsed_time(m[5]) for m in marks]
+    # how long the compute stream sat idle between steps, and the fill and
+    # drain of the pipeline (first upload, last download)
+    gaps_ms = [marks[k][3].elapsed_time(marks[k + 1][2]) for k in range(len(marks) - 1)]
+    fill_ms = a.elapsed_time(marks[0][2]) if marks else 0.0
+    drain_ms = marks[-1][3].elapsed_time(b) if marks else 0.0
     if world > 1:
         t = torch.tensor([e2e_s], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -525,6 +539,10 @@ def main():
            "h2d_bytes_per_step": int(h_j.numel() + h_l.numel()),
            "d2h_bytes_per_step": int(h_spec.numel() * 4 + h_state.numel()),
            "pipelining": "two device buffer sets; copies of one step overlap the neighbouring step's compute",
+           "timeline_ms": {"upload": up_ms, "compute": comp_ms, "download": down_ms,
+                           "compute_idle_between_steps": gaps_ms, "fill": fill_ms, "drain": drain_ms,
+                           "h2d_gbs": [(h_j.numel() + h_l.numel()) / (u / 1e3) / 1e9 for u in up_ms],
+                           "d2h_gbs": [(h_spec.numel() * 4 + h_state.numel()) / (d / 1e3) / 1e9 for d in down_ms]},
            "clocks": e2e_clk.summary()}
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
