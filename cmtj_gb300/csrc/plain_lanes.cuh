@@ -88,11 +88,23 @@ __device__ __forceinline__ FieldOnly<V> field_only_load(const cmtj_layer_t &L, c
   return f;
 }
 
+static __device__ __forceinline__ C3 vsel(bool c, const C3 &a, const C3 &b) { return C3{c ? a.v : b.v}; }
+static __device__ __forceinline__ D3 vsel(bool c, const D3 &a, const D3 &b) { return c ? a : b; }
+
 // rhs()'s IEC term of a field-only layer (the CMTJ_ZERO_J2 form), which
-// depends only on the neighbours, frozen for an RK4 step.
+// depends only on the neighbours, frozen for an RK4 step.  one_nb: no lane
+// of the warp has two neighbours (its junctions have at most two layers, so
+// at least one neighbour of every lane is the zero vector of an edge).  Then
+// each lane forms its one term with its own operands, the same operations
+// as the branch it would take, and the warp runs one division instead of
+// both branches in turn.
 template <class V>
-__device__ __forceinline__ V field_only_iec(const FieldOnly<V> &f, const V &bottom, const V &top) {
+__device__ __forceinline__ V field_only_iec(const FieldOnly<V> &f, const V &bottom, const V &top, bool one_nb) {
   const bool zb = is_zero3(bottom), ztop = is_zero3(top);
+  if (one_nb) {
+    const V r = (vsel(zb, top, bottom) * (zb ? f.Jt : f.Jb)) / f.Mst;
+    return vsel(zb && ztop, V::zero(), r);
+  }
   if (!zb && !ztop) return (bottom * f.Jb) / f.Mst + (top * f.Jt) / f.Mst;
   if (!zb) return (bottom * f.Jb) / f.Mst;
   if (!ztop) return (top * f.Jt) / f.Mst;
@@ -269,7 +281,8 @@ __device__ __forceinline__ int lane_step_fused(const cmtj_layer_t &L, const Fuse
 // n layers step (1 under runSingleLayerSolver).  cur overrides the current
 // driver (stacks), hres the reserved interaction field (groups).  fo: RK4
 // only, the layer is field-only (FieldOnly), with constant drivers or, under
-// FDYN, time-dependent field and anisotropy drivers.
+// FDYN, time-dependent field and anisotropy drivers; edge_only: no junction
+// of the warp has three or more layers, so no lane has two neighbours.
 // Returns the first layer whose m became NaN (RK4: the layers above it
 // keep their start-of-step m, as when rk4_step throws), or -1.
 template <int SOLVER, class V, bool FDYN = false>
@@ -277,7 +290,7 @@ __device__ __forceinline__ int lane_step(const cmtj_layer_t &L, const cmtj_const
                                          SideT<V> &side, bool step, const LaneGeo &g, int n, uint32_t i, double t,
                                          double dt, const double *tables, bool energies,
                                          const cmtj_driver_t *cur, uint32_t dyn, const double *hres = nullptr,
-                                         const FieldOnly<V> *fo = nullptr) {
+                                         const FieldOnly<V> *fo = nullptr, bool edge_only = false) {
   // neighbours at the start of the step; zero beyond the stack's ends
   V below = shfl_vec(mag, g.below_src), above = shfl_vec(mag, g.above_src);
   if (g.l == 0) below = V::zero();
@@ -290,7 +303,7 @@ __device__ __forceinline__ int lane_step(const cmtj_layer_t &L, const cmtj_const
     if (step) {
       V k = V::zero(), acc = V::zero();
       if (fo) {
-        const V hiec = field_only_iec(*fo, below, above);
+        const V hiec = field_only_iec(*fo, below, above, edge_only);
 #pragma unroll
         for (int s = 0; s < 4; ++s) {
           const double ts = s == 0 ? t : (s == 3 ? t + dt : t + 0.5 * dt);

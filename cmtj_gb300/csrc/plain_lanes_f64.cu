@@ -86,6 +86,7 @@ __device__ __forceinline__ void run_lanes(const cmtj_junction_t *__restrict__ ju
   }
   FieldOnly<V> fo;
   if (FIELD) fo = field_only_load<V>(L, c);
+  const bool edge_only = !__any_sync(kWarpAll, n >= 3);
   Fused<V> fu;
   if (FUSED) fu = fused_load<V>(fo, dt);
   double *out = have ? log + (size_t)j * p.n_log * p.log_width : nullptr;
@@ -99,7 +100,7 @@ __device__ __forceinline__ void run_lanes(const cmtj_junction_t *__restrict__ ju
       first = lane_step_fused<V, DYN>(L, fu, mag, mine && run, g, n, i, t, dt, tables, dyn);
     else
       first = lane_step<SOLVER, V, DYN && FIELD>(L, c, mag, side, mine && run, g, n, i, t, dt, tables, energies,
-                                                 nullptr, dyn, nullptr, FIELD ? &fo : nullptr);
+                                                 nullptr, dyn, nullptr, FIELD ? &fo : nullptr, edge_only);
     if (first >= 0) {
       if (run) code = CMTJ_STATUS_NAN;
       run = false;
