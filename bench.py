@@ -81,7 +81,10 @@ def dist_info():
 
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed
-    region (every 200 ms)."""
+    region (every 200 ms).  Entering waits (at most 5 s) for the first
+    sample, so nvidia-smi's start-up (its first device query held up a
+    device-to-host copy by ~20 ms) falls before the timed region; the
+    summary covers the samples taken after that."""
 
     FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
@@ -91,6 +94,7 @@ class ClockSampler:
         self.index = index
         self.rows = []
         self.proc = None
+        self.mark = 0
 
     def __enter__(self):
         try:
@@ -99,6 +103,10 @@ class ClockSampler:
                  "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
+            t0 = time.perf_counter()
+            while not self.rows and self.proc.poll() is None and time.perf_counter() - t0 < 5.0:
+                time.sleep(0.01)
+            self.mark = len(self.rows)
         except OSError:
             self.proc = None
         return self
@@ -120,6 +128,8 @@ class ClockSampler:
     def summary(self):
         if not self.rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        if len(self.rows) > self.mark:
+            self.rows = self.rows[self.mark:]
         sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
         mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]

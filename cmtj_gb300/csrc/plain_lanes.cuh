@@ -10,6 +10,7 @@
 #pragma once
 #include "lane3.cuh"
 #include "plain_f64.cuh"
+#include "recip.cuh"
 
 namespace cmtjd {
 
@@ -61,8 +62,23 @@ template <class V>
 struct FieldOnly {
   V Hext, Hoe, Hdmi, Hres, anis;
   double K, Jb, Jt, Ms, Mst, ms_mu0, damping, conv, gyro;
+  Recip rMs, rMst;  // division by Ms and by Ms * thickness (recip.cuh)
   const double *demag;
 };
+
+// v / R.b componentwise, each quotient correctly rounded (recip.cuh).
+static __device__ __forceinline__ C3 vdiv(const C3 &a, const Recip &R) { return C3{div_by(a.v, R)}; }
+static __device__ __forceinline__ D3 vdiv(const D3 &a, const Recip &R) {
+  return d3(div_by(a.x, R), div_by(a.y, R), div_by(a.z, R));
+}
+// 6 split as recip_of(6.0) would: RN(1/6) and RN(1/6 - RN(1/6)).
+static __device__ __forceinline__ Recip recip_six() {
+  Recip R;
+  R.b = 6.0;
+  R.zh = 0x1.5555555555555p-3;
+  R.zl = 0x1.5555555555555p-57;
+  return R;
+}
 
 // The constants of a field-only layer whose driver slots are all constant
 // (each slot reads constantValue, as slot_at does with a zero slot mask).
@@ -80,6 +96,8 @@ __device__ __forceinline__ FieldOnly<V> field_only_load(const cmtj_layer_t &L, c
   f.Jt = L.drv[CMTJ_SLOT_IEC_TOP].constantValue;
   f.Ms = L.Ms;
   f.Mst = L.Ms * L.thickness;
+  f.rMs = recip_of(f.Ms);
+  f.rMst = recip_of(f.Mst);
   f.ms_mu0 = L.ms_over_mu0;
   f.damping = L.damping;
   f.conv = L.conv_term;
@@ -102,12 +120,12 @@ template <class V>
 __device__ __forceinline__ V field_only_iec(const FieldOnly<V> &f, const V &bottom, const V &top, bool one_nb) {
   const bool zb = is_zero3(bottom), ztop = is_zero3(top);
   if (one_nb) {
-    const V r = (vsel(zb, top, bottom) * (zb ? f.Jt : f.Jb)) / f.Mst;
+    const V r = vdiv(vsel(zb, top, bottom) * (zb ? f.Jt : f.Jb), f.rMst);
     return vsel(zb && ztop, V::zero(), r);
   }
-  if (!zb && !ztop) return (bottom * f.Jb) / f.Mst + (top * f.Jt) / f.Mst;
-  if (!zb) return (bottom * f.Jb) / f.Mst;
-  if (!ztop) return (top * f.Jt) / f.Mst;
+  if (!zb && !ztop) return vdiv(bottom * f.Jb, f.rMst) + vdiv(top * f.Jt, f.rMst);
+  if (!zb) return vdiv(bottom * f.Jb, f.rMst);
+  if (!ztop) return vdiv(top * f.Jt, f.rMst);
   return V::zero();
 }
 
@@ -126,7 +144,7 @@ __device__ __forceinline__ V rhs_field_only(const FieldOnly<V> &f, const cmtj_la
   const V Hres = DYN ? V::axial(L, CMTJ_SLOT_HRES, time, dc, dyn) : f.Hres;
   const double K = DYN ? slot_at(L, CMTJ_SLOT_ANIS, time, dc, dyn) : f.K;
   const V Hdemag = tensor_mul(m, f.demag, f.ms_mu0);
-  const V Hanis = f.anis * ((2 * K) * dot(f.anis, m) / f.Ms);
+  const V Hanis = f.anis * div_by((2 * K) * dot(f.anis, m), f.rMs);
   V H = Hext + Hanis;
   H = H + Hiec;
   H = H + Hoe + Hdmi - Hdemag;
@@ -322,7 +340,7 @@ __device__ __forceinline__ int lane_step(const cmtj_layer_t &L, const cmtj_const
           acc = s == 0 ? k : acc + (s == 3 ? k : k * 2.0);
         }
       }
-      next = normalized(mag + acc / 6.0);
+      next = normalized(mag + vdiv(acc, recip_six()));
       nan = x_is_nan(next);
     }
     const unsigned bad = __ballot_sync(kWarpAll, nan) & g.group;
