@@ -81,7 +81,7 @@ def dist_info():
 
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed
-    region (every 200 ms).  Entering waits (at most 5 s) for the first
+    region (every 100 ms).  Entering waits (at most 5 s) for the first
     sample, so nvidia-smi's start-up (its first device query held up a
     device-to-host copy by ~20 ms) falls before the timed region; the
     summary covers the samples taken after that."""
@@ -100,7 +100,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
             t0 = time.perf_counter()
