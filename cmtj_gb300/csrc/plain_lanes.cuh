@@ -64,7 +64,72 @@ struct FieldOnly {
   double K, Jb, Jt, Ms, Mst, ms_mu0, damping, conv, gyro;
   Recip rMs, rMst;  // division by Ms and by Ms * thickness (recip.cuh)
   const double *demag;
+  // the same on every lane of the warp (field_only_flags): every lane's
+  // demag rows have +-0 off the diagonal; every lane's Hoe / Hdmi / Hres
+  // slot is constant and +-0
+  bool diag, zoe, zdmi, zres;
 };
+
+static __device__ __forceinline__ unsigned long long dbits(double x) {
+  return (unsigned long long)__double_as_longlong(x);
+}
+
+// x + z for z = +-0 (rounding to nearest): x, except -0 + +0 = +0.  No
+// FP64 instruction.
+static __device__ __forceinline__ double add_zero(double x, double z) {
+  return (dbits(x) == 0x8000000000000000ull && dbits(z) == 0ull) ? 0.0 : x;
+}
+static __device__ __forceinline__ C3 add_zero(const C3 &a, const C3 &z) { return C3{add_zero(a.v, z.v)}; }
+static __device__ __forceinline__ D3 add_zero(const D3 &a, const D3 &z) {
+  return d3(add_zero(a.x, z.x), add_zero(a.y, z.y), add_zero(a.z, z.z));
+}
+
+// (r0 mx + r1 my) + r2 mz, as tensor_mul forms it, for a row whose entries
+// other than r[c] are +-0: the zero products change the diagonal product d
+// in no bit unless d is itself zero, and then the sum is a zero that is -0
+// only when all three products are -0.  An inf or NaN component takes the
+// full sum (row_full).  One FP64 instruction instead of five.
+// The full row sum, out of line: a predicated copy would still hold the
+// FP64 pipe for its five instructions on every call.
+static __device__ __noinline__ double row_full(const double *r, double mx, double my, double mz) {
+  return r[0] * mx + r[1] * my + r[2] * mz;
+}
+static __device__ __forceinline__ double diag_row(const double *r, int c, double mx, double my, double mz) {
+  const unsigned long long e = 0x7ff0000000000000ull;
+  const unsigned long long bx = dbits(mx), by = dbits(my), bz = dbits(mz);
+  if ((bx & e) == e || (by & e) == e || (bz & e) == e) return row_full(r, mx, my, mz);
+  const double d = r[c] * (c == 0 ? mx : (c == 1 ? my : mz));
+  if ((dbits(d) << 1) != 0ull) return d;
+  const unsigned long long neg = (dbits(r[0]) ^ bx) & (dbits(r[1]) ^ by) & (dbits(r[2]) ^ bz);
+  return (neg >> 63) ? -0.0 : 0.0;
+}
+static __device__ __forceinline__ C3 tensor_mul_diag(const C3 &m, const double *t, double ms_mu0) {
+  const double mx = quad_get(m.v, 0), my = quad_get(m.v, 1), mz = quad_get(m.v, 2);
+  const int c = quad_comp();
+  return C3{diag_row(t + 3 * c, c, mx, my, mz) * ms_mu0};
+}
+static __device__ __forceinline__ D3 tensor_mul_diag(const D3 &m, const double *t, double ms_mu0) {
+  return d3(diag_row(t, 0, m.x, m.y, m.z), diag_row(t + 3, 1, m.x, m.y, m.z), diag_row(t + 6, 2, m.x, m.y, m.z)) *
+         ms_mu0;
+}
+// The components the lane holds are +-0 (a warp vote over every lane then
+// covers every component of every layer).
+static __device__ __forceinline__ bool lane_zero(const C3 &a) { return (dbits(a.v) << 1) == 0ull; }
+static __device__ __forceinline__ bool lane_zero(const D3 &a) {
+  return ((dbits(a.x) | dbits(a.y) | dbits(a.z)) << 1) == 0ull;
+}
+// The lane's demag rows (C3: its component's row; D3: all three) have +-0
+// off the diagonal.
+static __device__ __forceinline__ bool offdiag_zero(const double *t, const C3 &) {
+  const int c = quad_comp();
+  bool z = true;
+  for (int i = 0; i < 3; ++i)
+    if (i != c) z = z && (dbits(t[3 * c + i]) << 1) == 0ull;
+  return z;
+}
+static __device__ __forceinline__ bool offdiag_zero(const double *t, const D3 &) {
+  return ((dbits(t[1]) | dbits(t[2]) | dbits(t[3]) | dbits(t[5]) | dbits(t[6]) | dbits(t[7])) << 1) == 0ull;
+}
 
 // v / R.b componentwise, each quotient correctly rounded (recip.cuh).
 static __device__ __forceinline__ C3 vdiv(const C3 &a, const Recip &R) { return C3{div_by(a.v, R)}; }
@@ -109,6 +174,16 @@ __device__ __forceinline__ FieldOnly<V> field_only_load(const cmtj_layer_t &L, c
 static __device__ __forceinline__ C3 vsel(bool c, const C3 &a, const C3 &b) { return C3{c ? a.v : b.v}; }
 static __device__ __forceinline__ D3 vsel(bool c, const D3 &a, const D3 &b) { return c ? a : b; }
 
+// The warp-uniform flags of FieldOnly.  Called by every lane of the warp;
+// dyn: the lane's time-dependent slots (0 when none may be).
+template <class V>
+__device__ __forceinline__ void field_only_flags(FieldOnly<V> &f, uint32_t dyn) {
+  f.diag = __all_sync(kWarpAll, offdiag_zero(f.demag, f.anis));
+  f.zoe = __all_sync(kWarpAll, lane_zero(f.Hoe) && !(dyn & (7u << CMTJ_SLOT_HOE)));
+  f.zdmi = __all_sync(kWarpAll, lane_zero(f.Hdmi) && !(dyn & (7u << CMTJ_SLOT_HDMI)));
+  f.zres = __all_sync(kWarpAll, lane_zero(f.Hres) && !(dyn & (7u << CMTJ_SLOT_HRES)));
+}
+
 // rhs()'s IEC term of a field-only layer (the CMTJ_ZERO_J2 form), which
 // depends only on the neighbours, frozen for an RK4 step.  one_nb: no lane
 // of the warp has two neighbours (its junctions have at most two layers, so
@@ -143,12 +218,22 @@ __device__ __forceinline__ V rhs_field_only(const FieldOnly<V> &f, const cmtj_la
   const V Hdmi = DYN ? V::axial(L, CMTJ_SLOT_HDMI, time, dc, dyn) : f.Hdmi;
   const V Hres = DYN ? V::axial(L, CMTJ_SLOT_HRES, time, dc, dyn) : f.Hres;
   const double K = DYN ? slot_at(L, CMTJ_SLOT_ANIS, time, dc, dyn) : f.K;
-  const V Hdemag = tensor_mul(m, f.demag, f.ms_mu0);
+  // A layer per lane (D3, large batches, bound by FP64 issue): a diagonal
+  // demag tensor takes one product per component, and a slot that is a
+  // constant +-0 on every lane of the warp is added without an FP64 add,
+  // both bit-exactly.  The quad layout (small batches, bound by the step's
+  // latency) ran 3 % slower with them, so it keeps the plain sums.
+  constexpr bool kExact0 = V::kLanes == 1;
+  const V Hdemag =
+      (kExact0 && f.diag) ? tensor_mul_diag(m, f.demag, f.ms_mu0) : tensor_mul(m, f.demag, f.ms_mu0);
   const V Hanis = f.anis * div_by((2 * K) * dot(f.anis, m), f.rMs);
   V H = Hext + Hanis;
   H = H + Hiec;
-  H = H + Hoe + Hdmi - Hdemag;
-  H = H + Hres;
+  // H + Hoe + Hdmi - Hdemag, then + Hres
+  H = (kExact0 && f.zoe) ? add_zero(H, Hoe) : H + Hoe;
+  H = (kExact0 && f.zdmi) ? add_zero(H, Hdmi) : H + Hdmi;
+  H = H - Hdemag;
+  H = (kExact0 && f.zres) ? add_zero(H, Hres) : H + Hres;
   if (side) {
     side->K = K;
     side->K2 = 0.0;

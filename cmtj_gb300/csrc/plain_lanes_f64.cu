@@ -85,7 +85,10 @@ __device__ __forceinline__ void run_lanes(const cmtj_junction_t *__restrict__ ju
     if (DYN) dyn = dynamic_slots(L);
   }
   FieldOnly<V> fo;
-  if (FIELD) fo = field_only_load<V>(L, c);
+  if constexpr (FIELD) {
+    fo = field_only_load<V>(L, c);
+    field_only_flags<V>(fo, dyn);
+  }
   const bool edge_only = !__any_sync(kWarpAll, n >= 3);
   Fused<V> fu;
   if (FUSED) fu = fused_load<V>(fo, dt);
