@@ -325,17 +325,29 @@ static __device__ __forceinline__ V alpha_sample(const cmtj_layer_t &L, uint32_t
   return v * L.alpha_scale;
 }
 
+// The thermal field's standard deviation at temperature temp
+// (getLangevinStochasticStandardDeviation, junction.hpp:1111-1120).
+static __device__ __forceinline__ double langevin_sigma(const cmtj_layer_t &L, const cmtj_constants_t &c,
+                                                        double temp) {
+  const double mainFactor = (2 * L.damping * c.kB * temp) / (L.Ms * L.cellVolume * c.gyro);
+  return sqrt(mainFactor);
+}
+
 // getStochasticLangevinVector (junction.hpp:1111-1128), plus the buffered
 // alpha noise where the layer has one: dW of the Euler-Heun and Heun
-// runners (junction.hpp:1726-1727, 1792-1793).
+// runners (junction.hpp:1726-1727, 1792-1793).  sigma_run: the lane's sigma
+// formed once for the run (langevin_sigma of its constant temperature; the
+// same value every step), or -1 to form it at this step (the test reads the
+// sign bit: no FP64 compare).
 template <class V = D3>
 static __device__ __forceinline__ V langevin(const cmtj_layer_t &L, const cmtj_constants_t &c, double time,
-                                       uint32_t i, const DriverCtx &dc, uint32_t dyn = 0xffffffffu) {
+                                       uint32_t i, const DriverCtx &dc, uint32_t dyn = 0xffffffffu,
+                                       double sigma_run = -1.0) {
   V dW = V::zero();
   if (L.temperatureSet) {
-    const double temp = slot_at(L, CMTJ_SLOT_TEMPERATURE, time, dc, dyn);
-    const double mainFactor = (2 * L.damping * c.kB * temp) / (L.Ms * L.cellVolume * c.gyro);
-    const double sigma = sqrt(mainFactor);
+    const double sigma = (__double_as_longlong(sigma_run) >= 0)
+                             ? sigma_run
+                             : langevin_sigma(L, c, slot_at(L, CMTJ_SLOT_TEMPERATURE, time, dc, dyn));
     double g0, g1, g2;
     cmtj_gaussian3_f64(L.seed_lo, L.seed_hi, L.noise_step + i, g0, g1, g2);
     dW = V::make(g0, g1, g2) * sigma;

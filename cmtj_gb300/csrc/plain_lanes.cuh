@@ -385,7 +385,8 @@ __device__ __forceinline__ int lane_step_fused(const cmtj_layer_t &L, const Fuse
 // driver (stacks), hres the reserved interaction field (groups).  fo: RK4
 // only, the layer is field-only (FieldOnly), with constant drivers or, under
 // FDYN, time-dependent field and anisotropy drivers; edge_only: no junction
-// of the warp has three or more layers, so no lane has two neighbours.
+// of the warp has three or more layers, so no lane has two neighbours;
+// sigma_run: the lane's thermal sigma for the whole run (langevin), or -1.
 // Returns the first layer whose m became NaN (RK4: the layers above it
 // keep their start-of-step m, as when rk4_step throws), or -1.
 template <int SOLVER, class V, bool FDYN = false>
@@ -393,12 +394,13 @@ __device__ __forceinline__ int lane_step(const cmtj_layer_t &L, const cmtj_const
                                          SideT<V> &side, bool step, const LaneGeo &g, int n, uint32_t i, double t,
                                          double dt, const double *tables, bool energies,
                                          const cmtj_driver_t *cur, uint32_t dyn, const double *hres = nullptr,
-                                         const FieldOnly<V> *fo = nullptr, bool edge_only = false) {
+                                         const FieldOnly<V> *fo = nullptr, bool edge_only = false,
+                                         double sigma_run = -1.0) {
   // neighbours at the start of the step; zero beyond the stack's ends
   V below = shfl_vec(mag, g.below_src), above = shfl_vec(mag, g.above_src);
   if (g.l == 0) below = V::zero();
   if (g.l >= n - 1) above = V::zero();
-  if (SOLVER == CMTJ_RK4) {
+  if constexpr (SOLVER == CMTJ_RK4) {
     // Layer::rk4_step (1017-1041); neighbours frozen for all four stages
     // (runMultiLayerSolver, 1680-1707)
     V next = mag;
@@ -435,11 +437,11 @@ __device__ __forceinline__ int lane_step(const cmtj_layer_t &L, const cmtj_const
       return first;
     }
     if (step) mag = next;
-  } else if (SOLVER == CMTJ_EULER_HEUN) {
+  } else if constexpr (SOLVER == CMTJ_EULER_HEUN) {
     // eulerHeunSolverStep (1709-1754)
     if (step) {
       const DriverCtx d0 = {tables, i, 0};
-      const V dW = langevin<V>(L, c, t, i, d0, dyn);
+      const V dW = langevin<V>(L, c, t, i, d0, dyn, sigma_run);
       const V f = rhs(L, c, t, mag, below, above, d0, energies ? &side : nullptr, cur, dyn, hres);
       const V gt = stoch_torque(L, c, mag, dW);
       const V mNext = mag + gt * sqrt(dt);
@@ -453,7 +455,7 @@ __device__ __forceinline__ int lane_step(const cmtj_layer_t &L, const cmtj_const
     if (step) {
       const DriverCtx d0 = {tables, i, 0};
       fn = rhs(L, c, t, mag, below, above, d0, nullptr, cur, dyn, hres);
-      dW = langevin<V>(L, c, t, i, d0, dyn);
+      dW = langevin<V>(L, c, t, i, d0, dyn, sigma_run);
       gn = stoch_torque(L, c, mag, dW);
       pred = mag + fn * dt + gn * sqrt(dt);
     }

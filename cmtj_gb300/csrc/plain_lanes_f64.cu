@@ -90,6 +90,12 @@ __device__ __forceinline__ void run_lanes(const cmtj_junction_t *__restrict__ ju
     field_only_flags<V>(fo, dyn);
   }
   const bool edge_only = !__any_sync(kWarpAll, n >= 3);
+  // a constant temperature gives the same thermal sigma at every step
+  double sigma_run = -1.0;
+  if constexpr (SOLVER != CMTJ_RK4) {
+    if (mine && L.temperatureSet && !(dyn & (1u << CMTJ_SLOT_TEMPERATURE)))
+      sigma_run = langevin_sigma(L, c, L.drv[CMTJ_SLOT_TEMPERATURE].constantValue);
+  }
   Fused<V> fu;
   if (FUSED) fu = fused_load<V>(fo, dt);
   double *out = have ? log + (size_t)j * p.n_log * p.log_width : nullptr;
@@ -101,9 +107,12 @@ __device__ __forceinline__ void run_lanes(const cmtj_junction_t *__restrict__ ju
     int first;
     if constexpr (FUSED)
       first = lane_step_fused<V, DYN>(L, fu, mag, mine && run, g, n, i, t, dt, tables, dyn);
-    else
+    else if constexpr (SOLVER == CMTJ_RK4)
       first = lane_step<SOLVER, V, DYN && FIELD>(L, c, mag, side, mine && run, g, n, i, t, dt, tables, energies,
                                                  nullptr, dyn, nullptr, FIELD ? &fo : nullptr, edge_only);
+    else
+      first = lane_step<SOLVER, V, false>(L, c, mag, side, mine && run, g, n, i, t, dt, tables, energies, nullptr,
+                                          dyn, nullptr, nullptr, false, sigma_run);
     if (first >= 0) {
       if (run) code = CMTJ_STATUS_NAN;
       run = false;
