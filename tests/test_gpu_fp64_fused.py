@@ -164,3 +164,17 @@ def test_fused_choice_is_per_warp(gpu_lib):
         la, lb = a.getLogArrays(), b.getLogArrays()
         dms.append(max(float(np.max(np.abs(la[k] - lb[k]))) for k in KEYS))
     assert 0.0 < max(dms) <= TOL_M, dms
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("arithmetic", ["reference", "fused"])
+def test_blow_up_raises_like_the_reference(gpu_lib, arithmetic):
+    """A field large enough to overflow the torque makes m NaN within the
+    first steps.  Either arithmetic stops the junction there and raises the
+    RuntimeError of the reference's rk4_step ("NAN magnetisation"), keeping
+    the rows logged before it."""
+    j = _rh(1, 2e-12)[0]
+    j.setLayerExternalFieldDriver("all", cmtj_gb300.AxialDriver(1e308, 0, 0))
+    with pytest.raises(RuntimeError, match="NAN magnetisation"):
+        _run([j], 2e-12, arithmetic)
+    assert len(j.getLogArrays().get("time", [])) < 20
