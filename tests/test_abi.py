@@ -96,3 +96,28 @@ def test_f64_rejects_unknown_arithmetic(lib):
     with pytest.raises(ValueError, match="arithmetic"):
         _lower.make_params(plan, 0, False, 10, 2, "fast")
     assert int(_lower.make_params(plan, 0, False, 10, 2, "fused")["arithmetic"][0]) == _abi.ARITH_FUSED
+
+
+def test_empty_inputs_return_ok_before_touching_buffers(lib):
+    """Zero junctions, stacks, groups, rows or buffers: each entry point
+    checks its arguments and returns CMTJ_OK before it reads a pointer (no
+    GPU needed)."""
+    import numpy as np
+    from cmtj_gb300 import _abi, batch
+    p = np.zeros(1, dtype=_abi.SIM_PARAMS_DTYPE)
+    p["solver"] = 1  # RK4
+    p["write_every"] = 1
+    P = p.ctypes.data
+    assert lib.cmtj_run_simulation_f64(None, 0, None, None, P, None, None, None) == _abi.CMTJ_OK
+    assert lib.cmtj_run_stack_f64(None, 0, None, None, None, None, None, P, None, None, 5, 2, None, None) == \
+        _abi.CMTJ_OK
+    assert lib.cmtj_run_group_f64(None, 0, None, None, None, None, None, P, None, 1, None, None) == _abi.CMTJ_OK
+    fp = np.zeros(1, dtype=batch.F32_PARAMS_DTYPE)
+    assert lib.cmtj_batch_run_f32(None, None, None, None, 0, 2, 0, fp.ctypes.data, None, None, 0, None) == \
+        _abi.CMTJ_OK
+    assert lib.cmtj_spectrum_f32(None, 4096, 0, 4096, 4096, 1, 100, None, None) == _abi.CMTJ_OK
+    assert lib.cmtj_alpha_noise_f32(None, 0, 1000, None, None, None, 0, None) == _abi.CMTJ_OK
+    # limits: an FFT above 8192 points and a layer count above the FP32 form's
+    assert lib.cmtj_spectrum_f32(None, 16384, 1, 16384, 16384, 1, 100, None, None) == _abi.CMTJ_ERR_ARG
+    assert lib.cmtj_batch_run_f32(None, None, None, None, 1, 5, 0, fp.ctypes.data, None, None, 0, None) == \
+        _abi.CMTJ_ERR_ARG

@@ -339,3 +339,16 @@ def test_shared_unset_driver_is_never_changed():
     _lower.lower([j, cmtj.Junction([j2])], _lower.plan_run(1e-12, 1e-13, 1e-13), cmtj.SolverMode.RK4, True)
     assert snapshot(core._UNSET_DRIVER) == fresh
     assert j.layers[0].scalar["anis2"] is core._UNSET_DRIVER
+
+
+def test_layer_count_limits_raise_before_any_launch():
+    """Nine layers exceed the FP64 form's 8 (CMTJ_MAX_LAYERS), five the FP32
+    form's 4: both raise ValueError at lowering, before a launch."""
+    from cmtj_gb300 import SolverMode, _lower, batch, engine
+    nine = Junction([_layer("l%d" % k) for k in range(9)])
+    plan = engine.plan_run(1e-12, 1e-13, 1e-13)
+    with pytest.raises(ValueError, match="at most 8 layers"):
+        _lower.lower([nine], plan, SolverMode.RK4, False)
+    five = Junction([_layer("l%d" % k) for k in range(5)])
+    with pytest.raises(ValueError, match="1-4 layers"):
+        batch.BatchSpec.from_junctions([five])
