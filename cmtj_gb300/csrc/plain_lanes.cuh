@@ -84,16 +84,17 @@ static __device__ __forceinline__ D3 add_zero(const D3 &a, const D3 &z) {
   return d3(add_zero(a.x, z.x), add_zero(a.y, z.y), add_zero(a.z, z.z));
 }
 
+// A tensor row times m as tensor_mul forms it, out of line: a predicated
+// inline copy would still hold the FP64 pipe for its five instructions on
+// every call of diag_row.
+static __device__ __noinline__ double row_full(const double *r, double mx, double my, double mz) {
+  return r[0] * mx + r[1] * my + r[2] * mz;
+}
 // (r0 mx + r1 my) + r2 mz, as tensor_mul forms it, for a row whose entries
 // other than r[c] are +-0: the zero products change the diagonal product d
 // in no bit unless d is itself zero, and then the sum is a zero that is -0
 // only when all three products are -0.  An inf or NaN component takes the
 // full sum (row_full).  One FP64 instruction instead of five.
-// The full row sum, out of line: a predicated copy would still hold the
-// FP64 pipe for its five instructions on every call.
-static __device__ __noinline__ double row_full(const double *r, double mx, double my, double mz) {
-  return r[0] * mx + r[1] * my + r[2] * mz;
-}
 static __device__ __forceinline__ double diag_row(const double *r, int c, double mx, double my, double mz) {
   const unsigned long long e = 0x7ff0000000000000ull;
   const unsigned long long bx = dbits(mx), by = dbits(my), bz = dbits(mz);
