@@ -211,15 +211,17 @@ def test_spectrum_kernel_matches_numpy(gpu_lib, nfft):
     rows, length, stride = 37, nfft + 13, nfft + 20
     x = rng.standard_normal((rows, stride)).astype(np.float32) + 0.5
     d_x = t.from_numpy(x.ravel().copy()).cuda()
-    lo, hi = 0, nfft // 2 + 1
-    out = t.empty((rows, hi - lo), dtype=t.float32, device="cuda")
-    rc = lib.cmtj_spectrum_f32(engine.ptr(d_x), stride, rows, length, nfft, lo, hi, engine.ptr(out),
-                               engine.stream_ptr())
-    _abi.check(rc, lib)
-    got = out.cpu().numpy()
-    ref = np.abs(np.fft.fft(x[:, length - nfft:length].astype(np.float64), axis=1))[:, lo:hi]
+    full = np.abs(np.fft.fft(x[:, length - nfft:length].astype(np.float64), axis=1))
     tol = 4 * np.finfo(np.float32).eps * np.log2(nfft) * np.linalg.norm(x[:, length - nfft:length], axis=1)
-    assert np.all(np.max(np.abs(got - ref), axis=1) <= tol)
+    # the lower half with bin n/2, and a window across n/2 to the last bin
+    # (|X[k]| = |X[n-k]| above n/2)
+    for lo, hi in ((0, nfft // 2 + 1), (nfft // 2 - 5, nfft)):
+        out = t.empty((rows, hi - lo), dtype=t.float32, device="cuda")
+        rc = lib.cmtj_spectrum_f32(engine.ptr(d_x), stride, rows, length, nfft, lo, hi, engine.ptr(out),
+                                   engine.stream_ptr())
+        _abi.check(rc, lib)
+        got = out.cpu().numpy()
+        assert np.all(np.max(np.abs(got - full[:, lo:hi]), axis=1) <= tol), (lo, hi)
 
 
 @pytest.mark.gpu
