@@ -1157,13 +1157,20 @@ def other_workloads():
     torch.cuda.synchronize()
     gen_s = a.elapsed_time(b) / 1e3
     del bufs
-    js = []
-    for k in range(1024):
-        j, _ = thermal_cases.pbit_sweep_junction(cm, 1e11, 1e-8)
-        j.layers[0].setAlphaNoise(1.0, 1.0, 0.05, cm.Axis.all)
-        j.layers[0].noise_seed = 5000 + k
-        js.append(j)
+    def alpha_junctions():
+        js = []
+        for k in range(1024):
+            j, _ = thermal_cases.pbit_sweep_junction(cm, 1e11, 1e-8)
+            j.layers[0].setAlphaNoise(1.0, 1.0, 0.05, cm.Axis.all)
+            j.layers[0].noise_seed = 5000 + k
+            js.append(j)
+        return js
+
     plan = engine.plan_run(1e-8, DT, 1e-9)
+    # an untimed run of the same batch first: it makes the run-time
+    # autotuner's lane-layout trials for this batch shape, once
+    engine.run_junctions(alpha_junctions(), plan, cm.SolverMode.EulerHeun)
+    js = alpha_junctions()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     engine.run_junctions(js, plan, cm.SolverMode.EulerHeun)
