@@ -611,6 +611,8 @@ class BatchRun:
                 idx = idx[np.argsort(-lowered.n_steps[idx], kind="stable")]
                 self.parts.append((nl, engine.to_device(idx.astype(np.int32)), int(idx.size), int(v)))
                 self.part_rows.append(idx)
+        self.launch_order = submission_order(
+            [(nl, int(lowered.n_steps[rows[0]])) for (nl, _, _, _), rows in zip(self.parts, self.part_rows)])
         # run-time launch choices per partition (cmtj_gb300.autotune):
         # (key, {"bound", "tile", ...}); None: the fixed defaults
         self.tuning = [None] * len(self.parts)
@@ -646,7 +648,10 @@ class BatchRun:
         logs stay 16-byte aligned.  Partitions (layer count x kernel
         variant) run concurrently, each on its own stream with its own work
         ticket, so a small partition's long junctions overlap the others
-        instead of adding their tail; `stream` waits for all of them.  Each
+        instead of adding their tail; `stream` waits for all of them.  They
+        are submitted in submission_order (longest critical path first), so
+        that the CTAs of the partition holding the longest junction reach
+        the SMs before the others fill them.  Each
         partition's log tile and resident-CTA bound come from the run-time
         autotuner (cmtj_gb300.autotune), which times them once per kind of
         partition; the choices change no result."""
@@ -667,8 +672,8 @@ class BatchRun:
         if multi:
             start.record(main)
         ends = []
-        for q in range(len(self.parts)):
-            s = self._streams[q % len(self._streams)] if multi else main
+        for i, q in enumerate(self.launch_order):
+            s = self._streams[i % len(self._streams)] if multi else main
             if multi:
                 s.wait_event(start)
             tile, code = choices[q]
@@ -752,6 +757,26 @@ class BatchRun:
         s, c = int(self.samples[k]), int(self.log_chans[k])
         a = log[self.log_starts[k]: self.log_starts[k] + self.log_pad[k] * c].reshape(-1, c)
         return a[:s]
+
+
+def submission_order(parts):
+    """Order in which launch() submits partitions, given (layer count,
+    longest junction's steps) per partition: longest critical path first.
+
+    One thread runs a junction from start to end, so a sweep can end no
+    sooner than its longest junction takes, at the speed one thread reaches
+    among the warps it shares an SM with.  The block scheduler places the
+    CTAs of concurrent launches roughly in submission order, and a mixed
+    sweep holds more CTAs than fit on the GPU at once (the 3- and 4-layer
+    kernels use up to 255 registers a thread), so a partition submitted
+    last waits for SM room that the others free only as their queues run
+    dry.  A thread's step costs about one unit per layer pair (the 1-layer
+    kernel: one unit), so the key is steps x ceil(layers / 2), ties going to
+    more layers, then to the earlier partition."""
+    def cost(q):
+        nl, steps = parts[q]
+        return (-int(steps) * ((int(nl) + 1) // 2), -int(nl), q)
+    return sorted(range(len(parts)), key=cost)
 
 
 def reduction_samples(n_steps, win_start, red_every):

@@ -245,6 +245,22 @@ def test_reduction_sample_counts():
         assert got.tolist() == want
 
 
+def test_partitions_submit_longest_critical_path_first():
+    from cmtj_gb300 import batch
+    # (layers, longest junction's steps) in the order partitions are built
+    parts = [(1, 500_000), (1, 400_000), (2, 500_000), (3, 200_000), (3, 500_000), (4, 500_000), (4, 100_000)]
+    order = batch.submission_order(parts)
+    assert sorted(order) == list(range(len(parts)))
+    # 4 layers at 500k steps first (2 pairs, ties go to more layers), then
+    # the 3-layer one; 1 and 2 layers at 500k cost one unit a step
+    assert order[:2] == [5, 4]
+    assert order[2:4] == [2, 0]
+    costs = [parts[q][1] * ((parts[q][0] + 1) // 2) for q in order]
+    assert costs == sorted(costs, reverse=True)
+    assert batch.submission_order([]) == []
+    assert batch.submission_order([(2, 10)]) == [0]
+
+
 def test_layer_records_mark_identically_zero_terms():
     """The FP64 solver skips field terms the host marks identically zero
     (CMTJ_ZERO_*); the mask must be set exactly when the term is zero, and
