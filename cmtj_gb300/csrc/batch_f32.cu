@@ -42,6 +42,16 @@ const CmtjBatchVariant *pick(int L, int solver, int features, int need_nw, int m
 
 inline int variant_code(const CmtjBatchVariant *v) { return v->feat | (v->nw << 16) | (v->mb << 24); }
 
+// Shared-memory words per thread of the cached reduction constants.
+int red_words(int L) {
+  switch (L) {
+  case 1: return cmtjf::red_words<1>();
+  case 2: return cmtjf::red_words<2>();
+  case 3: return cmtjf::red_words<3>();
+  default: return cmtjf::red_words<4>();
+  }
+}
+
 }  // namespace
 
 extern "C" int cmtj_batch_variant_f32(int32_t n_layers, int32_t solver, int32_t features) {
@@ -112,10 +122,15 @@ extern "C" int cmtj_batch_run_f32(const cmtj_f32_junction_t *d_junctions, const 
                    p->solver, features);
     return CMTJ_ERR_ARG;
   }
-  const int threads = 128;
-  // per thread: its log tile, then (weighted reduction) a compensated sum pair
-  const size_t smem =
-      (size_t)threads * ((channels > 0 ? p->log_tile * channels : 1) + (p->red_weights ? 2 : 0)) * sizeof(float);
+  const int threads = cmtjf::kRedStride;
+  // per thread: its log tile, then (weighted reduction) a compensated sum
+  // pair, then (any reduction) the cached reduction constants
+  const size_t smem = (size_t)threads *
+                      ((channels > 0 ? p->log_tile * channels : 1) + (p->red_weights ? 2 : 0) +
+                       (p->red_every ? red_words(n_layers) : 0)) *
+                      sizeof(float);
+  if (smem > 48u * 1024u)
+    CMTJ_CUDA_TRY(cudaFuncSetAttribute(v->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int blocks = grid_blocks;
   if (blocks <= 0) {
     int dev = 0, sms = 0, per_sm = 0;

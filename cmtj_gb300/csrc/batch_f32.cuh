@@ -687,6 +687,73 @@ __device__ __forceinline__ float resistance(const cmtj_f32_junction_t *J, const 
   return 1.f / acc;
 }
 
+// Constants of the on-device reductions, cached per thread in shared memory
+// when its junction is loaded, word k of thread t at rk[k * kRedStride + t]:
+// a warp reads 32 consecutive words, one wavefront.  Read from the junction
+// records instead (536 B apart, in length order) every load of a warp
+// gathers 32 cache lines, and with R reduced every step those gathers kept
+// the L1 busy.  Words: 0 MR mode; CLASSIC 1 (Rap - Rp) / 2, 2 Rp, 3-5 the
+// layer-0 reference (1 layer); SERIES / STRIP 1 + 3l, 2 + 3l, 3 + 3l
+// AMR_X, SMR_X, Rx0 of layer l; then vsd_ph0, vsd_dph (low, high words)
+// and red_total.  Integers are stored as their bits.
+constexpr int kRedStride = 128;  // threads per CTA of k_batch
+template <int L> __host__ __device__ constexpr int red_mr_words() { return 1 + (3 * L > 5 ? 3 * L : 5); }
+template <int L> __host__ __device__ constexpr int red_words() { return red_mr_words<L>() + 5; }
+
+template <int L>
+__device__ __forceinline__ void red_cache(float *rk, const cmtj_f32_junction_t &J, const float *ref0) {
+  const int mr = J.mr_mode;
+  rk[0] = __int_as_float(mr);
+  if (mr == CMTJ_MR_CLASSIC) {
+    rk[1 * kRedStride] = (J.Rap - J.Rp) * 0.5f;
+    rk[2 * kRedStride] = J.Rp;
+    if (L == 1) {
+      rk[3 * kRedStride] = ref0[0];
+      rk[4 * kRedStride] = ref0[1];
+      rk[5 * kRedStride] = ref0[2];
+    }
+  } else {
+#pragma unroll
+    for (int l = 0; l < L; ++l) {
+      rk[(1 + 3 * l) * kRedStride] = J.AMR_X[l];
+      rk[(2 + 3 * l) * kRedStride] = J.SMR_X[l];
+      rk[(3 + 3 * l) * kRedStride] = J.Rx0[l];
+    }
+  }
+  constexpr int b = red_mr_words<L>();
+  rk[b * kRedStride] = __uint_as_float((uint32_t)J.vsd_ph0);
+  rk[(b + 1) * kRedStride] = __uint_as_float((uint32_t)(J.vsd_ph0 >> 32));
+  rk[(b + 2) * kRedStride] = __uint_as_float((uint32_t)J.vsd_dph);
+  rk[(b + 3) * kRedStride] = __uint_as_float((uint32_t)(J.vsd_dph >> 32));
+  rk[(b + 4) * kRedStride] = __uint_as_float(J.red_total);
+}
+__device__ __forceinline__ uint64_t red_u64(const float *rk, int k) {
+  return ((uint64_t)__float_as_uint(rk[(k + 1) * kRedStride]) << 32) | __float_as_uint(rk[k * kRedStride]);
+}
+
+// resistance() on the cached constants: the same operations in the same
+// order, so the same bits.
+template <int L> __device__ __forceinline__ float resistance_cached(const float *rk, const F3 *m) {
+  const int mr = __float_as_int(rk[0]);
+  if (mr == CMTJ_MR_CLASSIC) {
+    const F3 other = L > 1 ? m[L > 1 ? 1 : 0] : f3(rk[3 * kRedStride], rk[4 * kRedStride], rk[5 * kRedStride]);
+    return fmaf(rk[1 * kRedStride], 1.f - dot(m[0], other), rk[2 * kRedStride]);
+  }
+  float acc = 0.f;
+  if (mr == CMTJ_MR_SERIES) {
+#pragma unroll
+    for (int l = 0; l < L; ++l)
+      acc += fmaf(rk[(1 + 3 * l) * kRedStride], m[l].x * m[l].x,
+                  fmaf(rk[(2 + 3 * l) * kRedStride], m[l].y * m[l].y, rk[(3 + 3 * l) * kRedStride]));
+    return acc;
+  }
+#pragma unroll
+  for (int l = 0; l < L; ++l)
+    acc += 1.f / fmaf(rk[(1 + 3 * l) * kRedStride], m[l].x * m[l].x,
+                      fmaf(rk[(2 + 3 * l) * kRedStride], m[l].y * m[l].y, rk[(3 + 3 * l) * kRedStride]));
+  return 1.f / acc;
+}
+
 template <int L> __device__ __forceinline__ int log_channels(int mode) {
   return mode == CMTJ_LOG_M ? 3 * L : (mode == CMTJ_LOG_NONE ? 0 : 1);
 }
@@ -741,10 +808,13 @@ __global__ void __launch_bounds__(128, (MB > 0 ? MB : min_blocks<L, SOLVER, FEAT
   const int C = log_channels<L>(p.log_mode);
   const uint32_t T = p.log_tile;
   // shared memory per thread: its log tile; after all tiles, when
-  // p.red_weights is set, the (sum, compensation) pair of the weighted sum
+  // p.red_weights is set, the (sum, compensation) pair of the weighted sum;
+  // then, when reducing, the reduction constants (red_cache, one column per
+  // thread)
   const uint32_t tile_floats = C > 0 ? T * (uint32_t)C : 1u;
   float *tile = smem + (size_t)threadIdx.x * tile_floats;
   float *wsum = smem + (size_t)blockDim.x * tile_floats + 2u * threadIdx.x;
+  float *rk = smem + (size_t)blockDim.x * (tile_floats + (p.red_weights ? 2u : 0u)) + threadIdx.x;
 
   // Packed two-layer RK4 for the variants with only constant / wave fields,
   // uniaxial anisotropy, diagonal demag and bilinear IEC.
@@ -837,6 +907,7 @@ __global__ void __launch_bounds__(128, (MB > 0 ? MB : min_blocks<L, SOLVER, FEAT
             win = J.win_start;
             Jp = &J;
             ref0 = A.Ly[J.layer_offset].ref;
+            if (p.red_every) red_cache<L>(rk, J, ref0);
             tcount = 0;
             logrow = A.log + (size_t)J.log_offset * 4u;
             // next sampling steps: log at step % log_every == 0, reductions
@@ -996,15 +1067,16 @@ __global__ void __launch_bounds__(128, (MB > 0 ? MB : min_blocks<L, SOLVER, FEAT
       // ---- reductions: R and I(t) R(t) from win_start on
       if (last == next_red) {
         next_red = (next_red > 0xffffffffu - p.red_every) ? 0xffffffffu : next_red + p.red_every;
-        const float R = resistance<L>(Jp, ref0, m);
+        constexpr int b = red_mr_words<L>();
+        const float R = resistance_cached<L>(rk, m);
         kadd(rs, rc, R);
-        const uint64_t vdph = Jp->vsd_dph;
+        const uint64_t vdph = red_u64(rk, b + 2);
         if (vdph) {
-          const uint64_t ph = Jp->vsd_ph0 + (uint64_t)last * vdph;
+          const uint64_t ph = red_u64(rk, b) + (uint64_t)last * vdph;
           const float I = sin2pi_phase(ph);
           kadd(vs, vc, I * R);
           if (p.red_weights) {
-            const uint32_t tot = Jp->red_total;
+            const uint32_t tot = __float_as_uint(rk[(b + 4) * kRedStride]);
             const float w = __ldg(p.red_weights + (tot > n_red ? tot - 1u - n_red : 0u));
             float ws = wsum[0], wc = wsum[1];
             kadd(ws, wc, w * (I * R));
