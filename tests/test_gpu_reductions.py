@@ -252,3 +252,46 @@ def test_windowed_mean_r_matches_fp64(gpu_lib):
         assert abs(r_all - r64) > 5.0, (fields[k], r_all, r64)
         tol = _mean_r_tolerance(100.0, r64)
         assert abs(r32[k] - r64) <= tol, (fields[k], r32[k], r64, tol)
+
+
+@pytest.mark.gpu
+def test_largest_shared_memory_layout_keeps_logs_and_reductions(gpu_lib):
+    """4-layer spin-diode junctions with every layer's m logged every step
+    in 8-sample tiles (96 floats per thread), the Butterworth-weighted sum
+    and the cached reduction constants: 59 KB of shared memory per CTA,
+    above the 48 KB a launch gets without opting in.  Logging leaves the
+    reductions bit for bit as a run without a log gives them, and reducing
+    leaves the log bit for bit as a run without reductions gives it."""
+    spec, ns = sweeps.vsd_config(n_f=4, n_h=64, dt=DT, t_min=1e-10, t_max=2e-10)
+    keep = np.nonzero(spec.n_layers == 4)[0]
+    spec, ns = spec.take(keep), ns[keep]
+    rows = batch.BatchRun(batch.lower(spec, DT, ns), DT, cm.SolverMode.RK4).part_rows[0]  # one kernel variant
+    spec, ns = spec.take(rows), ns[rows]
+    low = batch.lower(spec, DT, ns)
+    w = batch.lowpass_step_response(int(ns.max()), 1 / DT)
+    tile = 8
+    assert 128 * (tile * 12 + 2 + 18) * 4 > 48 * 1024
+
+    def run(logged, reduced):
+        mode = batch.LOG_M if logged else batch.LOG_NONE
+        kw = dict(red_every=1, red_weights=w) if reduced else {}
+        r = batch.BatchRun(low, DT, cm.SolverMode.RK4, mode, 1 if logged else 0, **kw)
+        assert len(r.parts) == 1
+        code = r.parts[0][3]
+        r._launch_part(0, None, engine.torch().cuda.current_stream(), tile if logged else 0, code)
+        st = r.state()
+        assert np.all(st["status"] == 0) and np.all(st["step"] == ns)
+        log = r.d_log.cpu().numpy()
+        samples = [r.log_of(k, log).copy() for k in range(r.n)] if logged else None
+        return st, samples
+
+    both, log_both = run(True, True)
+    red_only, _ = run(False, True)
+    log_only, log_alone = run(True, False)
+    for f in ("m", "n_red", "r_sum", "r_c", "v_sum", "v_c", "vw_sum", "vw_c"):
+        assert both[f].tobytes() == red_only[f].tobytes(), f
+    assert np.all(both["n_red"] == ns) and np.all(np.abs(both["v_sum"]) > 0)
+    assert both["m"].tobytes() == log_only["m"].tobytes()
+    assert np.array_equal(both["n_logged"], log_only["n_logged"]) and np.all(both["n_logged"] == ns)
+    for a, b in zip(log_both, log_alone):
+        assert a.shape == (a.shape[0], 12) and a.tobytes() == b.tobytes()
